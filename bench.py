@@ -1,0 +1,473 @@
+#!/usr/bin/env python
+"""Benchmark of the all-pairs hot path on GB300.
+
+Headline workload (the configuration the metric is quoted on): gpuCor
+pearson, cor(x) of x = 4096 observations x 20000 variables float32, values
+lognormal(mu=5, sigma=1) plus per-column offsets uniform in [0, 1e3].  One
+step = one full gt_pmcc_device call (FP64 column statistics, split-bf16
+tcgen05 Gram contraction, fused epilogue writing coefficients, t-scores and
+pair counts for all 20000^2 entries).  value = entries of the returned matrix
+per second.  The same line also carries the plain FP32 CUDA-core path and the
+3-way split on the same workload, the Euclidean precision workload (100000
+points x 128 from 1000 clusters, sd 1e-3, 5% exact duplicates, R `dist`
+layout), the max error against the FP64 oracle on sampled rows, the
+end-to-end number through the host C ABI (pinned host buffers, copies inside
+the timed region), the roofline of the Gram kernel, clocks and a CPU
+baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs an independent replica (the path is computed
+per GPU, no collective); value sums the ranks' entries over the slowest rank's
+time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Pearson/Euclid entries/s, split-BF16 TC vs FP32 at max rel err ≤1e-6 vs FP64"
+N_OBS, N_VARS = 4096, 20000
+E_POINTS, E_DIM, E_CLUSTERS, E_SD, E_DUP = 100_000, 128, 1000, 1e-3, 0.05
+SAMPLE_ROWS = 48
+
+
+# ----------------------------------------------------------------------------- helpers
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Ranks:
+    def __init__(self):
+        self.world, self.rank, self.local = dist_env()
+        self.dist = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("nccl")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling while the timed regions run."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            out["reasons"] = ["nvidia-smi unavailable"]
+            return out
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return out
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v == "Active"})
+        load = [r for r in rows if r[2] > 250.0] or rows
+        out.update(sm_mhz=float(np.median([r[0] for r in load])), sm_max_mhz=max(r[1] for r in rows),
+                   reasons=reasons, samples=len(rows))
+        return out
+
+
+def make_pearson_data(seed: int = 3) -> np.ndarray:
+    """(N_VARS, N_OBS) float32, variable-major (R's as.single(x) order)."""
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal((N_VARS, N_OBS), dtype=np.float32)
+    x = np.exp(z + np.float32(5.0), dtype=np.float32)
+    x += rng.uniform(0.0, 1e3, (N_VARS, 1)).astype(np.float32)
+    return x
+
+
+def make_euclid_data(seed: int = 4) -> np.ndarray:
+    """(E_POINTS, E_DIM) float32 from E_CLUSTERS Gaussian clusters (sd E_SD)
+    with E_DUP of the points exact copies of other points."""
+    rng = np.random.default_rng(seed)
+    centres = rng.standard_normal((E_CLUSTERS, E_DIM), dtype=np.float32)
+    lab = rng.integers(0, E_CLUSTERS, E_POINTS)
+    pts = centres[lab] + np.float32(E_SD) * rng.standard_normal((E_POINTS, E_DIM), dtype=np.float32)
+    ndup = int(E_DUP * E_POINTS)
+    dst = rng.choice(E_POINTS, ndup, replace=False)
+    src = rng.integers(0, E_POINTS, ndup)
+    pts[dst] = pts[src]
+    return np.ascontiguousarray(pts, dtype=np.float32)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
+# ----------------------------------------------------------------------------- reference arm
+
+def run_reference(args, ranks: Ranks):
+    """The reference's CPU implementation of the path (the FP64 oracle port;
+    the reference's own compiled loops cannot run on the GPU hosts) on bounded
+    samples of the headline workload, all host threads."""
+    if ranks.rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    X = make_pearson_data()
+    rows_per_step = 8
+    rng = np.random.default_rng(11)
+    for _ in range(args.warmup):
+        r = rng.choice(N_VARS, rows_per_step, replace=False)
+        oracle.pearson(X[r], X)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = rng.choice(N_VARS, rows_per_step, replace=False)
+        oracle.pearson(X[r], X)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = rows_per_step * N_VARS / dt
+    sample = f"{rows_per_step} rows x {N_VARS} variables x {N_OBS} obs per step (FP64 oracle port)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "entries/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"gpuCor pearson {N_OBS} obs x {N_VARS} vars, cor(x), everything",
+                   "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "entries/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "entries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- our arm
+
+def run_ours(args, ranks: Ranks):
+    import torch
+    import gputools_gb300 as g
+    from gputools_gb300 import _lib
+
+    torch.cuda.set_device(ranks.local)
+    lib = g.load()
+    dev = torch.device("cuda", ranks.local)
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    peaks, peaks_kind = load_peaks()
+
+    X = make_pearson_data()
+    dX = torch.from_numpy(X).to(dev)
+    P = N_VARS
+    corr = torch.empty((P, P), dtype=torch.float32, device=dev)
+    ts = torch.empty_like(corr)
+    pairs = torch.empty_like(corr)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def pearson_step():
+        _lib.check(lib.gt_pmcc_device(0, vp(dX), P, vp(dX), P, N_OBS, vp(pairs), vp(corr), vp(ts),
+                                      sptr))
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ranks.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.gt_kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ranks.barrier()
+        ms = e0.elapsed_time(e1) / steps
+        return ranks.max(ms), lib.gt_kernel_launches() - l0
+
+    # pick the headline path: split-bf16 tensor cores unless unavailable
+    headline = "bf16x3"
+    try:
+        g.set_gram_path(headline)
+        pearson_step()
+        torch.cuda.synchronize()
+    except _lib.GpuToolsError:
+        headline = "fp32"
+        g.set_gram_path(headline)
+
+    clocks = Clocks(ranks.local)
+    clocks.start()
+    lib.gt_profile_reset()
+    lib.gt_profile_enable(1)
+    ms, launches = timed(pearson_step, args.steps, args.warmup)
+    lib.gt_profile_enable(0)
+    gram_ms = ctypes.c_double(0)
+    gram_n = ctypes.c_uint64(0)
+    lib.gt_profile_kernel_ms(b"pearson_gram", ctypes.byref(gram_ms), ctypes.byref(gram_n))
+    entries = float(P) * P
+    value = ranks.world * entries / (ms * 1e-3)
+
+    # precision on sampled rows against the FP64 oracle
+    import oracle
+    oracle.build()
+    rng = np.random.default_rng(7)
+    rows = np.sort(rng.choice(P, SAMPLE_ROWS, replace=False))
+
+    def max_err(c):
+        got = c[torch.from_numpy(rows).to(dev)].cpu().numpy().astype(np.float64)
+        want, _, _ = oracle.pearson(X[rows], X)
+        for k, r in enumerate(rows):
+            want[k, r] = 1.0
+        d = np.abs(got - want)
+        big = np.abs(want) >= 1e-2
+        return float(d.max()), float((d[big] / np.abs(want[big])).max())
+
+    t_cpu0 = time.perf_counter()
+    err_abs, err_rel = max_err(corr)
+    cpu_dt = time.perf_counter() - t_cpu0  # includes the oracle on SAMPLE_ROWS rows
+
+    # the other Gram paths on the same workload (rank 0 only; extras)
+    paths = {}
+    if ranks.rank == 0:
+        for pth in ("fp32", "bf16x6", "bf16x3"):
+            if pth == headline:
+                paths[pth] = {"entries_per_s": value / ranks.world, "ms_per_step": ms,
+                              "max_abs_err": err_abs, "max_rel_err_r_ge_0.01": err_rel}
+                continue
+            try:
+                g.set_gram_path(pth)
+                k = max(3, args.steps // 4)
+                pms, _ = timed(pearson_step, k, 1)
+                a, r = max_err(corr)
+                paths[pth] = {"entries_per_s": entries / (pms * 1e-3), "ms_per_step": pms,
+                              "max_abs_err": a, "max_rel_err_r_ge_0.01": r}
+            except _lib.GpuToolsError as e:
+                paths[pth] = {"unavailable": str(e)}
+        g.set_gram_path(headline)
+
+    # end to end through the host C ABI: pinned buffers, copies timed
+    hX = torch.from_numpy(X).pin_memory()
+    hc = torch.empty((P, P), dtype=torch.float32).pin_memory()
+    ht = torch.empty((P, P), dtype=torch.float32).pin_memory()
+    hp = torch.empty((P, P), dtype=torch.float32).pin_memory()
+    del corr, ts, pairs
+    torch.cuda.empty_cache()
+
+    def e2e_step():
+        _lib.check(lib.gt_pmcc(0, vp(hX), P, vp(hX), P, N_OBS, vp(hp), vp(hc), vp(ht)))
+
+    e2e_steps = max(3, args.steps // 4)
+    e2e_step()
+    ranks.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = ranks.max((time.perf_counter() - t0) / e2e_steps)
+    clk = clocks.stop()
+
+    # Euclidean precision workload (rank 0; R dist layout, 5e9 entries)
+    euclid = {}
+    if ranks.rank == 0 and not args.skip_euclid:
+        euclid = run_euclid(args, lib, g, _lib, stream, dev, headline)
+
+    if ranks.rank != 0:
+        return
+    flops = 2.0 * N_OBS * (P * (P + 1) / 2.0)   # useful flops per Gram launch
+    gram_avg_ms = gram_ms.value / max(1, gram_n.value)
+    tc = headline != "fp32"
+    if tc:
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        achieved = flops / (gram_avg_ms * 1e-3) / 1e12
+        products = {"bf16x3": 3, "bf16x6": 6}[headline]
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
+                "issued_frac": achieved * products / peak,
+                "kernel": "pearson_gram (tcgen05)", "kernel_ms": gram_avg_ms,
+                "traffic": load_traffic().get(f"pearson_gram_{headline}")}
+    else:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak = sms * 128 * 2 * (clk["sm_max_mhz"] or 2070.0) * 1e6 / 1e12
+        achieved = flops / (gram_avg_ms * 1e-3) / 1e12
+        roof = {"bound": "fp32-simt", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_kind": "nominal FP32 FMA rate",
+                "kernel": "pearson_gram (CUDA cores)", "kernel_ms": gram_avg_ms,
+                "traffic": load_traffic().get("pearson_gram_fp32")}
+    threads = oracle.threads()
+    line = {
+        "metric": METRIC, "value": value, "unit": "entries/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": headline,
+        "data": "synthetic: seeded lognormal(5,1) + U[0,1e3] column offsets",
+        "config": {"workload": f"gpuCor pearson cor(x), {N_OBS} obs x {N_VARS} vars, use=everything",
+                   "n_obs": N_OBS, "n_vars": N_VARS, "entries_per_step": entries,
+                   "outputs": "coefficients, ts, pairs: float32 20000x20000 each",
+                   "l2": "input 328 MB and outputs 4.8 GB exceed L2 (129 MB); no flush",
+                   "gram_path": headline, "parallelism": "replicas" if ranks.world > 1 else "single"},
+        "e2e": {"value": ranks.world * entries / e2e_s, "unit": "entries/s",
+                "h2d_bytes_per_step": int(P * N_OBS * 4), "d2h_bytes_per_step": int(3 * P * P * 4),
+                "api": "gt_pmcc (host buffers, pinned)", "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "precision": {"max_abs_err_r": err_abs, "max_rel_err_r_ge_0.01": err_rel,
+                      "sample": f"{SAMPLE_ROWS} rows x {N_VARS} vs FP64 oracle"},
+        "paths": paths,
+        "euclid": euclid,
+        "cpu_baseline": {"value": SAMPLE_ROWS * P / cpu_dt, "unit": "entries/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"FP64 oracle, {SAMPLE_ROWS} rows x {N_VARS} vars x {N_OBS} obs"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_euclid(args, lib, g, _lib, stream, dev, headline):
+    import torch
+    import oracle
+    pts = make_euclid_data()
+    dP = torch.from_numpy(pts).to(dev)
+    n = E_POINTS
+    m = n * (n - 1) // 2
+    out = torch.empty(m, dtype=torch.float32, device=dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        _lib.check(lib.gt_distances_device(ctypes.c_void_p(dP.data_ptr()), n, E_DIM,
+                                           ctypes.c_void_p(out.data_ptr()), 1, 0,
+                                           ctypes.c_float(2.0), sptr))
+
+    rng = np.random.default_rng(9)
+    rows = np.sort(rng.choice(n, 16, replace=False))
+    want = oracle.dist(pts, "euclidean", 2.0, b=pts[rows])  # [k, x] = d(x, rows[k])
+
+    def check():
+        o = out
+        errs = []
+        idx = []
+        for k, r in enumerate(rows):
+            x = np.arange(n)
+            x = x[x != r]
+            i = np.maximum(x, r); j = np.minimum(x, r)
+            idx.append(n * j - j * (j + 1) // 2 + i - j - 1)
+        idx = np.concatenate(idx)
+        got = o[torch.from_numpy(idx).to(dev)].cpu().numpy().astype(np.float64)
+        w = np.concatenate([want[k][np.arange(n) != r] for k, r in enumerate(rows)])
+        zero_ok = bool(np.all(got[w == 0] == 0))
+        rel = np.abs(got - w) / np.maximum(w, 1e-30)
+        nz = w > 0
+        return float(rel[nz].max()), zero_ok, int((w == 0).sum())
+
+    res = {"workload": f"gpuDist euclidean, {n} points x {E_DIM} dims, {E_CLUSTERS} clusters "
+                       f"(sd {E_SD}), {int(E_DUP*100)}% exact duplicates, R dist layout",
+           "entries_per_step": m}
+    for pth in (headline, "fp32") if headline != "fp32" else ("fp32",):
+        g.set_gram_path(pth)
+        k = max(3, args.steps // 4)
+        for _ in range(1):
+            step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        rel, zero_ok, nzero = check()
+        res[pth] = {"entries_per_s": m / (ms * 1e-3), "ms_per_step": ms, "max_rel_err": rel,
+                    "duplicates_exact_zero": zero_ok, "zero_pairs_in_sample": nzero}
+    g.set_gram_path(headline)
+    del out
+    torch.cuda.empty_cache()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--skip-euclid", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        # rank 0 alone times the CPU implementation; other ranks have no work
+        world, rank, _ = dist_env()
+        if rank == 0:
+            run_reference(args, type("R", (), {"rank": 0})())
+        return
+    ranks = Ranks()
+    try:
+        run_ours(args, ranks)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

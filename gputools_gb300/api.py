@@ -1,0 +1,240 @@
+"""Python mirror of gputools' R API for the all-pairs path.
+
+Same function names, argument meanings, method matching and error messages
+as the reference's R wrappers:
+
+* ``gpuDist``  -- R/gpuHclust.R:1-39
+* ``gpuCor``   -- R/gpuCor.R:1-62
+* ``gpuTtest`` -- R/gpuCor.R:64-74
+* ``chooseGpu`` / ``getGpuId`` -- R/chooseGpu.R, R/getGpuId.R
+
+Matrices follow R's conventions: ``points`` is N x D with one point per row,
+``x``/``y`` are n x p with one variable per column.  Results are float64
+arrays, as R hands back the float32 outputs of ``.C`` as doubles.  Every
+computation runs in libgputools_gb300.so through its C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+import warnings
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import GT_LAYOUT_DIST, GT_LAYOUT_FULL, check, load
+
+DIST_METHODS = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
+COR_METHODS = ("pearson", "kendall")
+COR_USES = ("everything", "pairwise.complete.obs")
+
+
+def pmatch(x: str, table: Sequence[str]) -> Optional[int]:
+    """R's pmatch for one string: exact match, else a unique prefix match,
+    else None (no match or ambiguous; the empty string matches nothing)."""
+    if not isinstance(x, str) or x == "":
+        return None
+    for i, t in enumerate(table):
+        if t == x:
+            return i
+    hits = [i for i, t in enumerate(table) if t.startswith(x)]
+    return hits[0] if len(hits) == 1 else None
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Dist:
+    """R's ``dist`` object: the strict lower triangle of the distance
+    matrix by columns, plus its attributes (Size, Labels, method, p)."""
+
+    def __init__(self, values: np.ndarray, size: int, method: str, labels=None, p=None):
+        self.values = values
+        self.size = size
+        self.method = method
+        self.labels = labels
+        self.p = p
+
+    def __len__(self):
+        return len(self.values)
+
+    def to_matrix(self) -> np.ndarray:
+        n = self.size
+        m = np.zeros((n, n), dtype=self.values.dtype)
+        # R's dist order is column-major over the lower triangle.
+        cols, rows = np.triu_indices(n, 1)
+        m[rows, cols] = self.values
+        m[cols, rows] = self.values
+        return m
+
+
+def gpuDist(points, method: str = "euclidean", p: float = 2.0, labels=None) -> Dist:
+    """Distances between the rows of ``points`` (R/gpuHclust.R:1-39)."""
+    if pmatch(method, ("euclidian",)) is not None:
+        method = "euclidean"
+    idx = pmatch(method, DIST_METHODS)
+    if idx is None:
+        raise ValueError("invalid distance method")
+    method = DIST_METHODS[idx]
+    pts = np.asarray(points, dtype=np.float64)
+    if pts.ndim == 1:
+        pts = pts.reshape(-1, 1)
+    if not np.all(np.isfinite(pts)):
+        # .C's default NAOK = FALSE rejects NA/NaN/Inf before the call.
+        raise ValueError("NA/NaN/Inf in foreign function call (arg 1)")
+    n, d = pts.shape
+    rowmajor = np.ascontiguousarray(pts, dtype=np.float32)
+    full = np.empty((n, n), dtype=np.float32)
+    lib = load()
+    if n > 0:
+        check(lib.gt_distances(_ptr(rowmajor), n, d, _ptr(full), idx, float(np.float32(p))))
+    # as.dist(matrix(d, N, N)): lower triangle, column by column.
+    cols, rows = np.triu_indices(n, 1)
+    values = full[cols, rows].astype(np.float64)
+    return Dist(values, n, method, labels, p if method == "minkowski" else None)
+
+
+def gpuCor(x, y=None, use: str = "everything", method: str = "pearson"):
+    """Pearson or Kendall correlation of every column pair (R/gpuCor.R:1-62)."""
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1)
+    size, nx = x.shape
+    same = y is None
+    y = x if same else np.asarray(y, dtype=np.float64)
+    if y.ndim == 1:
+        y = y.reshape(-1, 1)
+    ny = y.shape[1]
+    # pmatch(..., nomatch = -1): a miss is reported as "ambiguous", an
+    # ambiguous prefix as "invalid" -- the reference's messages, verbatim.
+    m = pmatch(method, COR_METHODS)
+    if m is None:
+        raise ValueError("ambiguous correlation method")
+    u = pmatch(use, COR_USES)
+    if u is None:
+        raise ValueError("ambiguous correlation method")
+    if y.shape[0] != size:
+        raise ValueError("x and y need the same number of rows")
+    # as.single(x) flattens column-major: variable j at [j*size .. j*size+size-1].
+    X = np.ascontiguousarray(x.T, dtype=np.float32)
+    Y = X if same else np.ascontiguousarray(y.T, dtype=np.float32)
+    lib = load()
+    if COR_METHODS[m] == "pearson":
+        corr = np.empty((nx, ny), np.float32)
+        ts = np.empty((nx, ny), np.float32)
+        pairs = np.empty((nx, ny), np.float32)
+        if nx and ny:
+            check(lib.gt_pmcc(u, _ptr(X), nx, _ptr(Y), ny, size, _ptr(pairs), _ptr(corr), _ptr(ts)))
+        return {"coefficients": corr.astype(np.float64), "ts": ts.astype(np.float64),
+                "pairs": pairs.astype(np.float64)}
+    if COR_USES[u] != "everything":
+        warnings.warn("NA handling for Kendall's is not yet supported. Defaulting to using "
+                      "everything. Sorry for any inconvenience.")
+    if np.isnan(X).any() or np.isnan(Y).any():
+        raise ValueError("NA/NaN/Inf in foreign function call (arg 1)")
+    res = np.empty((ny, nx), np.float64)  # answers[y*nx + x]
+    if nx and ny:
+        check(lib.gt_kendall(_ptr(X), nx, _ptr(Y), ny, size, _ptr(res)))
+    return {"coefficients": np.ascontiguousarray(res.T), "pairs": np.full((nx, ny), float(size))}
+
+
+def gpuTtest(goodPairs, coeffs) -> np.ndarray:
+    """t-scores of Pearson coefficients (R/gpuCor.R:64-74 via rtestT)."""
+    gp = np.ascontiguousarray(np.asarray(goodPairs, dtype=np.float32).ravel())
+    co = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float32).ravel())
+    n = ctypes.c_int(gp.size)
+    out = np.empty(gp.size, np.float32)
+    lib = load()
+    lib.rtestT(_ptr(gp), _ptr(co), ctypes.byref(n), _ptr(out))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return out.astype(np.float64)
+
+
+def chooseGpu(deviceId: int = 0) -> int:
+    """R/chooseGpu.R: select the device used by later calls."""
+    lib = load()
+    d = ctypes.c_int(int(deviceId))
+    lib.rsetDevice(ctypes.byref(d))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return int(deviceId)
+
+
+def getGpuId() -> int:
+    """R/getGpuId.R: the device currently used."""
+    lib = load()
+    d = ctypes.c_int(-1)
+    lib.rgetDevice(ctypes.byref(d))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return d.value
+
+
+# ---------------------------------------------------------------------------
+# Device-buffer entry points (torch tensors as the memory and stream owner).
+
+def _stream_ptr(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def distances_device(points, method: str = "euclidean", p: float = 2.0, layout: str = "full",
+                     out=None, stream=None):
+    """gt_distances_device on a CUDA float32 tensor of shape (N, D)."""
+    import torch
+    if points.dtype != torch.float32 or not points.is_cuda or not points.is_contiguous():
+        raise ValueError("points must be a contiguous float32 CUDA tensor")
+    n, d = points.shape
+    lay = GT_LAYOUT_FULL if layout == "full" else GT_LAYOUT_DIST
+    count = n * n if lay == GT_LAYOUT_FULL else n * (n - 1) // 2
+    if out is None:
+        out = torch.empty(count, dtype=torch.float32, device=points.device)
+    check(load().gt_distances_device(ctypes.c_void_p(points.data_ptr()), n, d,
+                                     ctypes.c_void_p(out.data_ptr()), lay,
+                                     DIST_METHODS.index(method), float(p), _stream_ptr(stream)))
+    return out
+
+
+def pmcc_device(A, B=None, use: int = 0, stream=None, outputs=("pairs", "corr", "ts")):
+    """gt_pmcc_device on variable-major CUDA tensors A (nA, n) and B (nB, n);
+    B None or the same tensor is the symmetric problem cor(x)."""
+    import torch
+    B = A if B is None else B
+    nA, n = A.shape
+    nB = B.shape[0]
+    res = {k: torch.empty((nA, nB), dtype=torch.float32, device=A.device) for k in outputs}
+    ptr = lambda k: ctypes.c_void_p(res[k].data_ptr()) if k in res else None
+    check(load().gt_pmcc_device(int(use), ctypes.c_void_p(A.data_ptr()), nA,
+                                ctypes.c_void_p(B.data_ptr()), nB, n, ptr("pairs"), ptr("corr"),
+                                ptr("ts"), _stream_ptr(stream)))
+    return res
+
+
+def kendall_device(X, Y=None, stream=None):
+    """gt_kendall_device on variable-major CUDA tensors; returns (ny, nx) float64."""
+    import torch
+    Y = X if Y is None else Y
+    nx, n = X.shape
+    ny = Y.shape[0]
+    out = torch.empty((ny, nx), dtype=torch.float64, device=X.device)
+    check(load().gt_kendall_device(ctypes.c_void_p(X.data_ptr()), nx,
+                                   ctypes.c_void_p(Y.data_ptr()), ny, n,
+                                   ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)))
+    return out
+
+
+def set_gram_path(path: str) -> None:
+    """"bf16x3" / "bf16x6" (tcgen05 split-bf16) or "fp32" (CUDA cores)."""
+    code = {"bf16x3": _lib.GT_GRAM_TC_BF16X3, "bf16x6": _lib.GT_GRAM_TC_BF16X6,
+            "fp32": _lib.GT_GRAM_FP32}[path]
+    check(load().gt_set_gram_path(code))
+
+
+def get_gram_path() -> str:
+    return {0: "bf16x3", 1: "bf16x6", 2: "fp32"}[load().gt_get_gram_path()]

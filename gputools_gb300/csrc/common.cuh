@@ -1,0 +1,73 @@
+// common.cuh -- shared runtime pieces of libgputools_gb300: status codes,
+// the thread-local error message, per-device streams and the grow-only
+// device workspace that replaces the reference's per-call cudaMalloc/cudaFree
+// (src/distance.cpp:277-316, src/correlation.cpp:83-160, src/kendall.cpp:13-55).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+
+#include "gputools_gb300.h"
+
+namespace gt {
+
+// Records `msg` as the calling thread's last error and returns `code`.
+int fail(int code, const char *fmt, ...);
+// Clears the calling thread's last error.
+void clear_error();
+const char *last_error();
+
+// CUDA runtime call -> GT_ECUDA with the call site in the message.
+#define GT_CUDA(expr)                                                          \
+  do {                                                                         \
+    cudaError_t _e = (expr);                                                   \
+    if (_e != cudaSuccess)                                                     \
+      return ::gt::fail(GT_ECUDA, "%s failed: %s (%s:%d)", #expr,              \
+                        cudaGetErrorString(_e), __FILE__, __LINE__);           \
+  } while (0)
+
+#define GT_TRY(expr)                                                           \
+  do {                                                                         \
+    int _s = (expr);                                                           \
+    if (_s != GT_OK) return _s;                                                \
+  } while (0)
+
+// Library-private non-blocking stream of the current device (created once).
+cudaStream_t lib_stream();
+
+// Named slots of the per-device workspace.  Each slot is a grow-only device
+// buffer kept across calls and released by gt_release_workspace().
+enum WsSlot {
+  WS_IN_A = 0, WS_IN_B, WS_OUT0, WS_OUT1, WS_OUT2, WS_SCRATCH0, WS_SCRATCH1,
+  WS_SCRATCH2, WS_SCRATCH3, WS_SCRATCH4, WS_NSLOTS
+};
+// Device buffer of at least `bytes` for `slot` on the current device.
+int ws_get(int slot, size_t bytes, void **ptr);
+void ws_release_all();
+
+// Counts kernel launches (gt_kernel_launches); call once per launch.
+void count_launch(int n = 1);
+
+// Event timing of one launch on its stream (enabled by gt_profile_enable).
+class ProfScope {
+ public:
+  ProfScope(const char *name, cudaStream_t st);
+  ~ProfScope();
+  ProfScope(const ProfScope &) = delete;
+  ProfScope &operator=(const ProfScope &) = delete;
+
+ private:
+  const char *name_;
+  cudaStream_t st_;
+  cudaEvent_t e0_ = nullptr;
+};
+
+// Host-side reads of the device the library runs on.
+int current_device(int *dev);
+int sm_count();
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace gt

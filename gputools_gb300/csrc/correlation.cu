@@ -1,0 +1,364 @@
+// correlation.cu -- gpuCor(method = "pearson") and gpuTtest.
+//
+// Reference: src/correlation.cpp:66-161 pmcc() runs three per-pair kernels
+// (inst/cuda/correlation.cu:7-292: means -> standard deviations -> sum of
+// z-score products), each one block per (x, y) pair that re-reads both
+// columns, stores O(nA*nB) temporary means/SDs, and computes t-scores on the
+// host (hostSignif, src/correlation.cpp:51-64).
+//
+// Here:
+//  * a prologue computes each variable's mean and norm once, in FP64
+//    (corrected two-pass), and writes the normalised column
+//    z = (x - mean) / ||x - mean||, so r(x, y) = <z_x, z_y>;
+//  * "everything": the Gram contraction runs on tcgen05 tensor cores
+//    (split bf16, gram_tc.cu) or, for GT_GRAM_FP32, on the CUDA-core engine;
+//  * "pairwise.complete.obs": the CUDA-core engine accumulates, per pair, the
+//    six masked sums (count, sums, squares, cross) of the standardised values
+//    and the epilogue forms r in FP64;
+//  * pairs, r and the t-score (hostSignif's rule, in float as the reference
+//    evaluates it) are written by the same epilogue; cor(x) computes each
+//    unordered pair once and mirrors it.
+#include "common.cuh"
+#include "allpairs_simt.cuh"
+#include "kernels.cuh"
+
+#include <cmath>
+
+namespace gt {
+
+namespace {
+
+constexpr int kStatThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = (l < kStatThreads / 32) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (l == 0) sh[0] = t;
+  }
+  __syncthreads();
+  return sh[0];
+}
+
+// One CTA per variable: FP64 mean (refined by the mean residual, the
+// corrected two-pass algorithm) and centred sum of squares.
+// use 0: every value counts and any NaN flags the variable;
+// use 1: NaN values are skipped.
+__global__ void __launch_bounds__(kStatThreads)
+colstats_kernel(const float *__restrict__ X, int64_t n, int use, ColStats *__restrict__ out) {
+  __shared__ double sh[32];
+  const float *x = X + int64_t(blockIdx.x) * n;
+  double s = 0.0, cnt = 0.0, nan = 0.0;
+  for (int64_t k = threadIdx.x; k < n; k += kStatThreads) {
+    const float v = x[k];
+    if (v != v) { nan += 1.0; continue; }
+    s += double(v);
+    cnt += 1.0;
+  }
+  s = block_sum(s, sh);
+  cnt = block_sum(cnt, sh);
+  nan = block_sum(nan, sh);
+  double mean = cnt > 0.0 ? s / cnt : 0.0;
+  double c = 0.0, ss = 0.0;
+  for (int64_t k = threadIdx.x; k < n; k += kStatThreads) {
+    const float v = x[k];
+    if (v != v) continue;
+    const double d = double(v) - mean;
+    c += d;
+    ss = fma(d, d, ss);
+  }
+  c = block_sum(c, sh);
+  ss = block_sum(ss, sh);
+  if (threadIdx.x == 0) {
+    ColStats st;
+    if (cnt > 0.0) {
+      mean += c / cnt;
+      ss -= c * c / cnt;
+    }
+    st.mean = mean;
+    st.flags = 0;
+    if (use == 0 && nan > 0.0) st.flags |= 1;
+    if (!(ss > 0.0) || cnt < 2.0) st.flags |= 2;
+    st.inv_norm = (st.flags & 2) ? 0.0 : 1.0 / sqrt(ss);
+    out[blockIdx.x] = st;
+  }
+}
+
+// z[v][k] = (x - mean) * inv_norm in float, rows of length ldz (>= n, pad
+// filled with `padv`).  Everything mode: a variable containing NaN or with
+// zero variance becomes all-NaN, so every r involving it is NaN.
+__global__ void normalize_f32_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
+                                     int64_t ldz, const ColStats *__restrict__ st, int use,
+                                     float padv, float *__restrict__ Z) {
+  const int64_t total = nvar * ldz;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t v = i / ldz, k = i - v * ldz;
+    float z;
+    if (k >= n) {
+      z = padv;
+    } else {
+      const ColStats s = st[v];
+      const float x = X[v * n + k];
+      if (use == 0 && s.flags) z = __int_as_float(0x7fc00000);
+      else z = float((double(x) - s.mean) * s.inv_norm);
+    }
+    Z[i] = z;
+  }
+}
+
+__device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
+
+// hostSignif (src/correlation.cpp:51-64), evaluated in float as there.
+__device__ __forceinline__ float signif(float r, float pairs) {
+  if (r >= 0.999f) return 10000.0f;
+  return r * sqrtf((pairs - 2.f) / (1.f - r * r));
+}
+
+struct OpDot {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const { c[0] = fmaf(a, b, c[0]); }
+};
+
+struct OutPearsonF32 {
+  PearsonOut o;
+  __device__ void operator()(int64_t r, int64_t c, const float (&acc)[1], bool mirror) const {
+    float v = clamp_r(acc[0]);
+    if (o.symmetric && r == c && v == v) v = 1.f;
+    const float t = signif(v, o.npairs);
+    const int64_t i0 = r * o.ld + c, i1 = c * o.ld + r;
+    if (o.corr) { o.corr[i0] = v; if (mirror) o.corr[i1] = v; }
+    if (o.ts) { o.ts[i0] = t; if (mirror) o.ts[i1] = t; }
+    if (o.pairs) { o.pairs[i0] = o.npairs; if (mirror) o.pairs[i1] = o.npairs; }
+  }
+};
+
+// Pairwise-complete sums over observations where both values are present:
+// count, sum a, sum b, sum a^2, sum b^2, sum a*b.
+struct OpPairwise {
+  static constexpr int NACC = 6;
+  __device__ static float pad() { return __int_as_float(0x7fc00000); }
+  __device__ void init(float (&c)[6]) const {
+#pragma unroll
+    for (int i = 0; i < 6; i++) c[i] = 0.f;
+  }
+  __device__ void step(float (&c)[6], float a, float b) const {
+    const bool both = (a == a) & (b == b);
+    const float fa = both ? a : 0.f, fb = both ? b : 0.f;
+    c[0] += both ? 1.f : 0.f;
+    c[1] += fa;
+    c[2] += fb;
+    c[3] = fmaf(fa, fa, c[3]);
+    c[4] = fmaf(fb, fb, c[4]);
+    c[5] = fmaf(fa, fb, c[5]);
+  }
+};
+
+struct OutPairwise {
+  PearsonOut o;
+  __device__ void operator()(int64_t r, int64_t c, const float (&acc)[6], bool mirror) const {
+    const double n = acc[0];
+    float v = __int_as_float(0x7fc00000);
+    if (n >= 2.0) {
+      const double sa = acc[1], sb = acc[2];
+      const double va = double(acc[3]) - sa * sa / n;
+      const double vb = double(acc[4]) - sb * sb / n;
+      const double cv = double(acc[5]) - sa * sb / n;
+      if (va > 0.0 && vb > 0.0) v = clamp_r(float(cv / sqrt(va * vb)));
+    }
+    if (o.symmetric && r == c && v == v) v = 1.f;
+    const float np = float(n);
+    const float t = signif(v, np);
+    const int64_t i0 = r * o.ld + c, i1 = c * o.ld + r;
+    if (o.corr) { o.corr[i0] = v; if (mirror) o.corr[i1] = v; }
+    if (o.ts) { o.ts[i0] = t; if (mirror) o.ts[i1] = t; }
+    if (o.pairs) { o.pairs[i0] = np; if (mirror) o.pairs[i1] = np; }
+  }
+};
+
+__global__ void ttest_kernel(const float *__restrict__ pairs, const float *__restrict__ r,
+                             int64_t n, float *__restrict__ ts) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const float c = r[i];
+    ts[i] = c * sqrtf((pairs[i] - 2.f) / (1.f - c * c));
+  }
+}
+
+__global__ void differ_kernel(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
+                              int64_t nwords, int *flag) {
+  int local = 0;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nwords;
+       i += int64_t(gridDim.x) * blockDim.x)
+    local |= (a[i] != b[i]);
+  if (__syncthreads_or(local) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+int grid_for(int64_t work, int threads) {
+  const int64_t g = cdiv(work, threads);
+  const int64_t cap = int64_t(sm_count()) * 16;
+  return int(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+// Column statistics + normalised float rows for one operand.
+int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz, int slot_z,
+                 int slot_st, float **Z, ColStats **st, cudaStream_t s) {
+  void *pz = nullptr, *pst = nullptr;
+  GT_TRY(ws_get(slot_z, size_t(nvar) * size_t(ldz) * 4, &pz));
+  GT_TRY(ws_get(slot_st, size_t(nvar) * sizeof(ColStats), &pst));
+  *Z = static_cast<float *>(pz);
+  *st = static_cast<ColStats *>(pst);
+  ProfScope prof("pearson_prologue", s);
+  colstats_kernel<<<unsigned(nvar), kStatThreads, 0, s>>>(dX, n, use, *st);
+  count_launch();
+  const float padv = use == 0 ? 0.f : __builtin_nanf("");
+  normalize_f32_kernel<<<grid_for(nvar * ldz, 256), 256, 0, s>>>(dX, nvar, n, ldz, *st, use,
+                                                                   padv, *Z);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+}  // namespace
+
+// prologue for the tensor-core path lives in gram_tc.cu
+int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, int slot_z,
+                        int slot_st, void **Z, int64_t *kpad, cudaStream_t s);
+
+int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t nB, int64_t n,
+                 float *pairs, float *corr, float *ts, int symmetric, cudaStream_t s) {
+  if (nA == 0 || nB == 0) return GT_OK;
+  PearsonOut po{corr, ts, pairs, nB, float(n), symmetric};
+  const int path = gt_get_gram_path();
+  if (use == GT_EVERYTHING && path != GT_GRAM_FP32) {
+    const int nsplit = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
+    void *zA = nullptr, *zB = nullptr;
+    int64_t kpad = 0;
+    GT_TRY(pearson_tc_prologue(dA, nA, n, nsplit, WS_SCRATCH0, WS_SCRATCH2, &zA, &kpad, s));
+    if (symmetric) zB = zA;
+    else GT_TRY(pearson_tc_prologue(dB, nB, n, nsplit, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
+    return pearson_tc(zA, nA, zB, nB, kpad, nsplit, po, s);
+  }
+  const int64_t ldz = (n + 3) / 4 * 4;
+  float *zA = nullptr, *zB = nullptr;
+  ColStats *sA = nullptr, *sB = nullptr;
+  GT_TRY(prologue_f32(dA, nA, n, use, ldz, WS_SCRATCH0, WS_SCRATCH2, &zA, &sA, s));
+  if (symmetric) zB = zA;
+  else GT_TRY(prologue_f32(dB, nB, n, use, ldz, WS_SCRATCH1, WS_SCRATCH3, &zB, &sB, s));
+  SimtArgs a;
+  a.R = zA; a.C = zB;
+  a.ldr = a.ldc = ldz;
+  a.nr = nA; a.nc = nB;
+  a.K = ldz;
+  a.symmetric = symmetric;
+  a.vec_ok = 1;
+  cudaError_t e;
+  ProfScope prof(use == GT_EVERYTHING ? "pearson_gram" : "pearson_pairwise", s);
+  if (use == GT_EVERYTHING) {
+    const int64_t t = cdiv(nA, 128) * cdiv(nB, 128) / (symmetric ? 2 : 1);
+    if (t >= 2 * sm_count())
+      e = launch_allpairs_simt<OpDot, OutPearsonF32, 8, 8>(a, OpDot{}, OutPearsonF32{po}, s);
+    else
+      e = launch_allpairs_simt<OpDot, OutPearsonF32, 4, 4>(a, OpDot{}, OutPearsonF32{po}, s);
+  } else {
+    e = launch_allpairs_simt<OpPairwise, OutPairwise, 4, 4>(a, OpPairwise{}, OutPairwise{po}, s);
+  }
+  if (e != cudaSuccess) return fail(GT_ECUDA, "pearson kernel launch: %s", cudaGetErrorString(e));
+  return GT_OK;
+}
+
+int pearson_check(int use, int64_t nA, int64_t nB, int64_t n) {
+  if (use != GT_EVERYTHING && use != GT_PAIRWISE_COMPLETE)
+    return fail(GT_EINVAL, "unknown use method");
+  if (nA < 0 || nB < 0 || n < 0) return fail(GT_EINVAL, "negative size");
+  if (nA > 2147483647LL || nB > 2147483647LL) return fail(GT_EINVAL, "too many variables");
+  if (cdiv(nA, 64) > 65535) return fail(GT_EINVAL, "too many variables (%lld)", (long long)nA);
+  return GT_OK;
+}
+
+// Device-side equality of two float buffers (bitwise), used to recognise
+// gpuCor(x) called through .C, which always passes two copies of x.
+int same_contents(const float *a, const float *b, int64_t count, bool *same, cudaStream_t s) {
+  void *pf = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH4, 256, &pf));
+  int *flag = static_cast<int *>(pf);
+  GT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  if (count > 0)
+    differ_kernel<<<grid_for(count, 256), 256, 0, s>>>(reinterpret_cast<const uint32_t *>(a),
+                                                        reinterpret_cast<const uint32_t *>(b),
+                                                        count, flag);
+  if (count > 0) count_launch();
+  int h = 1;
+  GT_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GT_CUDA(cudaStreamSynchronize(s));
+  *same = (h == 0);
+  return GT_OK;
+}
+
+}  // namespace gt
+
+extern "C" int gt_pmcc_device(int use, const float *d_A, int64_t nA, const float *d_B, int64_t nB,
+                              int64_t n, float *d_pairs, float *d_corr, float *d_ts,
+                              void *stream) {
+  gt::clear_error();
+  GT_TRY(gt::pearson_check(use, nA, nB, n));
+  if ((nA > 0 && !d_A) || (nB > 0 && !d_B)) return gt::fail(GT_EINVAL, "null device pointer");
+  const int sym = (d_A == d_B && nA == nB) ? 1 : 0;
+  return gt::pearson_impl(use, d_A, nA, d_B, nB, n, d_pairs, d_corr, d_ts, sym,
+                          static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int64_t nB, int64_t n,
+                       float *pairs, float *corr, float *ts) {
+  gt::clear_error();
+  GT_TRY(gt::pearson_check(use, nA, nB, n));
+  if (nA == 0 || nB == 0) return GT_OK;
+  if (!A || !B) return gt::fail(GT_EINVAL, "null host pointer");
+  cudaStream_t s = gt::lib_stream();
+  const size_t inA = size_t(nA) * size_t(n) * 4, inB = size_t(nB) * size_t(n) * 4;
+  const size_t outb = size_t(nA) * size_t(nB) * 4;
+  void *dA = nullptr, *dB = nullptr, *o0 = nullptr, *o1 = nullptr, *o2 = nullptr;
+  GT_TRY(gt::ws_get(gt::WS_IN_A, inA, &dA));
+  GT_CUDA(cudaMemcpyAsync(dA, A, inA, cudaMemcpyHostToDevice, s));
+  bool sym = (A == B && nA == nB);
+  if (!sym) {
+    GT_TRY(gt::ws_get(gt::WS_IN_B, inB, &dB));
+    GT_CUDA(cudaMemcpyAsync(dB, B, inB, cudaMemcpyHostToDevice, s));
+    if (nA == nB)
+      GT_TRY(gt::same_contents(static_cast<float *>(dA), static_cast<float *>(dB), nA * n, &sym, s));
+  }
+  if (sym) dB = dA;
+  if (corr) GT_TRY(gt::ws_get(gt::WS_OUT0, outb, &o0));
+  if (ts) GT_TRY(gt::ws_get(gt::WS_OUT1, outb, &o1));
+  if (pairs) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));
+  GT_TRY(gt::pearson_impl(use, static_cast<float *>(dA), nA, static_cast<float *>(dB), nB, n,
+                          static_cast<float *>(o2), static_cast<float *>(o0),
+                          static_cast<float *>(o1), sym ? 1 : 0, s));
+  if (corr) GT_CUDA(cudaMemcpyAsync(corr, o0, outb, cudaMemcpyDeviceToHost, s));
+  if (ts) GT_CUDA(cudaMemcpyAsync(ts, o1, outb, cudaMemcpyDeviceToHost, s));
+  if (pairs) GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
+  GT_CUDA(cudaStreamSynchronize(s));
+  return GT_OK;
+}
+
+extern "C" int gt_ttest_device(const float *d_pairs, const float *d_coeffs, int64_t n, float *d_ts,
+                               void *stream) {
+  gt::clear_error();
+  if (n < 0) return gt::fail(GT_EINVAL, "negative size");
+  if (n == 0) return GT_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gt::ttest_kernel<<<gt::grid_for(n, 256), 256, 0, s>>>(d_pairs, d_coeffs, n, d_ts);
+  gt::count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}

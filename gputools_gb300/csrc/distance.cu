@@ -1,0 +1,216 @@
+// distance.cu -- gpuDist's six metrics on CUDA cores.
+//
+// Reference: src/distance.cpp:209-316 (distance, distance_device) launching
+// the `*_kernel_same` kernels of inst/cuda/distance.cu (euclidean :40-78,
+// maximum :116-154, manhattan :192-232, canberra :273-316, binary :366-415,
+// minkowski :453-493).  Those kernels use one 32-thread block per (x, y) with
+// a shared-memory tree reduction; here every metric runs on the tiled engine
+// of allpairs_simt.cuh, computing each unordered pair once.
+//
+// Semantics follow R's stats::dist (the reference's documented model):
+//  * canberra omits terms whose numerator and denominator are both zero
+//    (a = b = 0) and scales the sum by dim / terms-used; a term with a zero
+//    denominator only (a = -b != 0) is +Inf.  The reference kernel instead
+//    skips every zero-denominator term and never rescales
+//    (inst/cuda/distance.cu:294), so the two differ only when zeros occur.
+//  * minkowski evaluates |a-b|^p exactly for p = 1, 2, 3 and with powf
+//    otherwise (the reference uses the low-accuracy __powf, :471, :487); the
+//    final root is taken in double.
+#include "common.cuh"
+#include "allpairs_simt.cuh"
+#include "kernels.cuh"
+
+#include <cmath>
+
+namespace gt {
+
+namespace {
+
+struct OpEuclid {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const {
+    const float d = a - b;
+    c[0] = fmaf(d, d, c[0]);
+  }
+  __device__ float finish(const float (&c)[1], int64_t) const { return sqrtf(c[0]); }
+};
+
+struct OpManhattan {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const { c[0] += fabsf(a - b); }
+  __device__ float finish(const float (&c)[1], int64_t) const { return c[0]; }
+};
+
+struct OpMaximum {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const { c[0] = fmaxf(c[0], fabsf(a - b)); }
+  __device__ float finish(const float (&c)[1], int64_t) const { return c[0]; }
+};
+
+struct OpCanberra {
+  static constexpr int NACC = 2;  // sum of terms, number of terms used
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[2]) const { c[0] = 0.f; c[1] = 0.f; }
+  __device__ void step(float (&c)[2], float a, float b) const {
+    const bool used = (a != 0.f) | (b != 0.f);
+    const float t = __fdiv_rn(fabsf(a - b), fabsf(a + b));
+    c[0] += used ? t : 0.f;
+    c[1] += used ? 1.f : 0.f;
+  }
+  __device__ float finish(const float (&c)[2], int64_t K) const {
+    if (c[1] == 0.f) return __int_as_float(0x7fc00000);
+    if (double(c[1]) < double(K)) return float(double(c[0]) / (double(c[1]) / double(K)));
+    return c[0];
+  }
+};
+
+struct OpBinary {
+  static constexpr int NACC = 2;  // bits on in exactly one, bits on in either
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[2]) const { c[0] = 0.f; c[1] = 0.f; }
+  __device__ void step(float (&c)[2], float a, float b) const {
+    const bool x = a != 0.f, y = b != 0.f;
+    c[0] += (x != y) ? 1.f : 0.f;
+    c[1] += (x || y) ? 1.f : 0.f;
+  }
+  __device__ float finish(const float (&c)[2], int64_t) const {
+    return c[1] != 0.f ? c[0] / c[1] : 0.f;
+  }
+};
+
+struct OpMink3 {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const {
+    const float d = fabsf(a - b);
+    c[0] = fmaf(d * d, d, c[0]);
+  }
+  __device__ float finish(const float (&c)[1], int64_t) const { return float(cbrt(double(c[0]))); }
+};
+
+struct OpMinkP {
+  static constexpr int NACC = 1;
+  float p;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const { c[0] += powf(fabsf(a - b), p); }
+  __device__ float finish(const float (&c)[1], int64_t) const {
+    return float(pow(double(c[0]), 1.0 / double(p)));
+  }
+};
+
+// Writes one distance in the full square layout (d[y*n + x], both halves)
+// or R's dist layout (strict lower triangle by columns).
+template <class Op>
+struct OutDist {
+  Op op;
+  float *out;
+  int64_t n, K;
+  int layout;
+  __device__ void operator()(int64_t r, int64_t c, const float (&acc)[Op::NACC], bool mirror) const {
+    if (layout == GT_LAYOUT_FULL) {
+      const float v = (r == c) ? 0.f : op.finish(acc, K);
+      out[r * n + c] = v;
+      if (mirror) out[c * n + r] = v;
+    } else {
+      if (c <= r) return;  // each unordered pair once; (r, c) with c > r
+      const int64_t i = c, j = r;
+      out[n * j - j * (j + 1) / 2 + i - j - 1] = op.finish(acc, K);
+    }
+  }
+};
+
+template <class Op>
+cudaError_t run_metric(const Op &op, const float *pts, int64_t n, int64_t dim, float *out,
+                       int layout, cudaStream_t st) {
+  SimtArgs a;
+  a.R = a.C = pts;
+  a.ldr = a.ldc = dim;
+  a.nr = a.nc = n;
+  a.K = dim;
+  a.symmetric = 1;
+  a.vec_ok = (dim % 4 == 0) && aligned16(pts);
+  OutDist<Op> o{op, out, n, dim, layout};
+  ProfScope prof("dist", st);
+  const int64_t t128 = cdiv(n, 128);
+  if (Op::NACC == 1 && t128 * (t128 + 1) / 2 >= 2 * sm_count())
+    return launch_allpairs_simt<Op, OutDist<Op>, 8, 8>(a, op, o, st);
+  return launch_allpairs_simt<Op, OutDist<Op>, 4, 4>(a, op, o, st);
+}
+
+}  // namespace
+
+int dist_check_args(int64_t n, int64_t dim, int method, int layout) {
+  if (n < 0 || dim < 0) return fail(GT_EINVAL, "negative size (n=%lld, dim=%lld)",
+                                    (long long)n, (long long)dim);
+  if (method < GT_EUCLIDEAN || method > GT_MINKOWSKI)
+    return fail(GT_EINVAL, "unknown distance method %d", method);
+  if (layout != GT_LAYOUT_FULL && layout != GT_LAYOUT_DIST)
+    return fail(GT_EINVAL, "unknown output layout %d", layout);
+  if (cdiv(n, 64) > 65535) return fail(GT_EINVAL, "too many points (%lld)", (long long)n);
+  return GT_OK;
+}
+
+// Euclidean distances on the FP32 CUDA-core path; used directly for
+// GT_GRAM_FP32 and as the reference point of the tensor-core path.
+int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout, int method,
+              float p, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  switch (method) {
+  case GT_EUCLIDEAN: e = run_metric(OpEuclid{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_MAXIMUM: e = run_metric(OpMaximum{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_MANHATTAN: e = run_metric(OpManhattan{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_CANBERRA: e = run_metric(OpCanberra{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_BINARY: e = run_metric(OpBinary{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_MINKOWSKI:
+    if (p == 1.f) e = run_metric(OpManhattan{}, d_pts, n, dim, d_out, layout, st);
+    else if (p == 2.f) e = run_metric(OpEuclid{}, d_pts, n, dim, d_out, layout, st);
+    else if (p == 3.f) e = run_metric(OpMink3{}, d_pts, n, dim, d_out, layout, st);
+    else e = run_metric(OpMinkP{p}, d_pts, n, dim, d_out, layout, st);
+    break;
+  default: return fail(GT_EINVAL, "unknown distance method %d", method);
+  }
+  if (e != cudaSuccess) return fail(GT_ECUDA, "distance kernel launch: %s", cudaGetErrorString(e));
+  return GT_OK;
+}
+
+}  // namespace gt
+
+extern "C" int gt_distances_device(const float *d_points, int64_t n, int64_t dim, float *d_out,
+                                   int layout, int method, float p, void *stream) {
+  gt::clear_error();
+  GT_TRY(gt::dist_check_args(n, dim, method, layout));
+  if (n == 0) return GT_OK;
+  if (!d_points || !d_out) return gt::fail(GT_EINVAL, "null device pointer");
+  if (method == GT_MINKOWSKI && !(p > 0.f))
+    return gt::fail(GT_EINVAL, "minkowski power must be positive (p=%g)", double(p));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (method == GT_EUCLIDEAN && gt_get_gram_path() != GT_GRAM_FP32)
+    return gt::euclid_tc(d_points, n, dim, d_out, layout, st);
+  return gt::dist_simt(d_points, n, dim, d_out, layout, method, p, st);
+}
+
+extern "C" int gt_distances(const float *points, int64_t n, int64_t dim, float *out, int method,
+                            float p) {
+  gt::clear_error();
+  GT_TRY(gt::dist_check_args(n, dim, method, GT_LAYOUT_FULL));
+  if (n == 0) return GT_OK;
+  if (!points || !out) return gt::fail(GT_EINVAL, "null host pointer");
+  cudaStream_t st = gt::lib_stream();
+  void *dp = nullptr, *dout = nullptr;
+  GT_TRY(gt::ws_get(gt::WS_IN_A, size_t(n) * size_t(dim) * 4, &dp));
+  GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(n) * size_t(n) * 4, &dout));
+  GT_CUDA(cudaMemcpyAsync(dp, points, size_t(n) * size_t(dim) * 4, cudaMemcpyHostToDevice, st));
+  GT_TRY(gt_distances_device(static_cast<float *>(dp), n, dim, static_cast<float *>(dout),
+                             GT_LAYOUT_FULL, method, p, st));
+  GT_CUDA(cudaMemcpyAsync(out, dout, size_t(n) * size_t(n) * 4, cudaMemcpyDeviceToHost, st));
+  GT_CUDA(cudaStreamSynchronize(st));
+  return GT_OK;
+}

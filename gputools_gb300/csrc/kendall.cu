@@ -1,0 +1,286 @@
+// kendall.cu -- gpuCor(method = "kendall"): tau-b from exact integer counts.
+//
+// Reference: src/kendall.cpp:13-55 masterKendall() launches
+// inst/cuda/kendall.cu:4-47 gpuKendall, one 16x16 block per variable pair
+// that loops over all observation pairs with float counters (exact only below
+// 2^24) and reports (C - (T - C)) / T with joint ties counted as concordant,
+// which is not R's cor(method = "kendall").
+//
+// Here the observation pairs are bit-sliced once per variable:
+//   pair p = (i, (i + d) mod n), d = 1 .. floor(n/2), i = 0 .. n-1
+//   (for even n the row d = n/2 keeps only i < n/2), which enumerates every
+//   unordered pair exactly once in rows of n bits;
+//   U_v[p] = x_v[j] != x_v[i]   (pair not tied),   G_v[p] = x_v[j] > x_v[i].
+// For a variable pair (x, y), with m = U_x & U_y:
+//   concordant - discordant = popc(m) - 2 popc(m & (G_x ^ G_y)),
+// accumulated over 32-bit words by a shared-memory-tiled CUDA-core kernel
+// (64x64 variable tiles, 128-bit loads, split over the pair dimension with
+// 64-bit atomics).  Tx = popc(U_x).  tau-b = S / (sqrt(Tx) * sqrt(Ty)) is then
+// evaluated in IEEE double with explicit round-to-nearest operations in R's
+// order, clamped to [-1, 1]; NaN when either variable is constant; exactly 1
+// on the diagonal of cor(x).
+#include "common.cuh"
+
+#include <cmath>
+
+namespace gt {
+
+namespace {
+
+constexpr int kKT = 256;        // threads per count CTA
+constexpr int kKBK = 16;        // words per shared slab
+constexpr int kKLd = 18;        // padded shared row, in words (uint2)
+
+// One warp per (variable, pair-row d, word w): lane b handles i = 32 w + b.
+__global__ void kendall_masks_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
+                                     int64_t d0, int64_t drows, int64_t Wn,
+                                     uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  const int64_t per_var = drows * Wn;
+  const int64_t total = nvar * per_var;
+  for (int64_t t = warp; t < total; t += nwarps) {
+    const int64_t v = t / per_var;
+    const int64_t rem = t - v * per_var;
+    const int64_t dr = rem / Wn, w = rem - dr * Wn;
+    const int64_t d = d0 + dr + 1;
+    const int64_t i = 32 * w + lane;
+    bool valid = i < n && (2 * d < n || i < n / 2);
+    bool untied = false, greater = false;
+    if (valid) {
+      int64_t j = i + d;
+      if (j >= n) j -= n;
+      const float xi = X[v * n + i], xj = X[v * n + j];
+      untied = xj != xi;
+      greater = xj > xi;
+    }
+    const unsigned u = __ballot_sync(0xffffffffu, untied);
+    const unsigned g = __ballot_sync(0xffffffffu, greater);
+    if (lane == 0) {
+      M[v * per_var + rem] = make_uint2(u, g);
+      if (u) atomicAdd(&T[v], (unsigned long long)__popc(u));
+    }
+  }
+}
+
+// S[r*ld + c] += sum over words of popc(m) - 2 popc(m & (Gr ^ Gc)).
+// Rows r index MR (the Y set), columns c index MC (the X set).
+__global__ void __launch_bounds__(kKT)
+kendall_count_kernel(const uint2 *__restrict__ MR, int64_t nr, const uint2 *__restrict__ MC,
+                     int64_t nc, int64_t K, int64_t kchunk, int symmetric,
+                     unsigned long long *__restrict__ S, int64_t ld) {
+  constexpr int TM = 4, TN = 4, BM = 64, BN = 64;
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (symmetric && ti > tj) return;
+  const int64_t row0 = int64_t(ti) * BM, col0 = int64_t(tj) * BN;
+  const int64_t kbeg = int64_t(blockIdx.z) * kchunk;
+  const int64_t kend = min(K, kbeg + kchunk);
+  if (kbeg >= kend) return;
+
+  __shared__ __align__(16) uint2 sR[BM * kKLd];
+  __shared__ __align__(16) uint2 sC[BN * kKLd];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  unsigned both[TM][TN], disc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; i++)
+#pragma unroll
+    for (int j = 0; j < TN; j++) both[i][j] = disc[i][j] = 0u;
+
+  for (int64_t k0 = kbeg; k0 < kend; k0 += kKBK) {
+    // 64 rows x 16 words = 512 uint4 (two words each) per operand.
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const int q = threadIdx.x + s * kKT;
+      const int row = q >> 3, c2 = q & 7;
+      const int64_t gk = k0 + 2 * c2;
+      uint4 vr = make_uint4(0u, 0u, 0u, 0u), vc = make_uint4(0u, 0u, 0u, 0u);
+      const int64_t gr = row0 + row, gc = col0 + row;
+      if (gr < nr) {
+        if (gk < kend) { const uint2 w = MR[gr * K + gk]; vr.x = w.x; vr.y = w.y; }
+        if (gk + 1 < kend) { const uint2 w = MR[gr * K + gk + 1]; vr.z = w.x; vr.w = w.y; }
+      }
+      if (gc < nc) {
+        if (gk < kend) { const uint2 w = MC[gc * K + gk]; vc.x = w.x; vc.y = w.y; }
+        if (gk + 1 < kend) { const uint2 w = MC[gc * K + gk + 1]; vc.z = w.x; vc.w = w.y; }
+      }
+      *reinterpret_cast<uint4 *>(&sR[row * kKLd + 2 * c2]) = vr;
+      *reinterpret_cast<uint4 *>(&sC[row * kKLd + 2 * c2]) = vc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kKBK / 2; kk++) {
+      uint4 a[TM];
+#pragma unroll
+      for (int i = 0; i < TM; i++)
+        a[i] = *reinterpret_cast<const uint4 *>(&sR[(ty + 16 * i) * kKLd + 2 * kk]);
+#pragma unroll
+      for (int j = 0; j < TN; j++) {
+        const uint4 b = *reinterpret_cast<const uint4 *>(&sC[(tx + 16 * j) * kKLd + 2 * kk]);
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+          const unsigned m0 = a[i].x & b.x, m1 = a[i].z & b.z;
+          both[i][j] += __popc(m0) + __popc(m1);
+          disc[i][j] += __popc(m0 & (a[i].y ^ b.y)) + __popc(m1 & (a[i].w ^ b.w));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const bool mirror = symmetric && ti != tj;
+#pragma unroll
+  for (int i = 0; i < TM; i++) {
+    const int64_t r = row0 + ty + 16 * i;
+    if (r >= nr) continue;
+#pragma unroll
+    for (int j = 0; j < TN; j++) {
+      const int64_t c = col0 + tx + 16 * j;
+      if (c >= nc) continue;
+      const long long sv = (long long)both[i][j] - 2LL * (long long)disc[i][j];
+      atomicAdd(&S[r * ld + c], (unsigned long long)sv);
+      if (mirror) atomicAdd(&S[c * ld + r], (unsigned long long)sv);
+    }
+  }
+}
+
+// out[y*nx + x] = S / (sqrt(Tx) * sqrt(Ty)), clamped; R's evaluation order.
+__global__ void kendall_finish_kernel(const unsigned long long *__restrict__ S,
+                                      const unsigned long long *__restrict__ TX,
+                                      const unsigned long long *__restrict__ TY, int64_t nx,
+                                      int64_t ny, int same, double *__restrict__ out) {
+  const int64_t total = nx * ny;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t y = i / nx, x = i - y * nx;
+    double r;
+    if (same && x == y) {
+      r = 1.0;
+    } else {
+      const unsigned long long tx = TX[x], ty = TY[y];
+      if (tx == 0 || ty == 0) {
+        r = __longlong_as_double(0x7ff8000000000000LL);
+      } else {
+        const double s = double((long long)S[i]);
+        r = __ddiv_rn(s, __dmul_rn(__dsqrt_rn(double(tx)), __dsqrt_rn(double(ty))));
+        if (r > 1.0) r = 1.0;
+        if (r < -1.0) r = -1.0;
+      }
+    }
+    out[i] = r;
+  }
+}
+
+int grid_cap(int64_t work, int threads) {
+  const int64_t g = cdiv(work, threads);
+  const int64_t cap = int64_t(sm_count()) * 16;
+  return int(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+}  // namespace
+
+int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64_t n, int same,
+                 double *d_out, cudaStream_t s) {
+  if (nx == 0 || ny == 0) return GT_OK;
+  const int64_t Dr = n / 2;            // pair rows
+  const int64_t Wn = cdiv(n, 32);      // words per pair row
+  const int64_t nvar = same ? nx : nx + ny;
+  // Mask memory per pair row for all variables; chunk the rows to a budget.
+  const int64_t per_row = nvar * Wn * 8;
+  const int64_t budget = int64_t(2) << 30;
+  int64_t rows_chunk = per_row > 0 ? budget / per_row : Dr;
+  if (rows_chunk < 1) rows_chunk = 1;
+  if (rows_chunk > Dr) rows_chunk = Dr;
+
+  void *pS = nullptr, *pT = nullptr, *pM = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH0, size_t(nx) * size_t(ny) * 8, &pS));
+  GT_TRY(ws_get(WS_SCRATCH1, size_t(nvar) * 8, &pT));
+  auto *S = static_cast<unsigned long long *>(pS);
+  auto *T = static_cast<unsigned long long *>(pT);
+  GT_CUDA(cudaMemsetAsync(S, 0, size_t(nx) * size_t(ny) * 8, s));
+  GT_CUDA(cudaMemsetAsync(T, 0, size_t(nvar) * 8, s));
+  unsigned long long *TX = T, *TY = same ? T : T + nx;
+
+  if (Dr > 0) {
+    GT_TRY(ws_get(WS_SCRATCH2, size_t(nvar) * size_t(rows_chunk) * size_t(Wn) * 8, &pM));
+    uint2 *M = static_cast<uint2 *>(pM);
+    for (int64_t d0 = 0; d0 < Dr; d0 += rows_chunk) {
+      const int64_t dr = (Dr - d0 < rows_chunk) ? Dr - d0 : rows_chunk;
+      const int64_t K = dr * Wn;
+      uint2 *MXs = M, *MYs = same ? M : M + nx * K;
+      kendall_masks_kernel<<<grid_cap(nx * K * 32, 256), 256, 0, s>>>(dX, nx, n, d0, dr, Wn, MXs,
+                                                                     TX);
+      count_launch();
+      if (!same)
+        kendall_masks_kernel<<<grid_cap(ny * K * 32, 256), 256, 0, s>>>(dY, ny, n, d0, dr, Wn,
+                                                                       MYs, TY);
+      if (!same) count_launch();
+      const int64_t gy = cdiv(ny, 64), gx = cdiv(nx, 64);
+      if (gy > 65535 || gx > 2147483647LL) return fail(GT_EINVAL, "too many variables");
+      const int64_t tiles = same ? gx * (gx + 1) / 2 : gx * gy;
+      int64_t splits = cdiv(2 * sm_count(), tiles);
+      const int64_t max_splits = cdiv(K, 256);
+      if (splits > max_splits) splits = max_splits;
+      if (splits < 1) splits = 1;
+      if (splits > 65535) splits = 65535;
+      const int64_t kchunk = cdiv(cdiv(K, splits), kKBK) * kKBK;
+      splits = cdiv(K, kchunk);
+      dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)splits);
+      ProfScope prof("kendall_count", s);
+      kendall_count_kernel<<<grid, kKT, 0, s>>>(MYs, ny, MXs, nx, K, kchunk, same, S, nx);
+      count_launch();
+      GT_CUDA(cudaGetLastError());
+    }
+  }
+  kendall_finish_kernel<<<grid_cap(nx * ny, 256), 256, 0, s>>>(S, TX, TY, nx, ny, same, d_out);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+int kendall_check(int64_t nx, int64_t ny, int64_t n) {
+  if (nx < 0 || ny < 0 || n < 0) return fail(GT_EINVAL, "negative size");
+  if (n > 65536) return fail(GT_EINVAL, "kendall supports at most 65536 observations (n=%lld)",
+                             (long long)n);
+  return GT_OK;
+}
+
+int same_contents(const float *a, const float *b, int64_t count, bool *same, cudaStream_t s);
+
+}  // namespace gt
+
+extern "C" int gt_kendall_device(const float *d_X, int64_t nx, const float *d_Y, int64_t ny,
+                                 int64_t n, double *d_out, void *stream) {
+  gt::clear_error();
+  GT_TRY(gt::kendall_check(nx, ny, n));
+  if ((nx > 0 && !d_X) || (ny > 0 && !d_Y) || (nx * ny > 0 && !d_out))
+    return gt::fail(GT_EINVAL, "null device pointer");
+  const int same = (d_X == d_Y && nx == ny) ? 1 : 0;
+  return gt::kendall_impl(d_X, nx, d_Y, ny, n, same, d_out, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny, int64_t n,
+                          double *out) {
+  gt::clear_error();
+  GT_TRY(gt::kendall_check(nx, ny, n));
+  if (nx == 0 || ny == 0) return GT_OK;
+  if (!X || !Y || !out) return gt::fail(GT_EINVAL, "null host pointer");
+  cudaStream_t s = gt::lib_stream();
+  const size_t bx = size_t(nx) * size_t(n) * 4, by = size_t(ny) * size_t(n) * 4;
+  void *dX = nullptr, *dY = nullptr, *dO = nullptr;
+  GT_TRY(gt::ws_get(gt::WS_IN_A, bx, &dX));
+  GT_CUDA(cudaMemcpyAsync(dX, X, bx, cudaMemcpyHostToDevice, s));
+  bool same = (X == Y && nx == ny);
+  if (!same) {
+    GT_TRY(gt::ws_get(gt::WS_IN_B, by, &dY));
+    GT_CUDA(cudaMemcpyAsync(dY, Y, by, cudaMemcpyHostToDevice, s));
+    if (nx == ny)
+      GT_TRY(gt::same_contents(static_cast<float *>(dX), static_cast<float *>(dY), nx * n, &same, s));
+  }
+  if (same) dY = dX;
+  GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(nx) * size_t(ny) * 8, &dO));
+  GT_TRY(gt::kendall_impl(static_cast<float *>(dX), nx, static_cast<float *>(dY), ny, n,
+                          same ? 1 : 0, static_cast<double *>(dO), s));
+  GT_CUDA(cudaMemcpyAsync(out, dO, size_t(nx) * size_t(ny) * 8, cudaMemcpyDeviceToHost, s));
+  GT_CUDA(cudaStreamSynchronize(s));
+  return GT_OK;
+}

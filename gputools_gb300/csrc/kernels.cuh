@@ -1,0 +1,41 @@
+// kernels.cuh -- internal entry points shared between the translation units
+// of libgputools_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace gt {
+
+// distance.cu
+int dist_check_args(int64_t n, int64_t dim, int method, int layout);
+int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout, int method,
+              float p, cudaStream_t st);
+
+// euclid_tc.cu: Euclidean distances as a split-bf16 tcgen05 Gram contraction
+// with FP64 norms and an FP64 recomputation of near-zero distances.
+int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
+              cudaStream_t st);
+
+// Per-variable statistics of the Pearson prologue (FP64).
+struct ColStats {
+  double mean;
+  double inv_norm;  // 1 / sqrt(sum (x - mean)^2), or 0 for a constant variable
+  int flags;        // bit 0: contains NaN; bit 1: zero variance
+};
+
+// gram_tc.cu: C[r][c] = sum_k Z_r[k] * Z_c[k] for the normalised Pearson
+// operands on tcgen05 tensor cores, with the Pearson epilogue fused.
+struct PearsonOut {
+  float *corr, *ts, *pairs;
+  int64_t ld;       // leading dimension of the outputs (nB)
+  float npairs;     // value of `pairs` (everything mode: n)
+  int symmetric;
+};
+
+// Operands for the tensor-core path: for each variable, `nsplit` bf16 rows
+// (hi, lo[, lo2]) of length kpad (multiple of 64), zero padded.
+int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64_t kpad,
+               int nsplit, const PearsonOut &out, cudaStream_t st);
+
+}  // namespace gt

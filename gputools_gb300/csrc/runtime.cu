@@ -1,0 +1,212 @@
+// runtime.cu -- error reporting, per-device streams and workspace, device
+// selection.  The reference allocates and frees every device buffer per call
+// (src/distance.cpp:277-316, src/correlation.cpp:83-160,
+// src/kendall.cpp:13-55) and reports errors by longjmp-ing through R's
+// error() (src/cuseful.cpp:95-102), which leaks what was allocated.  Here
+// buffers are grow-only per-device slots reused across calls, and every
+// failure is a status code plus a thread-local message.
+#include "common.cuh"
+
+#include <cstdarg>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace gt {
+
+namespace {
+thread_local char t_err[1024] = {0};
+
+constexpr int kMaxDevices = 64;
+
+struct DeviceState {
+  cudaStream_t stream = nullptr;
+  void *slot[WS_NSLOTS] = {};
+  size_t bytes[WS_NSLOTS] = {};
+  int sms = 0;
+};
+
+std::mutex g_mu;
+DeviceState g_dev[kMaxDevices];
+std::atomic<unsigned long long> g_launches{0};
+}  // namespace
+
+void count_launch(int n) { g_launches.fetch_add((unsigned long long)n); }
+
+namespace {
+struct ProfRecord {
+  std::string name;
+  cudaEvent_t e0, e1;
+};
+std::atomic<int> g_prof_on{0};
+std::mutex g_prof_mu;
+std::vector<ProfRecord> g_prof_pending;
+struct ProfTotal {
+  std::string name;
+  double ms;
+  unsigned long long count;
+};
+std::vector<ProfTotal> g_prof_totals;
+
+void prof_drain_locked() {
+  for (auto &r : g_prof_pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.e1) == cudaSuccess && cudaEventElapsedTime(&ms, r.e0, r.e1) == cudaSuccess) {
+      bool found = false;
+      for (auto &t : g_prof_totals)
+        if (t.name == r.name) { t.ms += ms; t.count++; found = true; break; }
+      if (!found) g_prof_totals.push_back({r.name, double(ms), 1});
+    }
+    cudaEventDestroy(r.e0);
+    cudaEventDestroy(r.e1);
+  }
+  g_prof_pending.clear();
+}
+}  // namespace
+
+ProfScope::ProfScope(const char *name, cudaStream_t st) : name_(name), st_(st) {
+  if (!g_prof_on.load()) return;
+  if (cudaEventCreate(&e0_) != cudaSuccess) { e0_ = nullptr; return; }
+  cudaEventRecord(e0_, st_);
+}
+
+ProfScope::~ProfScope() {
+  if (!e0_) return;
+  cudaEvent_t e1 = nullptr;
+  if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0_); return; }
+  cudaEventRecord(e1, st_);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_pending.push_back({name_, e0_, e1});
+}
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_err, sizeof(t_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+void clear_error() { t_err[0] = 0; }
+const char *last_error() { return t_err; }
+
+int current_device(int *dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e != cudaSuccess)
+    return fail(GT_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+  if (*dev < 0 || *dev >= kMaxDevices)
+    return fail(GT_ENODEV, "device ordinal %d out of range", *dev);
+  return GT_OK;
+}
+
+cudaStream_t lib_stream() {
+  int dev = 0;
+  if (current_device(&dev) != GT_OK) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState &d = g_dev[dev];
+  if (!d.stream) cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking);
+  return d.stream;
+}
+
+int sm_count() {
+  int dev = 0;
+  if (current_device(&dev) != GT_OK) return 148;
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState &d = g_dev[dev];
+  if (!d.sms) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    d.sms = v > 0 ? v : 148;
+  }
+  return d.sms;
+}
+
+int ws_get(int slot, size_t bytes, void **ptr) {
+  if (slot < 0 || slot >= WS_NSLOTS) return fail(GT_EINVAL, "bad workspace slot");
+  int dev = 0;
+  GT_TRY(current_device(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState &d = g_dev[dev];
+  if (bytes == 0) bytes = 256;
+  if (d.bytes[slot] < bytes) {
+    if (d.slot[slot]) {
+      // The slot may still be read by work queued earlier on any stream.
+      cudaDeviceSynchronize();
+      cudaFree(d.slot[slot]);
+      d.slot[slot] = nullptr;
+      d.bytes[slot] = 0;
+    }
+    // Round up so that slowly growing requests do not reallocate each call.
+    size_t want = bytes + bytes / 8;
+    want = (want + (1u << 20) - 1) & ~size_t((1u << 20) - 1);
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GT_ENOMEM, "device workspace of %zu bytes unavailable: %s", want,
+                  cudaGetErrorString(e));
+    }
+    d.slot[slot] = p;
+    d.bytes[slot] = want;
+  }
+  *ptr = d.slot[slot];
+  return GT_OK;
+}
+
+void ws_release_all() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int cur = -1;
+  cudaGetDevice(&cur);
+  for (int dev = 0; dev < kMaxDevices; dev++) {
+    DeviceState &d = g_dev[dev];
+    bool any = false;
+    for (int s = 0; s < WS_NSLOTS; s++) any |= d.slot[s] != nullptr;
+    if (!any) continue;
+    cudaSetDevice(dev);
+    cudaDeviceSynchronize();
+    for (int s = 0; s < WS_NSLOTS; s++) {
+      if (d.slot[s]) cudaFree(d.slot[s]);
+      d.slot[s] = nullptr;
+      d.bytes[s] = 0;
+    }
+  }
+  if (cur >= 0) cudaSetDevice(cur);
+}
+
+}  // namespace gt
+
+extern "C" {
+
+const char *gt_last_error(void) { return gt::last_error(); }
+
+int gt_version(void) { return 10000; }
+
+uint64_t gt_kernel_launches(void) { return gt::g_launches.load(); }
+
+void gt_release_workspace(void) { gt::ws_release_all(); }
+
+void gt_profile_enable(int on) { gt::g_prof_on.store(on ? 1 : 0); }
+
+void gt_profile_reset(void) {
+  std::lock_guard<std::mutex> lk(gt::g_prof_mu);
+  gt::prof_drain_locked();
+  gt::g_prof_totals.clear();
+}
+
+int gt_profile_kernel_ms(const char *name, double *total_ms, uint64_t *launches) {
+  gt::clear_error();
+  if (!name) return gt::fail(GT_EINVAL, "null kernel name");
+  std::lock_guard<std::mutex> lk(gt::g_prof_mu);
+  gt::prof_drain_locked();
+  double ms = 0.0;
+  unsigned long long c = 0;
+  for (auto &t : gt::g_prof_totals)
+    if (t.name == name) { ms = t.ms; c = t.count; }
+  if (total_ms) *total_ms = ms;
+  if (launches) *launches = c;
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+/*
+ * gputools_gb300.h -- C ABI of libgputools_gb300.so, the GB300 (sm_103a)
+ * implementation of gputools' all-pairs hot path (gpuDist, gpuCor).
+ *
+ * Two layers:
+ *
+ *  1. The reference's own `.C` entry points, same names, argument order and
+ *     meaning, so R's `useDynLib` + `.C("Rdistances", ...)` etc. bind to this
+ *     library unchanged.  They are synchronous, take host buffers, and report
+ *     errors through R's error() when the library is loaded into R (resolved
+ *     weakly at run time, after every device buffer is released), otherwise
+ *     through gt_last_error().
+ *
+ *  2. gt_* functions that return a status code (GT_OK = 0) for non-R callers,
+ *     with host-buffer and device-buffer variants.  Device variants take raw
+ *     device pointers and a cudaStream_t (passed as void*, NULL = the legacy
+ *     default stream); they are asynchronous with respect to the host.
+ *
+ * Layouts (identical to the reference):
+ *   points        row-major N x D float32, one point per row
+ *                 (src/distance.h:10-26, R/gpuHclust.R:21-27 passes t(points)).
+ *   distances     N x N float32, d(x, y) at [y*N + x], symmetric, zero
+ *                 diagonal (src/distance.h:15-17); or, GT_LAYOUT_DIST, R's
+ *                 `dist` vector: the strict lower triangle by columns,
+ *                 entry (i > j) at n*j - j*(j+1)/2 + i - j - 1.
+ *   correlation   inputs variable-contiguous: variable x occupies
+ *                 A[x*n .. x*n + n-1] (R's column-major n x p matrix);
+ *                 Pearson outputs at [x*nB + y] (inst/cuda/correlation.cu:149);
+ *                 Kendall output at [y*nx + x] (inst/cuda/kendall.cu:45).
+ */
+#ifndef GPUTOOLS_GB300_H
+#define GPUTOOLS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GT_OK 0
+#define GT_EINVAL 1      /* bad argument (size, method name, pointer)        */
+#define GT_ECUDA 2       /* a CUDA runtime call failed                       */
+#define GT_ENOMEM 3      /* device workspace could not be allocated          */
+#define GT_ENODEV 4      /* no usable CUDA device                            */
+#define GT_ETIMEOUT 5    /* a bounded device-side wait gave up               */
+#define GT_EUNSUPPORTED 6 /* valid request this build does not support       */
+
+/* ---- enums -------------------------------------------------------------- */
+/* src/distance.h:5-8 dist_method, same order. */
+enum gt_dist_method {
+  GT_EUCLIDEAN = 0, GT_MAXIMUM = 1, GT_MANHATTAN = 2,
+  GT_CANBERRA = 3, GT_BINARY = 4, GT_MINKOWSKI = 5
+};
+/* src/correlation.h:1 UseObs, same values as rpmcc's whichObs. */
+enum gt_use_obs { GT_EVERYTHING = 0, GT_PAIRWISE_COMPLETE = 1 };
+enum gt_layout { GT_LAYOUT_FULL = 0, GT_LAYOUT_DIST = 1 };
+/* How Pearson and Euclidean Gram contractions are evaluated. */
+enum gt_gram_path {
+  GT_GRAM_TC_BF16X3 = 0, /* tcgen05, each operand split hi+lo bf16, 3 products */
+  GT_GRAM_TC_BF16X6 = 1, /* tcgen05, 3-way bf16 split, 6 products             */
+  GT_GRAM_FP32 = 2       /* plain FP32 CUDA-core path                         */
+};
+
+/* ======================================================================== *
+ * 1. The reference's .C entry points                                        *
+ * ======================================================================== */
+
+/* Replaces src/rinterface.cpp:206-214 (declared src/rinterface.h:53-55).
+ * d(x,y) for every pair of rows of `points` (numPoints x dim, row-major) into
+ * `distances` (numPoints^2, [y*N + x]).  method: "euclidean", "maximum",
+ * "manhattan", "canberra", "binary", "minkowski"; any other string means
+ * euclidean, as src/rinterface.cpp:147-156 getDistEnum does.  p is the
+ * Minkowski power. */
+void Rdistances(const float *points, const int *numPoints, const int *dim,
+                float *distances, const char **method, const float *p);
+
+/* Replaces src/rinterface.cpp:33-55 (declared src/rinterface.h:4-8).
+ * whichObs 0 = "everything", 1 = "pairwise.complete.obs"; any other value is
+ * an error ("unknown use method").  For every pair (x in A, y in B):
+ * numPairs, correlations (Pearson r) and signifs (t-score, 10000 when
+ * r >= 0.999, src/correlation.cpp:51-64) at [x*numSamplesB + y]. */
+void rpmcc(const int *whichObs, const float *samplesA, const int *numSamplesA,
+           const float *samplesB, const int *numSamplesB,
+           const int *sampleSize, float *numPairs, float *correlations,
+           float *signifs);
+
+/* Replaces src/rinterface.cpp:128-132 (declared src/rinterface.h:41-42).
+ * Kendall's tau-b (R's cor(method = "kendall")) for every pair (x in X,
+ * y in Y) at answers[y*nx + x], from exact integer pair counts. */
+void RgpuKendall(const float *X, const int *nx, const float *Y, const int *ny,
+                 const int *sampleSize, double *answers);
+
+/* Replace src/rinterface.cpp:79-85 (declared src/rinterface.h:23-24). */
+void rsetDevice(const int *device);
+void rgetDevice(int *device);
+
+/* Replaces src/rinterface.cpp:87-91 (R/gpuCor.R:64-74 gpuTtest):
+ * ts[i] = coeffs[i] * sqrt((pairs[i] - 2) / (1 - coeffs[i]^2)). */
+void rtestT(const float *pairs, const float *coeffs, const int *n, float *ts);
+
+/* Replace src/cudaUtils.cpp:118-165 and :167-195.  The reference compiles its
+ * kernels with NVRTC when R loads the package (R/zzz.R:1-39); this library's
+ * kernels are compiled ahead of time for sm_103a, so cuCompile only checks
+ * that a device is present and unloadPackage frees the cached workspace. */
+void cuCompile(const int *numFiles, const char **cuFilenames,
+               const char **cuSrc);
+void unloadPackage(void);
+
+/* ======================================================================== *
+ * 2. Status-returning API                                                   *
+ * ======================================================================== */
+
+/* Message of the calling thread's last failure ("" if none). */
+const char *gt_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int gt_version(void);
+/* Frees the device workspace of every device this thread touched. */
+void gt_release_workspace(void);
+/* Number of CUDA kernels this library has launched in this process (a
+ * monotone counter, for measuring how many launches a call makes). */
+uint64_t gt_kernel_launches(void);
+
+/* Kernel timing with CUDA events recorded on the launching stream around the
+ * library's main kernels ("pearson_gram", "euclid_gram", "dist", "kendall_count",
+ * ...).  Enabling adds two event records per timed launch.
+ * gt_profile_kernel_ms waits for the recorded events and returns the summed
+ * duration and the number of launches of `name` since the last reset. */
+void gt_profile_enable(int on);
+void gt_profile_reset(void);
+int gt_profile_kernel_ms(const char *name, double *total_ms, uint64_t *launches);
+
+/* Select the evaluation of Pearson / Euclidean Gram contractions
+ * (enum gt_gram_path) for calls made afterwards by this process. */
+int gt_set_gram_path(int path);
+int gt_get_gram_path(void);
+
+/* Host buffers, synchronous.  Same result as Rdistances. */
+int gt_distances(const float *points, int64_t n, int64_t dim, float *out,
+                 int method, float p);
+
+/* Device buffers, asynchronous on `stream`.  layout = enum gt_layout;
+ * GT_LAYOUT_FULL writes n*n floats, GT_LAYOUT_DIST n*(n-1)/2. */
+int gt_distances_device(const float *d_points, int64_t n, int64_t dim,
+                        float *d_out, int layout, int method, float p,
+                        void *stream);
+
+/* Host buffers, synchronous.  Same result as rpmcc; any output may be NULL. */
+int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int64_t nB,
+            int64_t n, float *pairs, float *corr, float *ts);
+
+/* Device buffers.  d_B == d_A (same pointer) marks the symmetric problem
+ * cor(x), computed once per unordered pair and mirrored. */
+int gt_pmcc_device(int use, const float *d_A, int64_t nA, const float *d_B,
+                   int64_t nB, int64_t n, float *d_pairs, float *d_corr,
+                   float *d_ts, void *stream);
+
+/* Host buffers, synchronous.  Same result as RgpuKendall. */
+int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
+               int64_t n, double *out);
+
+/* Device buffers; d_Y == d_X marks cor(x) (diagonal exactly 1). */
+int gt_kendall_device(const float *d_X, int64_t nx, const float *d_Y,
+                      int64_t ny, int64_t n, double *d_out, void *stream);
+
+/* Device buffers: t-scores as rtestT. */
+int gt_ttest_device(const float *d_pairs, const float *d_coeffs, int64_t n,
+                    float *d_ts, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUTOOLS_GB300_H */

@@ -1,0 +1,232 @@
+"""FP64 CPU oracle for gputools' all-pairs statistics.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, bench.py's CPU-baseline leg (and its
+``--impl reference`` arm) and ``__graft_entry__.smoke()`` may import this
+package, and only as the checker or the CPU baseline.  The shipped library
+(`gputools_gb300`) never imports, links or calls it.
+
+Two back ends:
+
+* ``liboracle.so`` -- ``oracle.c``, a double-precision restatement of R's
+  ``stats::dist`` / ``stats::cor`` semantics as gputools exposes them (see
+  ``oracle.h`` for the reference lines each function follows).
+* ``_ref/libref_cpu.so`` -- the reference's own CPU loops compiled straight
+  from the reference tree by ``build_ref.sh`` (``distance_host`` in
+  src/distance.cpp:174-207, ``hostKendall``/``permHostKendall`` in
+  src/correlation.cpp:488-516, ``hostSignif`` in src/correlation.cpp:51-64).
+  It exists only where the reference tree is present; it pins the
+  restatement (tests/test_oracle.py) and generated tests/golden/.
+
+Parity pinning: the reference ships no tests or golden vectors, so the oracle
+is pinned (a) against the reference's own CPU loops (float32 arithmetic, so to
+float32 tolerance) and the committed fixtures made from them, and (b) against
+scipy / numpy implementations of the same R definitions.  R itself is not
+available, so R's last-bit behaviour (Kendall tau-b evaluation order) is
+restated, not run.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_cpu.so")
+
+METHODS = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.c (gcc, -O3, OpenMP) into _build/liboracle.so, and the
+    reference CPU loops into _ref/ when the reference tree is present."""
+    src = os.path.join(HERE, "oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        os.makedirs(BUILD, exist_ok=True)
+        subprocess.check_call(
+            ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11", "-Wall",
+             "-o", LIB, src, "-lm"])
+    ref_script = os.path.join(HERE, "build_ref.sh")
+    if (force or not os.path.exists(REF_LIB)) and os.path.isdir(
+            os.environ.get("GPUTOOLS_REFERENCE", "/root/reference")):
+        subprocess.check_call(["bash", ref_script])
+    return LIB
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = ctypes.CDLL(LIB)
+        i64, dp, fp = ctypes.c_int64, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+        lib.orc_dist.argtypes = [fp, i64, fp, i64, i64, ctypes.c_int, ctypes.c_double, fp]
+        lib.orc_pearson.argtypes = [ctypes.c_int, fp, i64, fp, i64, i64, fp, fp, fp]
+        lib.orc_kendall.argtypes = [fp, i64, fp, i64, i64, ctypes.c_int, fp, fp, fp, fp]
+        lib.orc_ttest.argtypes = [fp, fp, i64, fp]
+        lib.orc_signif.argtypes = [fp, fp, i64, fp]
+        lib.orc_set_threads.argtypes = [ctypes.c_int]
+        lib.orc_get_threads.restype = ctypes.c_int
+        del dp
+        _lib = lib
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _ref_lib():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("reference CPU build missing: run oracle/build_ref.sh "
+                               "where the reference tree is present")
+        _ref = ctypes.CDLL(REF_LIB)
+    return _ref
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    _load().orc_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(_load().orc_get_threads())
+
+
+def method_index(method: str) -> int:
+    return METHODS.index(method)
+
+
+def dist(a: np.ndarray, method: str = "euclidean", p: float = 2.0,
+         b: Optional[np.ndarray] = None) -> np.ndarray:
+    """Distances between the rows of ``a`` (and ``b``; default ``a``).
+
+    Returns D with D[y, x] = d(a_x, b_y), float64 (the reference layout
+    d[y*N + x])."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = a if b is None else np.ascontiguousarray(b, dtype=np.float32)
+    if a.ndim != 2 or b.ndim != 2 or a.shape[1] != b.shape[1]:
+        raise ValueError("points must be 2-D with equal dimension")
+    out = np.empty((b.shape[0], a.shape[0]), dtype=np.float64)
+    rc = _load().orc_dist(_ptr(a), a.shape[0], _ptr(b), b.shape[0], a.shape[1],
+                          method_index(method), float(p), _ptr(out))
+    if rc != 0:
+        raise ValueError(f"orc_dist failed ({rc})")
+    return out
+
+
+def pearson(A: np.ndarray, B: Optional[np.ndarray] = None, use: int = 0):
+    """Pearson r for every pair of variables.
+
+    ``A`` is (na, n): one variable per row, observations contiguous (the
+    reference's A[x*n + k]).  Returns (corr, pairs, ts), each (na, nb) with
+    [x, y] the pair (A_x, B_y)."""
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = A if B is None else np.ascontiguousarray(B, dtype=np.float32)
+    na, n = A.shape
+    nb = B.shape[0]
+    if B.shape[1] != n:
+        raise ValueError("A and B need the same number of observations")
+    corr = np.empty((na, nb)); pairs = np.empty((na, nb)); ts = np.empty((na, nb))
+    rc = _load().orc_pearson(int(use), _ptr(A), na, _ptr(B), nb, n, _ptr(corr),
+                             _ptr(pairs), _ptr(ts))
+    if rc != 0:
+        raise ValueError(f"orc_pearson failed ({rc})")
+    return corr, pairs, ts
+
+
+def kendall(X: np.ndarray, Y: Optional[np.ndarray] = None, same: Optional[bool] = None):
+    """Kendall tau-b for every pair of variables; X is (nx, n), Y (ny, n).
+
+    Returns (tau, S, Tx, Ty), each shaped (ny, nx) -- the reference's
+    results[y*nx + x] layout."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    if same is None:
+        same = Y is None
+    Y = X if Y is None else np.ascontiguousarray(Y, dtype=np.float32)
+    nx, n = X.shape
+    ny = Y.shape[0]
+    tau = np.empty((ny, nx)); S = np.empty((ny, nx), np.int64)
+    Tx = np.empty((ny, nx), np.int64); Ty = np.empty((ny, nx), np.int64)
+    rc = _load().orc_kendall(_ptr(X), nx, _ptr(Y), ny, n, int(bool(same)), _ptr(tau),
+                             _ptr(S), _ptr(Tx), _ptr(Ty))
+    if rc != 0:
+        raise ValueError(f"orc_kendall failed ({rc})")
+    return tau, S, Tx, Ty
+
+
+def ttest(pairs: np.ndarray, r: np.ndarray) -> np.ndarray:
+    pairs = np.ascontiguousarray(pairs, np.float64); r = np.ascontiguousarray(r, np.float64)
+    out = np.empty_like(r)
+    _load().orc_ttest(_ptr(pairs), _ptr(r), r.size, _ptr(out))
+    return out
+
+
+def signif(pairs: np.ndarray, r: np.ndarray) -> np.ndarray:
+    pairs = np.ascontiguousarray(pairs, np.float64); r = np.ascontiguousarray(r, np.float64)
+    out = np.empty_like(r)
+    _load().orc_signif(_ptr(pairs), _ptr(r), r.size, _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's own CPU loops (float32), for pinning the restatement.
+
+def ref_distance_host(points: np.ndarray, method: str = "euclidean", p: float = 2.0) -> np.ndarray:
+    """src/distance.cpp:174-207 ``distance_host`` on the rows of ``points``.
+
+    That function writes d[y*dim + x] (its row stride is the dimension, not
+    n_a), so it is called once per y with n_b = 1, where the stride is
+    irrelevant.  Returns (N, N) float32 with [y, x] = d(x, y)."""
+    lib = _ref_lib()
+    fn = lib._Z13distance_hostPKfmmS0_mmmPfm11dist_methodf
+    sz = ctypes.c_size_t
+    fn.argtypes = [ctypes.c_void_p, sz, sz, ctypes.c_void_p, sz, sz, sz, ctypes.c_void_p,
+                   sz, ctypes.c_int, ctypes.c_float]
+    pts = np.ascontiguousarray(points, np.float32)
+    N, D = pts.shape
+    out = np.empty((N, N), np.float32)
+    row = np.empty(max(N, D), np.float32)
+    for y in range(N):
+        fn(_ptr(pts), D * 4, N, pts[y:y + 1].ctypes.data_as(ctypes.c_void_p), D * 4, 1, D,
+           _ptr(row), N * 4, method_index(method), float(p))
+        out[y] = row[:N]
+    return out
+
+
+def ref_host_kendall(X: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """src/correlation.cpp:506-516 ``permHostKendall`` (the reference's tau-a
+    variant, float counters).  Returns (ny, nx) with [y, x]."""
+    lib = _ref_lib()
+    fn = lib._Z15permHostKendallPKfmS0_mmPd
+    sz = ctypes.c_size_t
+    fn.argtypes = [ctypes.c_void_p, sz, ctypes.c_void_p, sz, sz, ctypes.c_void_p]
+    X = np.ascontiguousarray(X, np.float32); Y = np.ascontiguousarray(Y, np.float32)
+    nx, n = X.shape
+    ny = Y.shape[0]
+    out = np.empty((ny, nx), np.float64)
+    fn(_ptr(X), nx, _ptr(Y), ny, n, _ptr(out))
+    return out
+
+
+def ref_host_signif(pairs: np.ndarray, r: np.ndarray) -> np.ndarray:
+    """src/correlation.cpp:51-64 ``hostSignif`` (float32)."""
+    lib = _ref_lib()
+    fn = lib._Z10hostSignifPKfS0_mPf
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    pairs = np.ascontiguousarray(pairs, np.float32); r = np.ascontiguousarray(r, np.float32)
+    out = np.empty(r.shape, np.float32)
+    fn(_ptr(pairs), _ptr(r), r.size, _ptr(out))
+    return out

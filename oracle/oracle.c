@@ -1,0 +1,251 @@
+/*
+ * oracle.c -- FP64 CPU restatement of gputools' all-pairs statistics.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, by bench.py's CPU-baseline leg and
+ * by __graft_entry__.smoke() as the checker.  The shipped library never links
+ * or calls it.  See oracle.h for the semantics and the reference lines each
+ * function follows.
+ *
+ * Sums use Neumaier compensation so the oracle is accurate to a few ulp of
+ * double, far below the float32 tolerances the CUDA path is held to.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 0;
+
+void orc_set_threads(int nthreads) { g_threads = nthreads; }
+
+int orc_get_threads(void) {
+#ifdef _OPENMP
+  return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* Neumaier-compensated accumulator. */
+typedef struct { double s, c; } ksum;
+static inline void ks_add(ksum *k, double v) {
+  double t = k->s + v;
+  if (!isfinite(t)) { k->s = t; return; }  /* Inf/NaN: no compensation */
+  if (fabs(k->s) >= fabs(v)) k->c += (k->s - t) + v;
+  else k->c += (v - t) + k->s;
+  k->s = t;
+}
+static inline double ks_val(const ksum *k) { return k->s + k->c; }
+
+/* ---------------------------------------------------------------- dist --- */
+
+/* One distance between two float32 vectors of length dim, in double.
+ * euclidean  sqrt(sum (a-b)^2)              distance.cu:40-78
+ * maximum    max |a-b|                      distance.cu:116-154
+ * manhattan  sum |a-b|                      distance.cu:192-232
+ * canberra   sum |a-b|/|a+b|                distance.cu:273-316; terms with
+ *            a zero numerator and zero denominator are omitted and the sum is
+ *            scaled by dim/used (R ?dist); no term used -> NaN.
+ * binary     #(on xor) / #(on or), 0 when no bit is on  distance.cu:366-415
+ * minkowski  (sum |a-b|^p)^(1/p)            distance.cu:453-493
+ */
+static double dist1(const float *a, const float *b, int64_t dim, int method,
+                    double p) {
+  ksum acc = {0.0, 0.0};
+  switch (method) {
+  case ORC_EUCLIDEAN:
+    for (int64_t k = 0; k < dim; k++) {
+      double t = (double)a[k] - (double)b[k];
+      ks_add(&acc, t * t);
+    }
+    return sqrt(ks_val(&acc));
+  case ORC_MAXIMUM: {
+    double m = 0.0;
+    for (int64_t k = 0; k < dim; k++) {
+      double t = fabs((double)a[k] - (double)b[k]);
+      if (t > m) m = t;
+    }
+    return m;
+  }
+  case ORC_MANHATTAN:
+    for (int64_t k = 0; k < dim; k++)
+      ks_add(&acc, fabs((double)a[k] - (double)b[k]));
+    return ks_val(&acc);
+  case ORC_CANBERRA: {
+    int64_t used = 0;
+    for (int64_t k = 0; k < dim; k++) {
+      double num = fabs((double)a[k] - (double)b[k]);
+      double den = fabs((double)a[k] + (double)b[k]);
+      if (num == 0.0 && den == 0.0) continue;
+      ks_add(&acc, num / den);
+      used++;
+    }
+    if (used == 0) return NAN;
+    double s = ks_val(&acc);
+    if (used < dim) s = s / ((double)used / (double)dim);
+    return s;
+  }
+  case ORC_BINARY: {
+    int64_t either = 0, onlyone = 0;
+    for (int64_t k = 0; k < dim; k++) {
+      int x = a[k] != 0.0f, y = b[k] != 0.0f;
+      either += (x | y);
+      onlyone += (x ^ y);
+    }
+    return either ? (double)onlyone / (double)either : 0.0;
+  }
+  case ORC_MINKOWSKI:
+    for (int64_t k = 0; k < dim; k++)
+      ks_add(&acc, pow(fabs((double)a[k] - (double)b[k]), p));
+    return pow(ks_val(&acc), 1.0 / p);
+  default:
+    return NAN;
+  }
+}
+
+int orc_dist(const float *a, int64_t na, const float *b, int64_t nb,
+             int64_t dim, int method, double p, double *out) {
+  if (method < ORC_EUCLIDEAN || method > ORC_MINKOWSKI) return -1;
+  if (na < 0 || nb < 0 || dim < 0) return -2;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(orc_get_threads())
+  for (int64_t y = 0; y < nb; y++)
+    for (int64_t x = 0; x < na; x++)
+      out[y * na + x] = dist1(a + x * dim, b + y * dim, dim, method, p);
+  return 0;
+}
+
+/* ------------------------------------------------------------- pearson --- */
+
+/* r, and the pair count, for one pair of variables.
+ * everything  (correlation.cu:152-292 NoTest kernels): every observation is
+ *             used, any NaN makes r NaN, pairs = n.
+ * pairwise    (correlation.cu:7-150): observations where either value is NaN
+ *             are dropped; pairs = the number kept; fewer than 2 -> NaN.
+ * Two-pass: means first, then centred second moments, all in double.  A zero
+ * variance gives NaN (R returns NA for it). */
+static double pearson1(int use, const float *x, const float *y, int64_t n,
+                       double *npairs) {
+  ksum sx = {0, 0}, sy = {0, 0};
+  int64_t cnt = 0;
+  int has_nan = 0;
+  for (int64_t k = 0; k < n; k++) {
+    double a = x[k], b = y[k];
+    if (isnan(a) || isnan(b)) {
+      has_nan = 1;
+      if (use == 1) continue;
+    }
+    ks_add(&sx, a);
+    ks_add(&sy, b);
+    cnt++;
+  }
+  if (use == 0) {
+    *npairs = (double)n;
+    if (has_nan) return NAN;
+  } else {
+    *npairs = (double)cnt;
+  }
+  if (cnt < 2) return NAN;
+  double mx = ks_val(&sx) / (double)cnt, my = ks_val(&sy) / (double)cnt;
+  ksum sxx = {0, 0}, syy = {0, 0}, sxy = {0, 0};
+  for (int64_t k = 0; k < n; k++) {
+    double a = x[k], b = y[k];
+    if (isnan(a) || isnan(b)) continue;
+    double da = a - mx, db = b - my;
+    ks_add(&sxx, da * da);
+    ks_add(&syy, db * db);
+    ks_add(&sxy, da * db);
+  }
+  double vx = ks_val(&sxx), vy = ks_val(&syy);
+  if (vx == 0.0 || vy == 0.0) return NAN;
+  double r = ks_val(&sxy) / (sqrt(vx) * sqrt(vy));
+  if (r > 1.0) r = 1.0;
+  if (r < -1.0) r = -1.0;
+  return r;
+}
+
+int orc_pearson(int use, const float *A, int64_t na, const float *B,
+                int64_t nb, int64_t n, double *corr, double *pairs,
+                double *ts) {
+  if (use != 0 && use != 1) return -1;
+  if (na < 0 || nb < 0 || n < 0) return -2;
+#pragma omp parallel for collapse(2) schedule(dynamic, 64) num_threads(orc_get_threads())
+  for (int64_t x = 0; x < na; x++) {
+    for (int64_t y = 0; y < nb; y++) {
+      double np;
+      double r = pearson1(use, A + x * n, B + y * n, n, &np);
+      int64_t o = x * nb + y;
+      if (corr) corr[o] = r;
+      if (pairs) pairs[o] = np;
+      if (ts) orc_signif(&np, &r, 1, ts + o);
+    }
+  }
+  return 0;
+}
+
+void orc_ttest(const double *pairs, const double *r, int64_t len,
+               double *out) {
+  for (int64_t i = 0; i < len; i++)
+    out[i] = r[i] * sqrt((pairs[i] - 2.0) / (1.0 - r[i] * r[i]));
+}
+
+/* src/correlation.cpp:51-64: r at or above 0.999 reports the sentinel 10000. */
+void orc_signif(const double *pairs, const double *r, int64_t len,
+                double *out) {
+  for (int64_t i = 0; i < len; i++) {
+    if (r[i] >= 0.999) out[i] = 10000.0;
+    else out[i] = r[i] * sqrt((pairs[i] - 2.0) / (1.0 - r[i] * r[i]));
+  }
+}
+
+/* ------------------------------------------------------------- kendall --- */
+
+static inline int sgn(float a, float b) { return (b > a) - (b < a); }
+
+/* S = sum_{i<j} sign(x_j - x_i) sign(y_j - y_i); Tx, Ty = untied pairs. */
+static void kendall_counts(const float *x, const float *y, int64_t n,
+                           int64_t *S, int64_t *Tx, int64_t *Ty) {
+  int64_t s = 0, tx = 0, ty = 0;
+  for (int64_t i = 0; i < n; i++) {
+    for (int64_t j = i + 1; j < n; j++) {
+      int a = sgn(x[i], x[j]), b = sgn(y[i], y[j]);
+      s += a * b;
+      tx += a * a;
+      ty += b * b;
+    }
+  }
+  *S = s;
+  *Tx = tx;
+  *Ty = ty;
+}
+
+/* tau-b exactly as R evaluates it: S / (sqrt(Tx) * sqrt(Ty)), clamped. */
+static double taub(int64_t S, int64_t Tx, int64_t Ty) {
+  if (Tx == 0 || Ty == 0) return NAN;
+  double r = (double)S / (sqrt((double)Tx) * sqrt((double)Ty));
+  if (r > 1.0) r = 1.0;
+  if (r < -1.0) r = -1.0;
+  return r;
+}
+
+int orc_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
+                int64_t n, int same, double *out, int64_t *S, int64_t *Tx,
+                int64_t *Ty) {
+  if (nx < 0 || ny < 0 || n < 0) return -2;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(orc_get_threads())
+  for (int64_t y = 0; y < ny; y++) {
+    for (int64_t x = 0; x < nx; x++) {
+      int64_t s, tx, ty;
+      kendall_counts(X + x * n, Y + y * n, n, &s, &tx, &ty);
+      int64_t o = y * nx + x;
+      if (S) S[o] = s;
+      if (Tx) Tx[o] = tx;
+      if (Ty) Ty[o] = ty;
+      if (out) out[o] = (same && x == y) ? 1.0 : taub(s, tx, ty);
+    }
+  }
+  return 0;
+}

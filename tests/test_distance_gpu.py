@@ -1,0 +1,141 @@
+"""gpuDist parity: the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances are float32-level: every metric is accumulated in float32 over at
+most a few hundred terms, so the relative error bound used is 2e-5
+(|gpu - oracle| <= 2e-5 * max(|oracle|, 1e-3)); binary counts are exact and
+only the final division rounds.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
+RTOL = 2e-5
+
+
+def rdistances(lib, pts, method, p=2.0):
+    pts = np.ascontiguousarray(pts, np.float32)
+    n, d = pts.shape
+    out = np.full((n, n), np.nan, np.float32)
+    N, D = ctypes.c_int(n), ctypes.c_int(d)
+    m = ctypes.c_char_p(method.encode())
+    pf = ctypes.c_float(p)
+    lib.Rdistances(pts.ctypes.data_as(ctypes.c_void_p), ctypes.byref(N), ctypes.byref(D),
+                   out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(m), ctypes.byref(pf))
+    err = lib.gt_last_error().decode()
+    assert err == "", err
+    return out
+
+
+def check_close(got, want, rtol=RTOL):
+    got = np.asarray(got, np.float64)
+    assert got.shape == want.shape
+    nan_g, nan_w = np.isnan(got), np.isnan(want)
+    assert np.array_equal(nan_g, nan_w)
+    inf_g, inf_w = np.isinf(got), np.isinf(want)
+    assert np.array_equal(inf_g, inf_w)
+    ok = ~(nan_w | inf_w)
+    err = np.abs(got[ok] - want[ok]) / np.maximum(np.abs(want[ok]), 1e-3)
+    assert err.size == 0 or err.max() <= rtol, float(err.max())
+
+
+def data_for(method, n, d, rng):
+    if method == "binary":
+        return (rng.random((n, d)) < 0.3).astype(np.float32)
+    return rng.standard_normal((n, d)).astype(np.float32)
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("n,d", [(1, 3), (2, 1), (5, 10), (37, 13), (130, 7), (300, 64),
+                                 (257, 100)])
+def test_rdistances_vs_oracle(gpu, oracle_mod, rng, method, n, d):
+    pts = data_for(method, n, d, rng)
+    p = 3.0 if method == "minkowski" else 2.0
+    got = rdistances(gpu, pts, method, p)
+    want = oracle_mod.dist(pts, method, p)
+    np.fill_diagonal(want, 0.0)  # the reference writes 0 on the diagonal
+    check_close(got, want)
+    assert np.array_equal(got, got.T)
+
+
+@pytest.mark.parametrize("p", [1.0, 2.0, 3.0, 4.0, 2.5, 0.5])
+def test_minkowski_powers(gpu, oracle_mod, rng, p):
+    pts = rng.standard_normal((70, 9)).astype(np.float32)
+    got = rdistances(gpu, pts, "minkowski", p)
+    want = oracle_mod.dist(pts, "minkowski", p)
+    np.fill_diagonal(want, 0.0)
+    check_close(got, want, rtol=5e-5)
+
+
+def test_canberra_zero_terms_follow_R(gpu, oracle_mod, rng):
+    pts = rng.standard_normal((40, 12)).astype(np.float32)
+    pts[rng.random(pts.shape) < 0.4] = 0.0
+    pts[3] = 0.0                       # all-zero rows: no usable term -> NaN
+    pts[4] = 0.0
+    pts[5, :6] = -pts[6, :6]           # a = -b != 0 -> infinite term
+    got = rdistances(gpu, pts, "canberra")
+    want = oracle_mod.dist(pts, "canberra")
+    np.fill_diagonal(want, 0.0)
+    check_close(got, want)
+    assert np.isnan(got[3, 4]) and np.isinf(got[5, 6])
+
+
+def test_unknown_method_string_means_euclidean(gpu, oracle_mod, rng):
+    pts = rng.standard_normal((20, 4)).astype(np.float32)
+    got = rdistances(gpu, pts, "dot")
+    want = oracle_mod.dist(pts, "euclidean")
+    check_close(got, want)
+
+
+def test_duplicates_are_exactly_zero(gpu, rng):
+    pts = rng.standard_normal((50, 16)).astype(np.float32)
+    pts[10] = pts[20]
+    for m in METHODS:
+        got = rdistances(gpu, pts, m, 3.0)
+        if m == "binary":
+            continue
+        assert got[10, 20] == 0.0 and got[20, 10] == 0.0, m
+
+
+def test_cfg_4000x100_rows_sampled(gpu, oracle_mod, rng):
+    """The 4000 x 100 configuration, every method, checked on sampled rows."""
+    base = rng.standard_normal((4000, 100)).astype(np.float32)
+    bern = (rng.random((4000, 100)) < 0.3).astype(np.float32)
+    rows = rng.choice(4000, 24, replace=False)
+    for m in METHODS:
+        pts = bern if m == "binary" else base
+        p = 3.0 if m == "minkowski" else 2.0
+        got = rdistances(gpu, pts, m, p)
+        want = oracle_mod.dist(pts, m, p, b=pts[rows])  # [k, x] = d(x, rows[k])
+        want[np.arange(len(rows)), rows] = 0.0
+        check_close(got[rows], want)
+
+
+def test_device_layouts_agree(gpu, rng):
+    import torch
+    import gputools_gb300 as g
+    pts = torch.from_numpy(rng.standard_normal((333, 24)).astype(np.float32)).cuda()
+    for m in ("euclidean", "manhattan", "canberra"):
+        full = g.distances_device(pts, m, layout="full").view(333, 333).cpu().numpy()
+        cond = g.distances_device(pts, m, layout="dist").cpu().numpy()
+        cols, rows = np.triu_indices(333, 1)
+        assert np.array_equal(cond, full[cols, rows]), m
+    torch.cuda.synchronize()
+
+
+def test_gpuDist_api_matches_oracle(gpu, oracle_mod, rng):
+    import gputools_gb300 as g
+    pts = rng.random((5, 10))  # man/gpuDist.Rd example shape
+    for m in ("euclidean", "maximum", "manhattan"):
+        d = g.gpuDist(pts, m)
+        want = oracle_mod.dist(pts.astype(np.float32), m)
+        cols, rows = np.triu_indices(5, 1)
+        np.testing.assert_allclose(d.values, want[cols, rows], rtol=RTOL)
+        assert d.method == m and d.size == 5
+    d = g.gpuDist(pts, "minkowski", 4)
+    assert d.p == 4
+    d = g.gpuDist(pts, "euclidian")
+    assert d.method == "euclidean"

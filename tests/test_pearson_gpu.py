@@ -1,0 +1,169 @@
+"""gpuCor(method = "pearson") parity through the C ABI (rpmcc, gt_pmcc,
+gt_pmcc_device) against the FP64 oracle.
+
+Error metric: absolute error of r (r is already scale free, |r| <= 1).
+Tolerances, per Gram evaluation:
+  fp32    2e-6 * sqrt(n / 100) + 1e-6   (float32 accumulation of n products)
+  bf16x6  same as fp32                  (3-way bf16 split: float32-exact products)
+  bf16x3  2e-5                          (2-way split drops the lo*lo product, ~2^-16)
+pairs must match exactly; t-scores are checked against hostSignif's rule
+applied to the returned r, and against the oracle away from |r| -> 1.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PATHS = ("fp32", "bf16x3", "bf16x6")
+
+
+def tol(path, n):
+    if path == "bf16x3":
+        return 2e-5
+    return 2e-6 * np.sqrt(max(n, 1) / 100.0) + 1e-6
+
+
+def rpmcc(lib, use, A, B):
+    """A, B variable-major (na, n), (nb, n) -- R's as.single(x) order."""
+    A = np.ascontiguousarray(A, np.float32); B = np.ascontiguousarray(B, np.float32)
+    na, n = A.shape
+    nb = B.shape[0]
+    pairs = np.full((na, nb), -1, np.float32)
+    corr = np.full((na, nb), -7, np.float32)
+    ts = np.full((na, nb), -7, np.float32)
+    ci = lambda v: ctypes.byref(ctypes.c_int(v))
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    lib.rpmcc(ci(use), vp(A), ci(na), vp(B), ci(nb), ci(n), vp(pairs), vp(corr), vp(ts))
+    err = lib.gt_last_error().decode()
+    assert err == "", err
+    return corr, pairs, ts
+
+
+@pytest.fixture(params=PATHS)
+def path(request, gpu):
+    import gputools_gb300 as g
+    old = g.get_gram_path()
+    g.set_gram_path(request.param)
+    yield request.param
+    g.set_gram_path(old)
+
+
+def check_r(got, want, atol):
+    nan_g, nan_w = np.isnan(got), np.isnan(want)
+    assert np.array_equal(nan_g, nan_w)
+    ok = ~nan_w
+    if ok.any():
+        err = np.abs(got[ok].astype(np.float64) - want[ok]).max()
+        assert err <= atol, err
+
+
+def check_ts(ts, corr, pairs, want_ts, want_r):
+    r = corr.astype(np.float32)
+    rule = np.where(r >= np.float32(0.999), np.float32(10000),
+                    r * np.sqrt((pairs - np.float32(2)) / (np.float32(1) - r * r)))
+    ok = ~np.isnan(rule)
+    np.testing.assert_allclose(ts[ok], rule[ok], rtol=2e-6, atol=1e-6)
+    away = ok & (np.abs(want_r) < 0.95)
+    np.testing.assert_allclose(ts[away], want_ts[away], rtol=2e-3, atol=2e-4)
+
+
+@pytest.mark.parametrize("na,nb,n", [(1, 1, 3), (3, 5, 30), (37, 1, 100), (130, 70, 257),
+                                     (200, 200, 64)])
+def test_everything_two_sets(gpu, oracle_mod, rng, path, na, nb, n):
+    A = rng.standard_normal((na, n)).astype(np.float32)
+    B = (rng.standard_normal((nb, n)) * 2 + 5).astype(np.float32)
+    corr, pairs, ts = rpmcc(gpu, 0, A, B)
+    wc, wp, wt = oracle_mod.pearson(A, B, use=0)
+    check_r(corr, wc, tol(path, n))
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_ts(ts, corr, pairs, wt, wc)
+
+
+@pytest.mark.parametrize("p,n", [(2, 5), (65, 40), (300, 500), (513, 129)])
+def test_everything_symmetric_copies(gpu, oracle_mod, rng, path, p, n):
+    """gpuCor(x): R passes two copies of x through .C; the library recognises
+    them and computes each unordered pair once."""
+    X = rng.standard_normal((p, n)).astype(np.float32)
+    corr, pairs, ts = rpmcc(gpu, 0, X, X.copy())
+    wc, wp, wt = oracle_mod.pearson(X, use=0)
+    check_r(corr, wc, tol(path, n))
+    assert np.array_equal(corr, corr.T)
+    assert np.all(np.diag(corr) == 1.0)
+    assert np.all(np.diag(ts) == 10000.0)
+
+
+def test_everything_nan_and_constant_columns(gpu, oracle_mod, rng, path):
+    X = rng.standard_normal((50, 80)).astype(np.float32)
+    X[7, 11] = np.nan
+    X[9, :] = 3.25
+    corr, pairs, ts = rpmcc(gpu, 0, X, X)
+    wc, wp, _ = oracle_mod.pearson(X, use=0)
+    check_r(corr, wc, tol(path, 80))
+    assert np.all(np.isnan(corr[7])) and np.all(np.isnan(corr[:, 9]))
+    assert np.all(pairs == 80)
+
+
+def test_centering_stress_offsets(gpu, oracle_mod, rng, path):
+    """Lognormal(5, 1) values plus per-column offsets in [0, 1e3] (the
+    precision configuration's distribution, at a small size)."""
+    n, p = 512, 96
+    X = (rng.lognormal(5.0, 1.0, (p, n)) + rng.uniform(0, 1e3, (p, 1))).astype(np.float32)
+    corr, _, _ = rpmcc(gpu, 0, X, X)
+    wc, _, _ = oracle_mod.pearson(X, use=0)
+    check_r(corr, wc, tol(path, n))
+
+
+@pytest.mark.parametrize("na,nb,n,frac", [(4, 4, 10, 0.2), (33, 65, 200, 0.1), (120, 120, 77, 0.3)])
+def test_pairwise_complete(gpu, oracle_mod, rng, na, nb, n, frac):
+    A = rng.standard_normal((na, n)).astype(np.float32)
+    B = rng.standard_normal((nb, n)).astype(np.float32) + 50
+    A[rng.random(A.shape) < frac] = np.nan
+    B[rng.random(B.shape) < frac] = np.nan
+    corr, pairs, ts = rpmcc(gpu, 1, A, B)
+    wc, wp, wt = oracle_mod.pearson(A, B, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, 2e-5)
+
+
+def test_pairwise_degenerate(gpu, oracle_mod):
+    A = np.array([[1, np.nan, 3, 4], [np.nan, np.nan, np.nan, 2], [5, 5, 5, 5]], np.float32)
+    corr, pairs, _ = rpmcc(gpu, 1, A, A.copy())
+    wc, wp, _ = oracle_mod.pearson(A, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, 1e-6)
+
+
+def test_status_and_device_variants_agree(gpu, rng):
+    import torch
+    import gputools_gb300 as g
+    X = rng.standard_normal((100, 64)).astype(np.float32)
+    corr, pairs, ts = rpmcc(gpu, 0, X, X)
+    dX = torch.from_numpy(X).cuda()
+    res = g.pmcc_device(dX)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(res["corr"].cpu().numpy(), corr)
+    np.testing.assert_array_equal(res["ts"].cpu().numpy(), ts)
+    np.testing.assert_array_equal(res["pairs"].cpu().numpy(), pairs)
+
+
+def test_gpuCor_api(gpu, oracle_mod, rng):
+    import gputools_gb300 as g
+    A = rng.random((30, 5)); B = rng.random((30, 10))  # man/gpuCor.Rd example shapes
+    res = g.gpuCor(A, B, method="pearson")
+    wc, _, _ = oracle_mod.pearson(A.T.astype(np.float32), B.T.astype(np.float32))
+    np.testing.assert_allclose(res["coefficients"], wc, atol=2e-5)
+    assert res["coefficients"].shape == (5, 10) and np.all(res["pairs"] == 30)
+    A[2, 1] = np.nan
+    res = g.gpuCor(A, B, use="pairwise.complete.obs", method="pearson")
+    assert np.all(res["pairs"][1] == 29) and np.all(res["pairs"][0] == 30)
+
+
+def test_gpuTtest(gpu, rng):
+    import gputools_gb300 as g
+    gp = rng.poisson(5, 10) + 3
+    co = rng.random(10)
+    got = g.gpuTtest(gp, co)
+    r = co.astype(np.float32); n = gp.astype(np.float32)
+    np.testing.assert_allclose(got, r * np.sqrt((n - 2) / (1 - r * r)), rtol=2e-6)
