@@ -231,6 +231,17 @@ int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz,
 
 }  // namespace
 
+// Column statistics (FP64 mean, inverse norm, flags) of nvar variables.
+int launch_colstats(const float *dX, int64_t nvar, int64_t n, int use, ColStats *st,
+                    cudaStream_t s) {
+  if (nvar == 0) return GT_OK;
+  if (nvar > 2147483647LL) return fail(GT_EINVAL, "too many variables");
+  colstats_kernel<<<unsigned(nvar), kStatThreads, 0, s>>>(dX, n, use, st);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
 // prologue for the tensor-core path lives in gram_tc.cu
 int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, int slot_z,
                         int slot_st, void **Z, int64_t *kpad, cudaStream_t s);
@@ -240,7 +251,7 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
   if (nA == 0 || nB == 0) return GT_OK;
   PearsonOut po{corr, ts, pairs, nB, float(n), symmetric};
   const int path = gt_get_gram_path();
-  if (use == GT_EVERYTHING && path != GT_GRAM_FP32) {
+  if (use == GT_EVERYTHING && path != GT_GRAM_FP32 && n > 0) {
     const int nsplit = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
     void *zA = nullptr, *zB = nullptr;
     int64_t kpad = 0;
@@ -348,6 +359,9 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
   if (ts) GT_CUDA(cudaMemcpyAsync(ts, o1, outb, cudaMemcpyDeviceToHost, s));
   if (pairs) GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
   GT_CUDA(cudaStreamSynchronize(s));
+  bool failed = false;
+  GT_TRY(gt::tc_check_error(s, &failed));
+  if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return GT_OK;
 }
 

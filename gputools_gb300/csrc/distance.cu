@@ -212,5 +212,8 @@ extern "C" int gt_distances(const float *points, int64_t n, int64_t dim, float *
                              GT_LAYOUT_FULL, method, p, st));
   GT_CUDA(cudaMemcpyAsync(out, dout, size_t(n) * size_t(n) * 4, cudaMemcpyDeviceToHost, st));
   GT_CUDA(cudaStreamSynchronize(st));
+  bool failed = false;
+  GT_TRY(gt::tc_check_error(st, &failed));
+  if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return GT_OK;
 }

@@ -24,6 +24,13 @@ struct ColStats {
   int flags;        // bit 0: contains NaN; bit 1: zero variance
 };
 
+// Reads and clears the tensor-core kernels' device error word (synchronises
+// `s`); *failed is set when a bounded wait inside a kernel gave up.
+int tc_check_error(cudaStream_t s, bool *failed);
+
+int launch_colstats(const float *dX, int64_t nvar, int64_t n, int use, ColStats *st,
+                    cudaStream_t s);
+
 // gram_tc.cu: C[r][c] = sum_k Z_r[k] * Z_c[k] for the normalised Pearson
 // operands on tcgen05 tensor cores, with the Pearson epilogue fused.
 struct PearsonOut {
