@@ -19,7 +19,7 @@ extern "C" void Rf_error(const char *fmt, ...) __attribute__((weak));
 namespace gt {
 namespace {
 
-std::atomic<int> g_gram_path{GT_GRAM_FP32};
+std::atomic<int> g_gram_path{GT_GRAM_TC_BF16X3};
 
 // src/rinterface.cpp:147-156 getDistEnum: exact names, anything else is
 // euclidean.
