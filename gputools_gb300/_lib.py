@@ -57,6 +57,7 @@ SIGNATURES = {
     "gt_distances_device": (_i, [_vp, _i64, _i64, _vp, _i, _i, _f, _vp]),
     "gt_pmcc": (_i, [_i, _vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp]),
     "gt_pmcc_device": (_i, [_i, _vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "gt_pmcc_device_noalloc": (_i, [_i, _vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
     "gt_kendall": (_i, [_vp, _i64, _vp, _i64, _i64, _vp]),
     "gt_kendall_device": (_i, [_vp, _i64, _vp, _i64, _i64, _vp, _vp]),
     "gt_ttest_device": (_i, [_vp, _vp, _i64, _vp, _vp]),

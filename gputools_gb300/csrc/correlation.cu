@@ -23,6 +23,7 @@
 #include "kernels.cuh"
 
 #include <cmath>
+#include <mutex>
 
 namespace gt {
 
@@ -374,5 +375,116 @@ extern "C" int gt_ttest_device(const float *d_pairs, const float *d_coeffs, int6
   gt::ttest_kernel<<<gt::grid_for(n, 256), 256, 0, s>>>(d_pairs, d_coeffs, n, d_ts);
   gt::count_launch();
   GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Pearson.
+//
+// Some callers cannot let a library allocate device memory: processes whose
+// device memory is owned by another allocator (a framework's caching
+// allocator, or a fixed per-process budget) where a cudaMalloc made behind
+// their back fails or breaks their accounting, and latency-sensitive callers
+// that cannot afford the device-wide synchronisation cudaMalloc/cudaFree may
+// bring.  gt_pmcc_device_noalloc serves them: it runs the FP32 CUDA-core
+// Pearson path with its scratch (normalised rows and column statistics) in
+// the file-scope array below, which every device that loads the library
+// holds until the process exits.
+namespace gt {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;  // 64 MiB
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+int noalloc_scratch(unsigned char **out) {
+  int dev = 0;
+  GT_TRY(current_device(&dev));
+  if (dev >= kNoAllocMaxDevices) return fail(GT_ENODEV, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(GT_ECUDA, "cudaGetSymbolAddress(g_noalloc_scratch) failed: %s",
+                  cudaGetErrorString(e));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+  return GT_OK;
+}
+
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace gt
+
+extern "C" int gt_pmcc_device_noalloc(int use, const float *d_A, int64_t nA, const float *d_B,
+                                      int64_t nB, int64_t n, float *d_pairs, float *d_corr,
+                                      float *d_ts, void *stream) {
+  using namespace gt;
+  clear_error();
+  GT_TRY(pearson_check(use, nA, nB, n));
+  if ((nA > 0 && !d_A) || (nB > 0 && !d_B)) return fail(GT_EINVAL, "null device pointer");
+  if (nA == 0 || nB == 0) return GT_OK;
+  const bool sym = (d_A == d_B && nA == nB);
+  const int64_t ldz = (n + 3) / 4 * 4;
+  // scratch layout: zA | zB (two sets only) | statsA | statsB
+  const size_t bzA = round256(size_t(nA) * size_t(ldz) * 4);
+  const size_t bzB = sym ? 0 : round256(size_t(nB) * size_t(ldz) * 4);
+  const size_t bsA = round256(size_t(nA) * sizeof(ColStats));
+  const size_t bsB = sym ? 0 : round256(size_t(nB) * sizeof(ColStats));
+  const size_t need = bzA + bzB + bsA + bsB;
+  if (need > kNoAllocScratchBytes)
+    return fail(GT_EINVAL,
+                "gt_pmcc_device_noalloc: this problem needs %zu bytes of scratch but the "
+                "allocation-free entry point has %zu (nA=%lld, nB=%lld, n=%lld); use "
+                "gt_pmcc_device",
+                need, kNoAllocScratchBytes, (long long)nA, (long long)nB, (long long)n);
+  unsigned char *base = nullptr;
+  GT_TRY(noalloc_scratch(&base));
+  float *zA = reinterpret_cast<float *>(base);
+  float *zB = sym ? zA : reinterpret_cast<float *>(base + bzA);
+  ColStats *sA = reinterpret_cast<ColStats *>(base + bzA + bzB);
+  ColStats *sB = sym ? sA : reinterpret_cast<ColStats *>(base + bzA + bzB + bsA);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Every scratch byte read below is written first in the same call (all ldz
+  // entries of each row, every statistic), so nothing has to be cleared.
+  const float padv = use == GT_EVERYTHING ? 0.f : __builtin_nanf("");
+  GT_TRY(launch_colstats(d_A, nA, n, use, sA, s));
+  normalize_f32_kernel<<<grid_for(nA * ldz, 256), 256, 0, s>>>(d_A, nA, n, ldz, sA, use, padv, zA);
+  count_launch();
+  if (!sym) {
+    GT_TRY(launch_colstats(d_B, nB, n, use, sB, s));
+    normalize_f32_kernel<<<grid_for(nB * ldz, 256), 256, 0, s>>>(d_B, nB, n, ldz, sB, use, padv,
+                                                                  zB);
+    count_launch();
+  }
+  GT_CUDA(cudaGetLastError());
+  PearsonOut po{d_corr, d_ts, d_pairs, nB, float(n), sym ? 1 : 0};
+  SimtArgs a;
+  a.R = zA; a.C = zB;
+  a.ldr = a.ldc = ldz;
+  a.nr = nA; a.nc = nB;
+  a.K = ldz;
+  a.symmetric = sym ? 1 : 0;
+  a.vec_ok = 1;
+  cudaError_t e;
+  if (use == GT_EVERYTHING) {
+    const int64_t t = cdiv(nA, 128) * cdiv(nB, 128) / (sym ? 2 : 1);
+    if (t >= 2 * sm_count())
+      e = launch_allpairs_simt<OpDot, OutPearsonF32, 8, 8>(a, OpDot{}, OutPearsonF32{po}, s);
+    else
+      e = launch_allpairs_simt<OpDot, OutPearsonF32, 4, 4>(a, OpDot{}, OutPearsonF32{po}, s);
+  } else {
+    e = launch_allpairs_simt<OpPairwise, OutPairwise, 4, 4>(a, OpPairwise{}, OutPairwise{po}, s);
+  }
+  if (e != cudaSuccess) return fail(GT_ECUDA, "pearson kernel launch: %s", cudaGetErrorString(e));
   return GT_OK;
 }

@@ -156,6 +156,23 @@ int gt_pmcc_device(int use, const float *d_A, int64_t nA, const float *d_B,
                    int64_t nB, int64_t n, float *d_pairs, float *d_corr,
                    float *d_ts, void *stream);
 
+/* No counterpart in the reference.  Same arguments and results as
+ * gt_pmcc_device evaluated on CUDA cores (GT_GRAM_FP32), but it allocates no
+ * device memory: for callers whose device memory belongs to another
+ * allocator or a fixed budget, or who cannot afford the synchronisation an
+ * allocation may bring.  Its scratch is a 64 MiB array in the library's
+ * device image, which every GPU that loads the library holds until exit;
+ * problems needing more scratch -- 4*(nA + nB)*round4(n) + 24*(nA + nB)
+ * bytes, nB terms omitted when d_B == d_A -- are rejected with GT_EINVAL.
+ * The first call on a device looks up the array's address (once per device,
+ * with that device current); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. */
+int gt_pmcc_device_noalloc(int use, const float *d_A, int64_t nA,
+                           const float *d_B, int64_t nB, int64_t n,
+                           float *d_pairs, float *d_corr, float *d_ts,
+                           void *stream);
+
 /* Host buffers, synchronous.  Same result as RgpuKendall. */
 int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
                int64_t n, double *out);
