@@ -446,6 +446,69 @@ def run_euclid(args, lib, g, _lib, stream, dev, headline):
     return res
 
 
+def run_case(args):
+    """One workload at a chosen size, for profiler captures and size sweeps:
+    prints the per-kernel CUDA-event times of the library's main kernels."""
+    import torch
+    import gputools_gb300 as g
+    from gputools_gb300 import _lib
+    lib = g.load()
+    g.set_gram_path(args.path)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    rng = np.random.default_rng(5)
+    n, p = args.n, args.p
+    if args.case == "pearson":
+        z = rng.standard_normal((p, n), dtype=np.float32)
+        X = np.exp(z + np.float32(5.0), dtype=np.float32) + rng.uniform(0, 1e3, (p, 1)).astype(np.float32)
+        dX = torch.from_numpy(X).to(dev)
+        outs = [torch.empty((p, p), dtype=torch.float32, device=dev) for _ in range(3)]
+        fn = lambda: _lib.check(lib.gt_pmcc_device(0, vp(dX), p, vp(dX), p, n, vp(outs[0]),
+                                                   vp(outs[1]), vp(outs[2]), sptr))
+        names = ("pearson_prologue", "pearson_gram")
+    elif args.case == "euclid":
+        centres = rng.standard_normal((1000, 128), dtype=np.float32)
+        pts = centres[rng.integers(0, 1000, p)] + np.float32(1e-3) * rng.standard_normal((p, 128), dtype=np.float32)
+        dP = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
+        lay = 0 if args.layout == "full" else 1
+        m = p * p if lay == 0 else p * (p - 1) // 2
+        out = torch.empty(m, dtype=torch.float32, device=dev)
+        fn = lambda: _lib.check(lib.gt_distances_device(vp(dP), p, 128, vp(out), lay, 0,
+                                                        ctypes.c_float(2.0), sptr))
+        names = ("euclid_prologue", "euclid_gram", "dist")
+    elif args.case == "kendall":
+        X = rng.integers(0, 10, (p, n)).astype(np.float32)
+        dX = torch.from_numpy(X).to(dev)
+        out = torch.empty((p, p), dtype=torch.float64, device=dev)
+        fn = lambda: _lib.check(lib.gt_kendall_device(vp(dX), p, vp(dX), p, n, vp(out), sptr))
+        names = ("kendall_count",)
+    else:
+        raise SystemExit(f"unknown case {args.case}")
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    lib.gt_profile_reset()
+    lib.gt_profile_enable(1)
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lib.gt_profile_enable(0)
+    res = {"case": args.case, "p": p, "n": n, "path": args.path, "layout": args.layout,
+           "ms_per_step": e0.elapsed_time(e1) / args.steps,
+           "bk": os.environ.get("GT_TC_BK", "64"), "chunk": os.environ.get("GT_TC_CHUNK", "256")}
+    for nm in names:
+        ms = ctypes.c_double(); c = ctypes.c_uint64()
+        lib.gt_profile_kernel_ms(nm.encode(), ctypes.byref(ms), ctypes.byref(c))
+        if c.value:
+            res[nm + "_ms"] = ms.value / c.value
+    print(json.dumps(res), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,7 +516,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--skip-euclid", action="store_true")
+    ap.add_argument("--case", choices=("pearson", "euclid", "kendall"),
+                    help="run one workload at the given size instead of the benchmark")
+    ap.add_argument("--p", type=int, default=4096, help="--case: variables / points")
+    ap.add_argument("--n", type=int, default=4096, help="--case: observations")
+    ap.add_argument("--path", default="bf16x3", help="--case: gram path")
+    ap.add_argument("--layout", default="dist", help="--case euclid: full or dist")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

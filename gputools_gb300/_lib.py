@@ -61,6 +61,12 @@ SIGNATURES = {
     "gt_kendall": (_i, [_vp, _i64, _vp, _i64, _i64, _vp]),
     "gt_kendall_device": (_i, [_vp, _i64, _vp, _i64, _i64, _vp, _vp]),
     "gt_ttest_device": (_i, [_vp, _vp, _i64, _vp, _vp]),
+    "gt_cor_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),
+    "gt_dist_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),
+    "gt_mds_stress_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "RgpuCorBackward": (None, [_vp, _pi, _pi, _vp, _vp]),
+    "RgpuDistBackward": (None, [_vp, _pi, _pi, _vp, _vp]),
+    "RgpuMdsStress": (None, [_vp, _pi, _pi, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -238,3 +238,63 @@ def set_gram_path(path: str) -> None:
 
 def get_gram_path() -> str:
     return {0: "bf16x3", 1: "bf16x6", 2: "fp32"}[load().gt_get_gram_path()]
+
+
+# ---------------------------------------------------------------------------
+# Adjoints (no counterpart in the reference): R-style gradient wrappers.
+
+def gpuCorBackward(x, grad) -> np.ndarray:
+    """dL/dx for C = cor(x) (pearson), x n x p, grad = dL/dC p x p."""
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1)
+    n, p = x.shape
+    X = np.ascontiguousarray(x.T, dtype=np.float32)          # as.single(x)
+    G = np.ascontiguousarray(np.asarray(grad, dtype=np.float32))
+    if G.shape != (p, p):
+        raise ValueError("grad must be p x p")
+    out = np.empty((p, n), np.float32)
+    lib = load()
+    lib.RgpuCorBackward(_ptr(X), ctypes.byref(ctypes.c_int(n)), ctypes.byref(ctypes.c_int(p)),
+                        _ptr(G), _ptr(out))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return np.ascontiguousarray(out.T).astype(np.float64)
+
+
+def gpuDistBackward(points, grad) -> np.ndarray:
+    """dL/dpoints for the Euclidean distance matrix D, grad = dL/dD (N x N)."""
+    pts = np.ascontiguousarray(np.asarray(points, dtype=np.float32))
+    n, d = pts.shape
+    G = np.ascontiguousarray(np.asarray(grad, dtype=np.float32))
+    if G.shape != (n, n):
+        raise ValueError("grad must be N x N")
+    out = np.empty((n, d), np.float32)
+    lib = load()
+    lib.RgpuDistBackward(_ptr(pts), ctypes.byref(ctypes.c_int(n)), ctypes.byref(ctypes.c_int(d)),
+                         _ptr(G), _ptr(out))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return out.astype(np.float64)
+
+
+def gpuMdsStress(points, delta):
+    """(stress, gradient) of sum_{i<j} (D_ij - delta_ij)^2; delta a Dist or its
+    values in R's dist order."""
+    pts = np.ascontiguousarray(np.asarray(points, dtype=np.float32))
+    n, d = pts.shape
+    dv = delta.values if isinstance(delta, Dist) else delta
+    dv = np.ascontiguousarray(np.asarray(dv, dtype=np.float32))
+    if dv.size != n * (n - 1) // 2:
+        raise ValueError("delta must hold N(N-1)/2 values")
+    out = np.empty((n, d), np.float32)
+    loss = np.zeros(1, np.float64)
+    lib = load()
+    lib.RgpuMdsStress(_ptr(pts), ctypes.byref(ctypes.c_int(n)), ctypes.byref(ctypes.c_int(d)),
+                      _ptr(dv), _ptr(loss), _ptr(out))
+    err = _lib.last_error()
+    if err:
+        raise RuntimeError(err)
+    return float(loss[0]), out.astype(np.float64)

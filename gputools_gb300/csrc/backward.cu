@@ -1,0 +1,353 @@
+// backward.cu -- adjoints of gpuCor (pearson) and gpuDist (euclidean), and
+// the MDS stress gradient.  No counterpart in the reference (gputools has no
+// differentiation); the forward quantities follow inst/cuda/correlation.cu:
+// 152-292 and inst/cuda/distance.cu:40-78.
+//
+// Pearson.  With c_j = x_j - mean, s_j = |c_j|, z_j = c_j / s_j and
+// C_ij = z_i . z_j, an upstream G = dL/dC gives
+//   W = S Z  (S = G + G^T, Z the p x n matrix of the z_j),
+//   dL/dx_j = (w_j - z_j (z_j . w_j)) / s_j,
+// i.e. one GEMM plus a rank-1 correction per variable.  Means and norms are
+// recomputed in FP64 (not stored by the forward pass); S and Z^T are split
+// into bf16 planes and W runs on the tcgen05 chunked-accumulation kernel
+// (gram_tc.cu), or on the CUDA-core engine for GT_GRAM_FP32.
+//
+// Distances.  dL/dx_i = sum_j W_ij (x_i - x_j) = x_i rowsum(W)_i - (W X)_i with
+// W_ij = (G_ij + G_ji) / D_ij (0 where D_ij = 0), or for MDS stress
+// W_ij = 2 (D_ij - delta_ij) / D_ij.  A fused CUDA-core kernel recomputes D_ij
+// from the points and never materialises W.
+#include "common.cuh"
+#include "allpairs_simt.cuh"
+#include "kernels.cuh"
+#include "tc_ptx.cuh"
+
+#include <cuda_bf16.h>
+
+namespace gt {
+
+namespace {
+
+constexpr int64_t kKPadB = 64;
+
+__device__ __forceinline__ float zval(const float *X, const ColStats *st, int64_t n, int64_t i,
+                                      int64_t k) {
+  const ColStats s = st[i];
+  if (s.flags) return 0.f;
+  return float((double(X[i * n + k]) - s.mean) * s.inv_norm);
+}
+
+template <class T>
+__device__ __forceinline__ void put_parts(T *dst, int64_t plane, int64_t idx, float v, int ns);
+
+template <>
+__device__ __forceinline__ void put_parts<float>(float *dst, int64_t, int64_t idx, float v, int) {
+  dst[idx] = v;
+}
+
+template <>
+__device__ __forceinline__ void put_parts<__nv_bfloat16>(__nv_bfloat16 *dst, int64_t plane,
+                                                         int64_t idx, float v, int ns) {
+  __nv_bfloat16 p[3];
+  if (ns == 3) tc::split_bf16<3>(v, p);
+  else tc::split_bf16<2>(v, p);
+  for (int q = 0; q < ns; q++) dst[q * plane + idx] = p[q];
+}
+
+// S = G + G^T as rows j, columns i (ld kp >= p, zero padded), float or bf16
+// planes.  32 x 32 tiles transposed through shared memory.
+template <class T>
+__global__ void sym_operand_kernel(const float *__restrict__ G, int64_t p, int64_t kp, int ns,
+                                   T *__restrict__ S) {
+  __shared__ float tile[32][33];
+  const int64_t i0 = int64_t(blockIdx.x) * 32, j0 = int64_t(blockIdx.y) * 32;
+  const int tx = threadIdx.x, ty0 = threadIdx.y;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t i = i0 + ty, j = j0 + tx;
+    tile[ty][tx] = (i < p && j < p) ? G[i * p + j] : 0.f;  // G[i][j], rows i
+  }
+  __syncthreads();
+  const int64_t plane = p * kp;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t j = j0 + ty, i = i0 + tx;
+    if (j >= p || i >= kp) continue;
+    const float v = (i < p) ? G[j * p + i] + tile[tx][ty] : 0.f;
+    put_parts<T>(S, plane, j * kp + i, v, ns);
+  }
+}
+
+// Z^T: rows k (observations), columns i (variables, ld kp), zero padded.
+template <class T>
+__global__ void zt_operand_kernel(const float *__restrict__ X, int64_t p, int64_t n, int64_t kp,
+                                  const ColStats *__restrict__ st, int ns, T *__restrict__ Zt) {
+  __shared__ float tile[32][33];
+  const int64_t k0 = int64_t(blockIdx.x) * 32, i0 = int64_t(blockIdx.y) * 32;
+  const int tx = threadIdx.x, ty0 = threadIdx.y;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t i = i0 + ty, k = k0 + tx;
+    tile[ty][tx] = (i < p && k < n) ? zval(X, st, n, i, k) : 0.f;  // rows i
+  }
+  __syncthreads();
+  const int64_t plane = n * kp;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t k = k0 + ty, i = i0 + tx;
+    if (k >= n || i >= kp) continue;
+    put_parts<T>(Zt, plane, k * kp + i, tile[tx][ty], ns);
+  }
+}
+
+constexpr int kFinThreads = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (l < kFinThreads / 32) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (l == 0) sh[0] = t;
+  }
+  __syncthreads();
+  return sh[0];
+}
+
+// dX_j = (w_j - z_j (z_j . w_j)) * inv_norm_j, one CTA per variable.
+__global__ void __launch_bounds__(kFinThreads)
+cor_backward_finish_kernel(const float *__restrict__ X, int64_t n, const ColStats *__restrict__ st,
+                           const float *__restrict__ W, float *__restrict__ dX) {
+  __shared__ double sh[32];
+  const int64_t j = blockIdx.x;
+  const ColStats s = st[j];
+  double d = 0.0;
+  for (int64_t k = threadIdx.x; k < n; k += kFinThreads)
+    d = fma(double(zval(X, st, n, j, k)), double(W[j * n + k]), d);
+  d = block_sum_d(d, sh);
+  for (int64_t k = threadIdx.x; k < n; k += kFinThreads) {
+    float v = 0.f;
+    if (!s.flags) {
+      const double z = (double(X[j * n + k]) - s.mean) * s.inv_norm;
+      v = float((double(W[j * n + k]) - z * d) * s.inv_norm);
+    }
+    dX[j * n + k] = v;
+  }
+}
+
+struct OpDotB {
+  static constexpr int NACC = 1;
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
+  __device__ void step(float (&c)[1], float a, float b) const { c[0] = fmaf(a, b, c[0]); }
+};
+
+struct OutStore {
+  float *out;
+  int64_t ld;
+  __device__ void operator()(int64_t r, int64_t c, const float (&acc)[1], bool) const {
+    out[r * ld + c] = acc[0];
+  }
+};
+
+// ------------------------------------------------------------ distances
+constexpr int kDbRows = 128;   // rows i per CTA (one per thread)
+constexpr int kDbCols = 32;    // points j per shared tile
+
+// mode 0: W_ij = (G_ij + G_ji) / D_ij ; mode 1: MDS, W_ij = 2 (D_ij - delta_ij) / D_ij
+template <int DMAX, int MODE>
+__global__ void __launch_bounds__(kDbRows)
+dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
+                     const float *__restrict__ aux, float *__restrict__ dX,
+                     double *__restrict__ loss) {
+  __shared__ float xj[kDbCols][DMAX + 1];
+  __shared__ float cf[kDbRows][kDbCols + 1];  // G_ij + G_ji, or delta_ij
+  __shared__ double sh[kDbRows / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t i0 = int64_t(blockIdx.x) * kDbRows;
+  const int64_t i = i0 + tid;
+  float xi[DMAX], acc[DMAX];
+#pragma unroll
+  for (int k = 0; k < DMAX; k++) {
+    xi[k] = (i < n && k < dim) ? X[i * dim + k] : 0.f;
+    acc[k] = 0.f;
+  }
+  float wsum = 0.f;
+  double lsum = 0.0;
+  for (int64_t j0 = 0; j0 < n; j0 += kDbCols) {
+    __syncthreads();
+    for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
+      const int jj = e / DMAX, k = e - jj * DMAX;
+      const int64_t j = j0 + jj;
+      xj[jj][k] = (j < n && k < dim) ? X[j * dim + k] : 0.f;
+    }
+    if (MODE == 0) {
+      // rows i, columns j: lanes along j (row-contiguous)
+      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
+        const int64_t gi = i0 + ii, gj = j0 + lane;
+        cf[ii][lane] = (gi < n && gj < n) ? aux[gi * n + gj] : 0.f;
+      }
+      __syncthreads();
+      // add G_ji: rows j, lanes along i
+      for (int jj = 0; jj < kDbCols; jj++) {
+        const int64_t gj = j0 + jj;
+        if (gj < n && i < n) cf[tid][jj] += aux[gj * n + i];
+      }
+    } else {
+      // delta in R dist layout: (a > b) at n*b - b*(b+1)/2 + a - b - 1
+      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
+        const int64_t gi = i0 + ii, gj = j0 + lane;
+        if (gi < n && gj < n && gj > gi) cf[ii][lane] = aux[n * gi - gi * (gi + 1) / 2 + gj - gi - 1];
+      }
+      for (int jj = 0; jj < kDbCols; jj++) {
+        const int64_t gj = j0 + jj;
+        if (gj < n && i < n && i > gj) cf[tid][jj] = aux[n * gj - gj * (gj + 1) / 2 + i - gj - 1];
+      }
+    }
+    __syncthreads();
+    if (i < n) {
+      const int jmax = (n - j0 < kDbCols) ? int(n - j0) : kDbCols;
+      for (int jj = 0; jj < jmax; jj++) {
+        const int64_t j = j0 + jj;
+        float d2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < DMAX; k++) {
+          const float t = xi[k] - xj[jj][k];
+          d2 = fmaf(t, t, d2);
+        }
+        if (j == i || !(d2 > 0.f)) continue;
+        const float d = sqrtf(d2);
+        float w;
+        if (MODE == 0) {
+          w = cf[tid][jj] / d;
+        } else {
+          const float del = cf[tid][jj];
+          w = 2.f * (d - del) / d;
+          if (j > i) lsum += double(d - del) * double(d - del);
+        }
+        wsum += w;
+#pragma unroll
+        for (int k = 0; k < DMAX; k++) acc[k] = fmaf(w, xj[jj][k], acc[k]);
+      }
+    }
+  }
+  if (i < n) {
+#pragma unroll
+    for (int k = 0; k < DMAX; k++)
+      if (k < dim) dX[i * dim + k] = fmaf(xi[k], wsum, -acc[k]);
+  }
+  if (MODE == 1 && loss) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0) sh[warp] = lsum;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kDbRows / 32; w++) t += sh[w];
+      atomicAdd(loss, t);
+    }
+  }
+}
+
+template <int MODE>
+int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *aux, float *dX,
+                         double *loss, cudaStream_t s) {
+  const unsigned grid = unsigned(cdiv(n, kDbRows));
+  if (dim <= 16)
+    dist_backward_kernel<16, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
+  else if (dim <= 32)
+    dist_backward_kernel<32, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
+  else if (dim <= 64)
+    dist_backward_kernel<64, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
+  else
+    return fail(GT_EUNSUPPORTED, "distance adjoint supports at most 64 dimensions (dim=%lld)",
+                (long long)dim);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+}  // namespace
+
+int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, float *d_dX,
+                      cudaStream_t s) {
+  if (p == 0 || n == 0) return GT_OK;
+  const int path = gt_get_gram_path();
+  const int64_t kp = cdiv(p, kKPadB) * kKPadB;
+  void *pst = nullptr, *pS = nullptr, *pZ = nullptr, *pW = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH3, size_t(p) * sizeof(ColStats), &pst));
+  ColStats *st = static_cast<ColStats *>(pst);
+  ProfScope prof("cor_backward", s);
+  GT_TRY(launch_colstats(dX, p, n, GT_EVERYTHING, st, s));
+  GT_TRY(ws_get(WS_SCRATCH4 + 0, 256, &pW));  // keep the small slot allocated
+  GT_TRY(ws_get(WS_OUT2, size_t(p) * size_t(n) * 4, &pW));
+  float *W = static_cast<float *>(pW);
+  const dim3 blk(32, 8);
+  if (path == GT_GRAM_FP32) {
+    GT_TRY(ws_get(WS_SCRATCH0, size_t(p) * size_t(kp) * 4, &pS));
+    GT_TRY(ws_get(WS_SCRATCH1, size_t(n) * size_t(kp) * 4, &pZ));
+    sym_operand_kernel<float><<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+        dG, p, kp, 1, static_cast<float *>(pS));
+    zt_operand_kernel<float><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
+        dX, p, n, kp, st, 1, static_cast<float *>(pZ));
+    count_launch(2);
+    SimtArgs a;
+    a.R = static_cast<float *>(pS); a.C = static_cast<float *>(pZ);
+    a.ldr = a.ldc = kp;
+    a.nr = p; a.nc = n; a.K = kp;
+    a.symmetric = 0; a.vec_ok = 1;
+    cudaError_t e = launch_allpairs_simt<OpDotB, OutStore, 8, 8>(a, OpDotB{}, OutStore{W, n}, s);
+    if (e != cudaSuccess) return fail(GT_ECUDA, "adjoint GEMM launch: %s", cudaGetErrorString(e));
+  } else {
+    const int ns = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
+    GT_TRY(ws_get(WS_SCRATCH0, size_t(ns) * size_t(p) * size_t(kp) * 2, &pS));
+    GT_TRY(ws_get(WS_SCRATCH1, size_t(ns) * size_t(n) * size_t(kp) * 2, &pZ));
+    sym_operand_kernel<__nv_bfloat16>
+        <<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+            dG, p, kp, ns, static_cast<__nv_bfloat16 *>(pS));
+    zt_operand_kernel<__nv_bfloat16><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
+        dX, p, n, kp, st, ns, static_cast<__nv_bfloat16 *>(pZ));
+    count_launch(2);
+    GT_CUDA(cudaGetLastError());
+    GT_TRY(gemm_tc_store(pS, p, pZ, n, kp, ns, W, n, s));
+  }
+  cor_backward_finish_kernel<<<unsigned(p), kFinThreads, 0, s>>>(dX, n, st, W, d_dX);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+}  // namespace gt
+
+extern "C" int gt_cor_backward_device(const float *d_X, int64_t p, int64_t n, const float *d_G,
+                                      float *d_dX, void *stream) {
+  gt::clear_error();
+  if (p < 0 || n < 0) return gt::fail(GT_EINVAL, "negative size");
+  if (p > 2147483647LL) return gt::fail(GT_EINVAL, "too many variables");
+  if (p > 0 && n > 0 && (!d_X || !d_G || !d_dX)) return gt::fail(GT_EINVAL, "null device pointer");
+  return gt::cor_backward_impl(d_X, p, n, d_G, d_dX, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gt_dist_backward_device(const float *d_X, int64_t n, int64_t dim, const float *d_G,
+                                       float *d_dX, void *stream) {
+  gt::clear_error();
+  if (n < 0 || dim < 0) return gt::fail(GT_EINVAL, "negative size");
+  if (n == 0 || dim == 0) return GT_OK;
+  if (!d_X || !d_G || !d_dX) return gt::fail(GT_EINVAL, "null device pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  gt::ProfScope prof("dist_backward", s);
+  return gt::launch_dist_backward<0>(d_X, n, dim, d_G, d_dX, nullptr, s);
+}
+
+extern "C" int gt_mds_stress_device(const float *d_X, int64_t n, int64_t dim,
+                                    const float *d_delta, float *d_dX, double *d_loss,
+                                    void *stream) {
+  gt::clear_error();
+  if (n < 0 || dim < 0) return gt::fail(GT_EINVAL, "negative size");
+  if (n == 0 || dim == 0) return GT_OK;
+  if (!d_X || !d_delta || !d_dX) return gt::fail(GT_EINVAL, "null device pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (d_loss) GT_CUDA(cudaMemsetAsync(d_loss, 0, sizeof(double), s));
+  gt::ProfScope prof("mds_stress", s);
+  return gt::launch_dist_backward<1>(d_X, n, dim, d_delta, d_dX, d_loss, s);
+}

@@ -51,6 +51,8 @@ constexpr int kTcThreads = 192;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per barrier wait
 constexpr uint64_t kDrainLimitNs = 200000000ull;  // 0.2 s for in-flight work at exit
 constexpr int kKPad = 64;                         // K padding of the operand planes
+constexpr int kMaxSmem = 232448;                  // dynamic shared memory per CTA (227 KB)
+constexpr int kEpiTileFloats = 32 * 33;           // one warp's padded 32 x 32 staging tile
 
 // ----------------------------------------------------------------- tiling
 struct TileSpace {
@@ -108,156 +110,117 @@ __device__ __forceinline__ float signif(float r, float pairs) {
   return r * sqrtf((pairs - 2.f) / (1.f - r * r));
 }
 
-// r = clamp(G), t-score, both orientations for cor(x).
-struct PearsonEpi {
-  float *corr, *ts;
-  int64_t ld, nr, nc;
-  float npairs;
-  int symmetric;
-
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32]) const {
-    if (r >= nr) return;
-    const bool full = c0 + 32 <= nc;
-    if (full && (!symmetric || r < c0)) {
-      float v[32], t[32];
+// Stores 32 consecutive floats of one output row: 128-bit stores when the
+// address allows, scalar otherwise.
+__device__ __forceinline__ void store_row32(float *p, const float (&v)[32]) {
+  if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+    float4 *q = reinterpret_cast<float4 *>(p);
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        v[j] = clamp_r(g[j]);
-        t[j] = signif(v[j], npairs);
-      }
-      if (corr) {
-        float4 *p = reinterpret_cast<float4 *>(corr + r * ld + c0);
-        if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+    for (int j = 0; j < 8; j++) q[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+  } else {
 #pragma unroll
-          for (int j = 0; j < 8; j++) p[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; j++) corr[r * ld + c0 + j] = v[j];
-        }
-        if (symmetric)
-#pragma unroll
-          for (int j = 0; j < 32; j++) corr[(c0 + j) * ld + r] = v[j];
-      }
-      if (ts) {
-        float4 *p = reinterpret_cast<float4 *>(ts + r * ld + c0);
-        if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-#pragma unroll
-          for (int j = 0; j < 8; j++) p[j] = make_float4(t[4 * j], t[4 * j + 1], t[4 * j + 2], t[4 * j + 3]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; j++) ts[r * ld + c0 + j] = t[j];
-        }
-        if (symmetric)
-#pragma unroll
-          for (int j = 0; j < 32; j++) ts[(c0 + j) * ld + r] = t[j];
-      }
-      return;
-    }
-#pragma unroll
-    for (int j = 0; j < 32; j++) {
-      const int64_t c = c0 + j;
-      if (c >= nc) break;
-      if (symmetric && r > c) continue;
-      float v = clamp_r(g[j]);
-      if (symmetric && r == c && v == v) v = 1.f;
-      const float t = signif(v, npairs);
-      if (corr) corr[r * ld + c] = v;
-      if (ts) ts[r * ld + c] = t;
-      if (symmetric && r != c) {
-        if (corr) corr[c * ld + r] = v;
-        if (ts) ts[c * ld + r] = t;
-      }
-    }
+    for (int j = 0; j < 32; j++) p[j] = v[j];
   }
-};
+}
 
-// d^2 = |a|^2 + |b|^2 - 2 G in FP64; entries whose d^2 is below tau*(|a|^2+|b|^2),
-// where the contraction's rounding could dominate, are recomputed exactly
-// from the float32 points by the warp (FP64 differences), which also makes
-// exact duplicates exactly 0.
+// Operands are the points centred by their column means (distances do not
+// change).  d^2 = |a|^2 + |b|^2 - 2 G with FP32 norms rounded from FP64; an
+// entry whose d^2 is below tau * (|a|^2 + |b|^2), where rounding of the
+// contraction could dominate, is recomputed from the original float points
+// by the warp: float differences, float partial sums of squares per lane,
+// FP64 sum across lanes.  Exact duplicates therefore come out exactly 0.
 struct EuclidEpi {
-  const double *norm2;
+  const float *norm2;
   const float *pts;
   float *out;
   int64_t n, dim;
   int layout;  // GT_LAYOUT_FULL / GT_LAYOUT_DIST
-  double tau;
+  float tau;
 
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32]) const {
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     float v[32];
     unsigned pend = 0u;
-    const double na = r < n ? norm2[r] : 0.0;
+    const float na = r < n ? norm2[r] : 0.f;
 #pragma unroll
     for (int j = 0; j < 32; j++) {
       const int64_t c = c0 + j;
       v[j] = 0.f;
       if (r < n && c < n && r < c) {
-        const double nb = norm2[c];
-        const double d2 = na + nb - 2.0 * double(g[j]);
-        if (d2 < tau * (na + nb)) pend |= 1u << j;
-        else v[j] = float(sqrt(d2));
+        const float s = na + norm2[c];
+        const float d2 = fmaf(-2.f, g[j], s);
+        if (d2 < tau * s) pend |= 1u << j;
+        else v[j] = sqrtf(d2);
       }
     }
-    // exact recomputation of the flagged entries, one entry per warp pass
     while (true) {
       const unsigned any = __ballot_sync(FULL, pend != 0u);
       if (!any) break;
       const int src = __ffs(int(any)) - 1;
       const int j = __shfl_sync(FULL, __ffs(int(pend)) - 1, src);
-      const int64_t rr = __shfl_sync(FULL, (long long)r, src);
+      const long long rr = __shfl_sync(FULL, (long long)r, src);
       const int64_t c = c0 + j;
       const float *pa = pts + rr * dim, *pb = pts + c * dim;
-      double acc = 0.0;
+      float part = 0.f;
       for (int64_t k = lane; k < dim; k += 32) {
-        const double d = double(pa[k]) - double(pb[k]);
-        acc = fma(d, d, acc);
+        const float d = pa[k] - pb[k];
+        part = fmaf(d, d, part);
       }
+      double acc = double(part);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
       if (lane == src) {
-        v[j] = float(sqrt(acc));
+        const float d2 = float(acc);
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+          if (q == j) v[q] = sqrtf(d2);
         pend &= ~(1u << j);
       }
     }
-    if (r >= n) return;
-    if (layout == GT_LAYOUT_FULL) {
+    // mirror orientation (lanes hold consecutive rows): coalesced from registers
+    if (layout == GT_LAYOUT_FULL && r < n) {
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const int64_t c = c0 + j;
-        if (c >= n) break;
-        if (r < c) {
-          out[r * n + c] = v[j];
-          out[c * n + r] = v[j];
-        } else if (r == c) {
-          out[r * n + c] = 0.f;
-        }
-      }
-    } else {
-      // R dist vector: entry (i = c, j = r), c > r, at n*r - r*(r+1)/2 + c - r - 1
-      const int64_t base = n * r - r * (r + 1) / 2 - r - 1;
-#pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int64_t c = c0 + j;
-        if (c >= n) break;
-        if (r < c) out[base + c] = v[j];
+        if (c < n && r < c) out[c * n + r] = v[j];
       }
     }
+    // row orientation: transpose the warp's 32 x 32 block through shared memory
+#pragma unroll
+    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = v[j];
+    __syncwarp();
+    const int64_t rbase = r - lane;
+    const int64_t c = c0 + lane;
+    for (int i = 0; i < 32; i++) {
+      const int64_t ri = rbase + i;
+      if (ri >= n) break;
+      const float x = wsm[i * 33 + lane];
+      if (c >= n || c < ri) continue;
+      if (layout == GT_LAYOUT_FULL) {
+        out[ri * n + c] = (c == ri) ? 0.f : x;
+      } else if (c > ri) {
+        // R dist vector: entry (i = c, j = ri) at n*ri - ri*(ri+1)/2 + c - ri - 1
+        out[n * ri - ri * (ri + 1) / 2 + c - ri - 1] = x;
+      }
+    }
+    __syncwarp();
   }
 };
 
 // ----------------------------------------------------------------- kernel
-template <int NSPLIT, int BN, int BK>
+template <int NSPLIT, int BN, int BK, int EPI_WARPS>
 struct TcCfg {
   static constexpr int BM = 128;
   static constexpr int ROW_BYTES = BK * 2;                // 128 or 64
   static constexpr int A_TILE = BM * BK * 2;
   static constexpr int B_TILE = BN * BK * 2;
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
-  static constexpr int STAGES_RAW = (220 * 1024) / STAGE;
+  // per epilogue warp: a 32 x 33 float tile for transposing its stores
+  static constexpr int EPI_BYTES = EPI_WARPS * kEpiTileFloats * 4;
+  static constexpr int STAGES_RAW = (kMaxSmem - 1024 - 256 - EPI_BYTES) / STAGE;
   static constexpr int STAGES = STAGES_RAW > 6 ? 6 : STAGES_RAW;
-  static constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+  static constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/ + EPI_BYTES;
   static constexpr int KSTEPS = BK / 16;
   static constexpr int NPROD = NSPLIT == 2 ? 3 : 6;
   static_assert(STAGES >= 2, "need at least two stages");
@@ -280,7 +243,7 @@ template <int NSPLIT, int BN, int BK, class Epi>
 __global__ void __launch_bounds__(kTcThreads, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                TileSpace tiles, int64_t nk, Epi epi, int *err) {
-  using C = TcCfg<NSPLIT, BN, BK>;
+  using C = TcCfg<NSPLIT, BN, BK, 4>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -291,6 +254,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   uint64_t *mma_done = acce + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  float *epi_smem = reinterpret_cast<float *>(smem + C::STAGES * C::STAGE + 256);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -422,7 +386,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       for (int c = 0; c < BN; c += 32) {
         float g[32];
         tc::tmem_ld32(tbase + uint32_t(c), g);
-        epi(r, tj * BN + c, g);
+        epi(r, tj * BN + c, g, epi_smem + (warp - 2) * kEpiTileFloats);
       }
       tc::tc_fence_before();
       __syncwarp();
@@ -437,20 +401,247 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   }
 }
 
-// ----------------------------------------------------------------- operands
-// Split of one FP64 value into bf16 parts (round to nearest each time).
-template <int NSPLIT>
-__device__ __forceinline__ void split_bf16(double z, __nv_bfloat16 (&p)[3]) {
-  double rem = z;
+// ----------------------------------------------------------------- chunked kernel
+// The tensor core's FP32 accumulation rounds every add toward zero, so its
+// error grows linearly with the number of adds into one accumulator (about
+// 2^-25 |acc| per add).  For the Pearson contraction, K is split into chunks
+// of `ckb` k-blocks: each chunk is accumulated in TMEM from zero, and the
+// epilogue warps add the chunk into FP32 registers with round-to-nearest.
+// Eight epilogue warps (two per TMEM lane quarter, 128 columns each) hold the
+// 128 x 256 running sums; chunks alternate between the two TMEM accumulators
+// so the MMAs of chunk c+1 overlap the epilogue's add of chunk c.
+constexpr int kTcChunkThreads = 320;
+
+// Pearson finish of a warp's 32 x 32 block (lane = row, 32 consecutive
+// columns in registers): r = clamp(G), hostSignif's t-score and the pair
+// count, stored row-wise through the warp's staging tile and, for cor(x),
+// mirrored column-wise; both kinds of store are coalesced.
+struct PearsonFinish {
+  float *corr, *ts, *pairs;
+  int64_t ld, nr, nc;
+  float npairs;
+  int symmetric;
+
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+    const int lane = threadIdx.x & 31;
+    // mirror orientation (lanes hold consecutive rows): coalesced from registers
+    if (symmetric && r < nr) {
 #pragma unroll
-  for (int i = 0; i < NSPLIT; i++) {
-    p[i] = __double2bfloat16(rem);
-    rem -= double(__bfloat162float(p[i]));
+      for (int j = 0; j < 32; j++) {
+        const int64_t c = c0 + j;
+        if (c < nc && r < c) {
+          const float v = clamp_r(g[j]);
+          const int64_t o = c * ld + r;
+          if (corr) corr[o] = v;
+          if (ts) ts[o] = signif(v, npairs);
+          if (pairs) pairs[o] = npairs;
+        }
+      }
+    }
+    // row orientation: transpose the warp's 32 x 32 block through shared memory
+#pragma unroll
+    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
+    __syncwarp();
+    const int64_t rbase = r - lane;
+    const int64_t c = c0 + lane;
+    for (int i = 0; i < 32; i++) {
+      const int64_t ri = rbase + i;
+      if (ri >= nr) break;
+      const float x = wsm[i * 33 + lane];
+      if (c >= nc || (symmetric && c < ri)) continue;
+      float v = clamp_r(x);
+      if (symmetric && c == ri && v == v) v = 1.f;
+      const int64_t o = ri * ld + c;
+      if (corr) corr[o] = v;
+      if (ts) ts[o] = signif(v, npairs);
+      if (pairs) pairs[o] = npairs;
+    }
+    __syncwarp();
+  }
+};
+
+template <int NSPLIT, int BN, int BK, class Fin>
+__global__ void __launch_bounds__(kTcChunkThreads, 1)
+gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
+                       const __grid_constant__ CUtensorMap mapB, TileSpace tiles, int64_t nk,
+                       int64_t ckb, Fin fin, int *err) {
+  using C = TcCfg<NSPLIT, BN, BK, 8>;
+  static_assert(BN == 256, "chunked kernel: two epilogue warps of 128 columns per lane quarter");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + C::STAGES * C::STAGE);
+  uint64_t *empty = full + C::STAGES;
+  uint64_t *accf = empty + C::STAGES;
+  uint64_t *acce = accf + 2;
+  uint64_t *mma_done = acce + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  float *epi_smem = reinterpret_cast<float *>(smem + C::STAGES * C::STAGE + 256);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::STAGES; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      tc::mbar_init(&accf[b], 1);
+      tc::mbar_init(&acce[b], 8);
+    }
+    tc::mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 0 && lane == 0) {
+    tc::prefetch_tensormap(&mapA);
+    tc::prefetch_tensormap(&mapB);
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, 2 * BN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int64_t nchunks = (nk + ckb - 1) / ckb;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int64_t it = 0;
+      for (int64_t t = blockIdx.x; t < tiles.ntiles && !*abort_flag; t += gridDim.x) {
+        int64_t ti, tj;
+        tile_coords(tiles, t, ti, tj);
+        for (int64_t kb = 0; kb < nk; kb++, it++) {
+          const int s = int(it % C::STAGES);
+          const uint32_t use = uint32_t(it / C::STAGES);
+          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
+            *abort_flag = 1;
+            break;
+          }
+          uint8_t *st = smem + s * C::STAGE;
+          tc::mbar_arrive_expect_tx(&full[s], C::STAGE);
+#pragma unroll
+          for (int p = 0; p < NSPLIT; p++)
+            tc::tma_load_3d(st + p * C::A_TILE, &mapA, &full[s], int32_t(kb * BK),
+                            int32_t(ti * C::BM), p);
+#pragma unroll
+          for (int p = 0; p < NSPLIT; p++)
+            tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, &mapB, &full[s],
+                            int32_t(kb * BK), int32_t(tj * BN), p);
+        }
+      }
+      if (*abort_flag) {
+        for (int s = 0; s < C::STAGES; s++) {
+          const int64_t fills = it / C::STAGES + (s < it % C::STAGES ? 1 : 0);
+          if (fills > 0) tc::mbar_wait_bounded(&full[s], uint32_t((fills - 1) & 1), kDrainLimitNs);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(128, BN);
+      int64_t it = 0, cc = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
+        for (int64_t ch = 0; ch < nchunks && ok; ch++, cc++) {
+          const int buf = int(cc & 1);
+          const uint32_t ause = uint32_t(cc >> 1);
+          if (!tc::mbar_wait(&acce[buf], (ause & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t d = tmem_base + uint32_t(buf * BN);
+          const int64_t kb0 = ch * ckb, kb1 = min(nk, kb0 + ckb);
+          for (int64_t kb = kb0; kb < kb1; kb++, it++) {
+            const int s = int(it % C::STAGES);
+            const uint32_t use = uint32_t(it / C::STAGES);
+            if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, kWaitLimitNs)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t sa = tc::smem_u32(smem + s * C::STAGE);
+            const uint32_t sb = sa + NSPLIT * C::A_TILE;
+#pragma unroll
+            for (int k = 0; k < C::KSTEPS; k++) {
+#pragma unroll
+              for (int p = 0; p < C::NPROD; p++) {
+                int pa, pb;
+                product_parts<NSPLIT>(p, pa, pb);
+                const uint64_t ad = tc::smem_desc_kmajor(sa + pa * C::A_TILE + k * 32, C::ROW_BYTES);
+                const uint64_t bd = tc::smem_desc_kmajor(sb + pb * C::B_TILE + k * 32, C::ROW_BYTES);
+                tc::umma_bf16(d, ad, bd, idesc, (kb != kb0 || k || p) ? 1u : 0u);
+              }
+            }
+            tc::umma_commit(&empty[s]);
+          }
+          if (ok) tc::umma_commit(&accf[buf]);
+        }
+      }
+      if (!ok) *abort_flag = 1;
+      tc::umma_commit(mma_done);
+      tc::mbar_wait_bounded(mma_done, 0u, kDrainLimitNs);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------ epilogue (warps 2..9)
+    const int q = warp & 3;                  // TMEM lane quarter
+    const int half = (warp - 2) >> 2;        // column half: 0 or 1
+    int64_t cc = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
+      int64_t ti, tj;
+      tile_coords(tiles, t, ti, tj);
+      float acc[128];
+#pragma unroll
+      for (int j = 0; j < 128; j++) acc[j] = 0.f;
+      for (int64_t ch = 0; ch < nchunks; ch++, cc++) {
+        const int buf = int(cc & 1);
+        const uint32_t ause = uint32_t(cc >> 1);
+        const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t tbase =
+            tmem_base + uint32_t(buf * BN + half * 128) + (uint32_t(q * 32) << 16);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          float g[32];
+          tc::tmem_ld32(tbase + uint32_t(32 * i), g);
+#pragma unroll
+          for (int j = 0; j < 32; j++) acc[32 * i + j] += g[j];
+        }
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&acce[buf]);
+      }
+      if (!ok) break;
+      const int64_t r = ti * 128 + q * 32 + lane;
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        float g[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
+        fin(r, tj * BN + half * 128 + 32 * i, g, epi_smem + (warp - 2) * kEpiTileFloats);
+      }
+    }
+    if (!ok) *abort_flag = 1;
+  }
+  __syncthreads();
+  if (*abort_flag && threadIdx.x == 0) atomicExch(err, 1);
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem_base, 2 * BN);
   }
 }
 
-// Pearson operand planes: z = (x - mean) * inv_norm, NaN rows for variables
-// that are NaN-flagged or constant; k >= n is zero.
+// ----------------------------------------------------------------- operands
+// Pearson operand planes: z = (x - mean) * inv_norm in FP64 (rounded to
+// float), NaN rows for variables that are NaN-flagged or constant; k >= n is
+// zero.
 template <int NSPLIT>
 __global__ void pearson_split_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
                                      int64_t kpad, const ColStats *__restrict__ st,
@@ -468,7 +659,7 @@ __global__ void pearson_split_kernel(const float *__restrict__ X, int64_t nvar, 
       if (s.flags) {
         p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
       } else {
-        split_bf16<NSPLIT>((double(X[v * n + k]) - s.mean) * s.inv_norm, p);
+        tc::split_bf16<NSPLIT>(float((double(X[v * n + k]) - s.mean) * s.inv_norm), p);
       }
     }
 #pragma unroll
@@ -476,24 +667,37 @@ __global__ void pearson_split_kernel(const float *__restrict__ X, int64_t nvar, 
   }
 }
 
-// Euclidean operand planes (raw coordinates) and FP64 squared norms, one warp
-// per point.
+// Column sums of the points (FP64), accumulated into sums[] (zeroed first).
+__global__ void euclid_colsum_kernel(const float *__restrict__ P, int64_t n, int64_t dim,
+                                     int64_t per_block, double *__restrict__ sums) {
+  const int64_t d = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (d >= dim) return;
+  const int64_t i0 = blockIdx.y * per_block;
+  const int64_t i1 = min(n, i0 + per_block);
+  double acc = 0.0;
+  for (int64_t i = i0; i < i1; i++) acc += double(P[i * dim + d]);
+  atomicAdd(&sums[d], acc);
+}
+
+// Euclidean operand planes of the centred points and their squared norms
+// (FP64, stored rounded to float), one warp per point.
 template <int NSPLIT>
 __global__ void euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t dim,
-                                    int64_t kpad, __nv_bfloat16 *__restrict__ Z,
-                                    double *__restrict__ norm2) {
+                                    int64_t kpad, const double *__restrict__ sums,
+                                    __nv_bfloat16 *__restrict__ Z, float *__restrict__ norm2) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
   const int64_t plane = n * kpad;
+  const double inv_n = 1.0 / double(n);
   for (int64_t v = warp; v < n; v += nwarps) {
     double acc = 0.0;
     for (int64_t k = lane; k < kpad; k += 32) {
       __nv_bfloat16 p[3];
       if (k < dim) {
-        const double x = P[v * dim + k];
+        const double x = double(P[v * dim + k]) - sums[k] * inv_n;
         acc = fma(x, x, acc);
-        split_bf16<NSPLIT>(x, p);
+        tc::split_bf16<NSPLIT>(float(x), p);
       } else {
         p[0] = p[1] = p[2] = __float2bfloat16(0.f);
       }
@@ -502,7 +706,7 @@ __global__ void euclid_split_kernel(const float *__restrict__ P, int64_t n, int6
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) norm2[v] = acc;
+    if (lane == 0) norm2[v] = float(acc);
   }
 }
 
@@ -550,7 +754,7 @@ int err_word(int **p) {
 template <int NSPLIT, int BN, int BK, class Epi>
 int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
                 bool symmetric, const Epi &epi, const char *prof_name, cudaStream_t s) {
-  using C = TcCfg<NSPLIT, BN, BK>;
+  using C = TcCfg<NSPLIT, BN, BK, 4>;
   if (symmetric && BN != 256) return fail(GT_EINVAL, "symmetric tiling needs BN = 256");
   if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
   CUtensorMap mA, mB;
@@ -571,6 +775,43 @@ int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t 
   return GT_OK;
 }
 
+template <int NSPLIT, int BK, class Fin>
+int launch_gram_chunked(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
+                        bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
+                        cudaStream_t s) {
+  constexpr int BN = 256;
+  using C = TcCfg<NSPLIT, BN, BK, 8>;
+  if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
+  if (ckb < 1) ckb = 1;
+  CUtensorMap mA, mB;
+  GT_TRY(make_plane_map(&mA, zA, nA, kpad, NSPLIT, 128, BK));
+  GT_TRY(make_plane_map(&mB, zB, nB, kpad, NSPLIT, BN, BK));
+  const TileSpace ts = make_tiles(nA, nB, BN, symmetric);
+  if (ts.ntiles == 0) return GT_OK;
+  int *err = nullptr;
+  GT_TRY(err_word(&err));
+  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  auto kern = gram_tc_chunked_kernel<NSPLIT, BN, BK, Fin>;
+  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+  const int64_t grid = ts.ntiles < sm_count() ? ts.ntiles : sm_count();
+  ProfScope prof(prof_name, s);
+  kern<<<unsigned(grid), kTcChunkThreads, C::SMEM, s>>>(mA, mB, ts, kpad / BK, ckb, fin, err);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+// k-blocks per accumulation chunk of the Pearson contraction (0 = one chunk).
+int64_t tc_chunk_kblocks(int bk) {
+  static int64_t elems = -1;
+  if (elems < 0) {
+    const char *e = std::getenv("GT_TC_CHUNK");
+    elems = e ? std::atoll(e) : 256;
+  }
+  if (elems <= 0) return int64_t(1) << 40;
+  return elems / bk > 0 ? elems / bk : 1;
+}
+
 int tc_config() {
   static int cfg = -1;
   if (cfg < 0) {
@@ -580,13 +821,40 @@ int tc_config() {
   return cfg;
 }
 
-__global__ void fill_kernel(float *__restrict__ p, int64_t count, float v) {
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count;
-       i += int64_t(gridDim.x) * blockDim.x)
-    p[i] = v;
-}
+// Plain FP32 store of the contraction, C[r*ld + c] (rows through the warp's
+// staging tile so every store is coalesced).
+struct StoreFinish {
+  float *out;
+  int64_t ld, nr, nc;
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
+    __syncwarp();
+    const int64_t rbase = r - lane, c = c0 + lane;
+    for (int i = 0; i < 32; i++) {
+      const int64_t ri = rbase + i;
+      if (ri >= nr) break;
+      if (c < nc) out[ri * ld + c] = wsm[i * 33 + lane];
+    }
+    __syncwarp();
+  }
+};
 
 }  // namespace
+
+// C[r][c] = sum_k A_r[k] B_c[k] over split-bf16 planes ([part][row][kpad]),
+// chunked FP32 accumulation, stored as a row-major float matrix.
+int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,
+                  int nsplit, float *C, int64_t ldc, cudaStream_t s) {
+  if (nA == 0 || nB == 0) return GT_OK;
+  StoreFinish fin{C, ldc, nA, nB};
+  if (nsplit == 3)
+    return launch_gram_chunked<3, 32>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(32),
+                                      fin, "gemm_store", s);
+  return launch_gram_chunked<2, 64>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(64),
+                                    fin, "gemm_store", s);
+}
 
 int tc_check_error(cudaStream_t s, bool *failed) {
   int *err = nullptr;
@@ -626,53 +894,49 @@ int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, in
 int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int nsplit,
                const PearsonOut &out, cudaStream_t s) {
   if (nA == 0 || nB == 0) return GT_OK;
-  PearsonEpi epi{out.corr, out.ts, out.ld, nA, nB, out.npairs, out.symmetric};
-  if (out.pairs) {
-    const int64_t count = nA * nB;
-    int64_t g = cdiv(count, 256);
-    if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
-    fill_kernel<<<unsigned(g), 256, 0, s>>>(out.pairs, count, out.npairs);
-    count_launch();
-  }
-  if (!out.corr && !out.ts) return GT_OK;
+  if (!out.corr && !out.ts && !out.pairs) return GT_OK;
+  PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs, out.symmetric};
   const bool sym = out.symmetric != 0;
-  if (nsplit == 3) {
-    if (sym || tc_config() == 32)
-      return launch_gram<3, 256, 32>(zA, nA, zB, nB, kpad, sym, epi, "pearson_gram", s);
-    return launch_gram<3, 128, 64>(zA, nA, zB, nB, kpad, sym, epi, "pearson_gram", s);
-  }
+  if (nsplit == 3)
+    return launch_gram_chunked<3, 32>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
+                                      "pearson_gram", s);
   if (tc_config() == 32)
-    return launch_gram<2, 256, 32>(zA, nA, zB, nB, kpad, sym, epi, "pearson_gram", s);
-  return launch_gram<2, 256, 64>(zA, nA, zB, nB, kpad, sym, epi, "pearson_gram", s);
+    return launch_gram_chunked<2, 32>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
+                                      "pearson_gram", s);
+  return launch_gram_chunked<2, 64>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64), fin,
+                                    "pearson_gram", s);
 }
 
 int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
               cudaStream_t st) {
   if (dim == 0 || n < 2) return dist_simt(d_pts, n, dim, d_out, layout, GT_EUCLIDEAN, 2.f, st);
-  const int nsplit = gt_get_gram_path() == GT_GRAM_TC_BF16X3 ? 2 : 3;
+  // Output writes bound this kernel at moderate dim, so the float32-exact
+  // 3-way split costs nothing over the 2-way one: always use it.
+  constexpr int NS = 3;
   const int64_t kpad = cdiv(dim, kKPad) * kKPad;
-  void *pz = nullptr, *pn = nullptr;
-  GT_TRY(ws_get(WS_SCRATCH0, size_t(nsplit) * size_t(n) * size_t(kpad) * 2, &pz));
-  GT_TRY(ws_get(WS_SCRATCH2, size_t(n) * 8, &pn));
+  void *pz = nullptr, *pn = nullptr, *psum = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n) * size_t(kpad) * 2, &pz));
+  GT_TRY(ws_get(WS_SCRATCH2, size_t(n) * 4, &pn));
+  GT_TRY(ws_get(WS_SCRATCH3, size_t(dim) * 8, &psum));
   auto *z = static_cast<__nv_bfloat16 *>(pz);
-  auto *norm2 = static_cast<double *>(pn);
+  auto *norm2 = static_cast<float *>(pn);
+  auto *sums = static_cast<double *>(psum);
   {
     ProfScope prof("euclid_prologue", st);
+    GT_CUDA(cudaMemsetAsync(sums, 0, size_t(dim) * 8, st));
+    const int64_t per_block = 2048;
+    dim3 cg((unsigned)cdiv(dim, 128), (unsigned)cdiv(n, per_block), 1u);
+    euclid_colsum_kernel<<<cg, 128, 0, st>>>(d_pts, n, dim, per_block, sums);
+    count_launch();
     int64_t g = cdiv(n * 32, 256);
     if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
-    if (nsplit == 3)
-      euclid_split_kernel<3><<<unsigned(g), 256, 0, st>>>(d_pts, n, dim, kpad, z, norm2);
-    else
-      euclid_split_kernel<2><<<unsigned(g), 256, 0, st>>>(d_pts, n, dim, kpad, z, norm2);
+    euclid_split_kernel<NS><<<unsigned(g), 256, 0, st>>>(d_pts, n, dim, kpad, sums, z, norm2);
     count_launch();
     GT_CUDA(cudaGetLastError());
   }
-  // Recompute entries whose d^2 is below this fraction of |a|^2 + |b|^2.
-  const double tau = nsplit == 3 ? 1.0 / 64.0 : 1.0 / 4.0;
-  EuclidEpi epi{norm2, d_pts, d_out, n, dim, layout, tau};
-  if (nsplit == 3) return launch_gram<3, 256, 32>(z, n, z, n, kpad, true, epi, "euclid_gram", st);
-  if (tc_config() == 32) return launch_gram<2, 256, 32>(z, n, z, n, kpad, true, epi, "euclid_gram", st);
-  return launch_gram<2, 256, 64>(z, n, z, n, kpad, true, epi, "euclid_gram", st);
+  // Entries with d^2 below an eighth of |a|^2 + |b|^2 are recomputed exactly.
+  EuclidEpi epi{norm2, d_pts, d_out, n, dim, layout, 0.125f};
+  return launch_gram<NS, 256, 32>(z, n, z, n, kpad, true, epi, "euclid_gram", st);
 }
 
 }  // namespace gt

@@ -45,4 +45,9 @@ struct PearsonOut {
 int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64_t kpad,
                int nsplit, const PearsonOut &out, cudaStream_t st);
 
+// C[r][c] = sum_k A_r[k] B_c[k] on tcgen05 from split-bf16 planes
+// ([part][row][kpad], kpad a multiple of 64), stored as row-major float.
+int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,
+                  int nsplit, float *C, int64_t ldc, cudaStream_t s);
+
 }  // namespace gt

@@ -144,6 +144,97 @@ void rtestT(const float *pairs, const float *coeffs, const int *n, float *ts) {
   gt::report(st, "rtestT");
 }
 
+// Host-buffer adjoints for the R gradient wrappers (no counterpart in the
+// reference): copy in, run the device adjoint, copy out, synchronously.
+void RgpuCorBackward(const float *X, const int *nobs, const int *nvar, const float *G,
+                     float *dX) {
+  gt::clear_error();
+  int st = GT_OK;
+  if (!nobs || !nvar || *nobs < 0 || *nvar < 0) {
+    st = gt::fail(GT_EINVAL, "bad sizes");
+  } else if (*nobs > 0 && *nvar > 0) {
+    const int64_t n = *nobs, p = *nvar;
+    const size_t bx = size_t(p) * size_t(n) * 4, bg = size_t(p) * size_t(p) * 4;
+    cudaStream_t s = gt::lib_stream();
+    void *dx = nullptr, *dg = nullptr, *dout = nullptr;
+    st = gt::ws_get(gt::WS_IN_A, bx, &dx);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bg, &dg);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_OUT0, bx, &dout);
+    if (st == GT_OK) {
+      cudaMemcpyAsync(dx, X, bx, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dg, G, bg, cudaMemcpyHostToDevice, s);
+      st = gt_cor_backward_device(static_cast<float *>(dx), p, n, static_cast<float *>(dg),
+                                  static_cast<float *>(dout), s);
+      if (st == GT_OK) {
+        cudaMemcpyAsync(dX, dout, bx, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = gt::fail(GT_ECUDA, "%s", cudaGetErrorString(e));
+      }
+    }
+  }
+  gt::report(st, "RgpuCorBackward");
+}
+
+void RgpuDistBackward(const float *points, const int *numPoints, const int *dim, const float *G,
+                      float *dX) {
+  gt::clear_error();
+  int st = GT_OK;
+  if (!numPoints || !dim || *numPoints < 0 || *dim < 0) {
+    st = gt::fail(GT_EINVAL, "bad sizes");
+  } else if (*numPoints > 0 && *dim > 0) {
+    const int64_t n = *numPoints, d = *dim;
+    const size_t bx = size_t(n) * size_t(d) * 4, bg = size_t(n) * size_t(n) * 4;
+    cudaStream_t s = gt::lib_stream();
+    void *dx = nullptr, *dg = nullptr, *dout = nullptr;
+    st = gt::ws_get(gt::WS_IN_A, bx, &dx);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bg, &dg);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_OUT0, bx, &dout);
+    if (st == GT_OK) {
+      cudaMemcpyAsync(dx, points, bx, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dg, G, bg, cudaMemcpyHostToDevice, s);
+      st = gt_dist_backward_device(static_cast<float *>(dx), n, d, static_cast<float *>(dg),
+                                   static_cast<float *>(dout), s);
+      if (st == GT_OK) {
+        cudaMemcpyAsync(dX, dout, bx, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = gt::fail(GT_ECUDA, "%s", cudaGetErrorString(e));
+      }
+    }
+  }
+  gt::report(st, "RgpuDistBackward");
+}
+
+void RgpuMdsStress(const float *points, const int *numPoints, const int *dim, const float *delta,
+                   double *loss, float *dX) {
+  gt::clear_error();
+  int st = GT_OK;
+  if (!numPoints || !dim || *numPoints < 0 || *dim < 0) {
+    st = gt::fail(GT_EINVAL, "bad sizes");
+  } else if (*numPoints > 0 && *dim > 0) {
+    const int64_t n = *numPoints, d = *dim;
+    const size_t bx = size_t(n) * size_t(d) * 4, bd = size_t(n) * size_t(n - 1) / 2 * 4;
+    cudaStream_t s = gt::lib_stream();
+    void *dx = nullptr, *dd = nullptr, *dout = nullptr, *dl = nullptr;
+    st = gt::ws_get(gt::WS_IN_A, bx, &dx);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bd > 0 ? bd : 4, &dd);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_OUT0, bx, &dout);
+    if (st == GT_OK) st = gt::ws_get(gt::WS_OUT1, 8, &dl);
+    if (st == GT_OK) {
+      cudaMemcpyAsync(dx, points, bx, cudaMemcpyHostToDevice, s);
+      if (bd) cudaMemcpyAsync(dd, delta, bd, cudaMemcpyHostToDevice, s);
+      st = gt_mds_stress_device(static_cast<float *>(dx), n, d, static_cast<float *>(dd),
+                                static_cast<float *>(dout), static_cast<double *>(dl), s);
+      if (st == GT_OK) {
+        if (dX) cudaMemcpyAsync(dX, dout, bx, cudaMemcpyDeviceToHost, s);
+        if (loss) cudaMemcpyAsync(loss, dl, 8, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = gt::fail(GT_ECUDA, "%s", cudaGetErrorString(e));
+      }
+    }
+  }
+  gt::report(st, "RgpuMdsStress");
+}
+
 // The reference NVRTC-compiles inst/cuda/*.cu here (src/cudaUtils.cpp:118-165);
 // this library ships sm_103a code, so loading only checks for a device.
 void cuCompile(const int *numFiles, const char **cuFilenames, const char **cuSrc) {

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -176,6 +177,18 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
          | (1u << 10)                 // B format bf16
          | (uint32_t(N >> 3) << 17)   // N / 8
          | (uint32_t(M >> 4) << 24);  // M / 16
+}
+
+// Split of a float into NSPLIT bf16 parts, each the round-to-nearest bf16 of
+// the remainder of the previous ones; every remainder is exact in float.
+template <int NSPLIT>
+__device__ __forceinline__ void split_bf16(float z, __nv_bfloat16 (&p)[3]) {
+  float rem = z;
+#pragma unroll
+  for (int i = 0; i < NSPLIT; i++) {
+    p[i] = __float2bfloat16_rn(rem);
+    rem -= __bfloat162float(p[i]);
+  }
 }
 
 }  // namespace tc

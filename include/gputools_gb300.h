@@ -181,6 +181,39 @@ int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
 int gt_kendall_device(const float *d_X, int64_t nx, const float *d_Y,
                       int64_t ny, int64_t n, double *d_out, void *stream);
 
+/* ---- adjoints (no counterpart in the reference) ------------------------- */
+
+/* dL/dX of C = cor(X) (Pearson, "everything") given G = dL/dC.
+ * X variable-major p x n (X[j*n + k]), G row-major p x p (G[i*p + j] =
+ * dL/dC_ij; G and its transpose give the same result), dX like X.  Means and
+ * norms are recomputed in FP64; the contraction W = (G + G^T) Z runs on the
+ * selected Gram path.  Constant variables get a zero gradient. */
+int gt_cor_backward_device(const float *d_X, int64_t p, int64_t n,
+                           const float *d_G, float *d_dX, void *stream);
+
+/* dL/dX of the Euclidean distances D of the rows of X (n x dim row-major)
+ * given G = dL/dD (n x n, G[i*n + j]); terms with D_ij = 0 contribute 0.
+ * dim <= 64. */
+int gt_dist_backward_device(const float *d_X, int64_t n, int64_t dim,
+                            const float *d_G, float *d_dX, void *stream);
+
+/* MDS stress L = sum_{i<j} (D_ij - delta_ij)^2 and dL/dX, delta in R's dist
+ * layout; *d_loss (double, may be NULL) receives L.  dim <= 64. */
+int gt_mds_stress_device(const float *d_X, int64_t n, int64_t dim,
+                         const float *d_delta, float *d_dX, double *d_loss,
+                         void *stream);
+
+/* .C-style host-buffer forms for an R gradient wrapper:
+ * gpuCorBackward(x, grad), gpuDistBackward(points, grad),
+ * gpuMdsStress(points, delta).  X as R's as.single(x) (n x p column-major =
+ * variable-major), G as as.single(grad) (either orientation). */
+void RgpuCorBackward(const float *X, const int *nobs, const int *nvar,
+                     const float *G, float *dX);
+void RgpuDistBackward(const float *points, const int *numPoints,
+                      const int *dim, const float *G, float *dX);
+void RgpuMdsStress(const float *points, const int *numPoints, const int *dim,
+                   const float *delta, double *loss, float *dX);
+
 /* Device buffers: t-scores as rtestT. */
 int gt_ttest_device(const float *d_pairs, const float *d_coeffs, int64_t n,
                     float *d_ts, void *stream);

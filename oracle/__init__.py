@@ -72,6 +72,9 @@ def _load():
         lib.orc_kendall.argtypes = [fp, i64, fp, i64, i64, ctypes.c_int, fp, fp, fp, fp]
         lib.orc_ttest.argtypes = [fp, fp, i64, fp]
         lib.orc_signif.argtypes = [fp, fp, i64, fp]
+        lib.orc_cor_backward.argtypes = [fp, i64, i64, fp, fp]
+        lib.orc_dist_backward.argtypes = [fp, i64, i64, fp, fp]
+        lib.orc_mds_stress.argtypes = [fp, i64, i64, fp, fp, fp]
         lib.orc_set_threads.argtypes = [ctypes.c_int]
         lib.orc_get_threads.restype = ctypes.c_int
         del dp
@@ -230,3 +233,39 @@ def ref_host_signif(pairs: np.ndarray, r: np.ndarray) -> np.ndarray:
     out = np.empty(r.shape, np.float32)
     fn(_ptr(pairs), _ptr(r), r.size, _ptr(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Adjoints (FP64), for the backward kernels.
+
+def cor_backward(X: np.ndarray, G: np.ndarray) -> np.ndarray:
+    """dL/dX for C = cor(X) (X variable-major (p, n)) given G = dL/dC (p, p)."""
+    X = np.ascontiguousarray(X, np.float32)
+    G = np.ascontiguousarray(G, np.float64)
+    p, n = X.shape
+    out = np.empty((p, n), np.float64)
+    rc = _load().orc_cor_backward(_ptr(X), p, n, _ptr(G), _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"orc_cor_backward failed ({rc})")
+    return out
+
+
+def dist_backward(X: np.ndarray, G: np.ndarray) -> np.ndarray:
+    """dL/dX for D = euclidean distances of the rows of X given G = dL/dD."""
+    X = np.ascontiguousarray(X, np.float32)
+    G = np.ascontiguousarray(G, np.float64)
+    n, d = X.shape
+    out = np.empty((n, d), np.float64)
+    _load().orc_dist_backward(_ptr(X), n, d, _ptr(G), _ptr(out))
+    return out
+
+
+def mds_stress(X: np.ndarray, delta: np.ndarray):
+    """(loss, dL/dX) of sum_{i<j} (D_ij - delta_ij)^2, delta in R dist layout."""
+    X = np.ascontiguousarray(X, np.float32)
+    delta = np.ascontiguousarray(delta, np.float32)
+    n, d = X.shape
+    loss = np.zeros(1, np.float64)
+    out = np.empty((n, d), np.float64)
+    _load().orc_mds_stress(_ptr(X), n, d, _ptr(delta), _ptr(loss), _ptr(out))
+    return float(loss[0]), out

@@ -249,3 +249,108 @@ int orc_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
   }
   return 0;
 }
+
+/* ------------------------------------------------------------ adjoints --- */
+/* No counterpart in the reference: the adjoints of the all-pairs statistics
+ * (dL/dX from an upstream dL/dC), restated from the calculus in FP64.
+ *
+ * Pearson, C = cor(X), variables x_j (columns, X[j*n + k]):
+ *   c_j = x_j - mean(x_j), s_j = |c_j|, z_j = c_j / s_j, C_ij = z_i . z_j
+ *   w_j = sum_i (G_ij + G_ji) z_i
+ *   dL/dx_j = (w_j - z_j (z_j . w_j)) / s_j      (w_j and z_j have zero mean)
+ * G is row-major p x p, G[i*p + j] = dL/dC_ij.  Constant variables get 0. */
+int orc_cor_backward(const float *X, int64_t p, int64_t n, const double *G,
+                     double *dX) {
+  double *Z = (double *)malloc(sizeof(double) * (size_t)(p * n));
+  double *inv = (double *)malloc(sizeof(double) * (size_t)p);
+  if (!Z || !inv) { free(Z); free(inv); return -3; }
+#pragma omp parallel for num_threads(orc_get_threads())
+  for (int64_t j = 0; j < p; j++) {
+    ksum s = {0, 0};
+    for (int64_t k = 0; k < n; k++) ks_add(&s, X[j * n + k]);
+    double m = ks_val(&s) / (double)n;
+    ksum q = {0, 0};
+    for (int64_t k = 0; k < n; k++) {
+      double d = X[j * n + k] - m;
+      ks_add(&q, d * d);
+    }
+    double nrm = sqrt(ks_val(&q));
+    inv[j] = nrm > 0 ? 1.0 / nrm : 0.0;
+    for (int64_t k = 0; k < n; k++) Z[j * n + k] = (X[j * n + k] - m) * inv[j];
+  }
+#pragma omp parallel for schedule(dynamic, 1) num_threads(orc_get_threads())
+  for (int64_t j = 0; j < p; j++) {
+    double *w = (double *)calloc((size_t)n, sizeof(double));
+    for (int64_t i = 0; i < p; i++) {
+      double g = G[i * p + j] + G[j * p + i];
+      if (g == 0.0) continue;
+      for (int64_t k = 0; k < n; k++) w[k] += g * Z[i * n + k];
+    }
+    ksum zw = {0, 0};
+    for (int64_t k = 0; k < n; k++) ks_add(&zw, Z[j * n + k] * w[k]);
+    double d = ks_val(&zw);
+    for (int64_t k = 0; k < n; k++)
+      dX[j * n + k] = (w[k] - Z[j * n + k] * d) * inv[j];
+    free(w);
+  }
+  free(Z);
+  free(inv);
+  return 0;
+}
+
+/* Euclidean distances, D_ij = |x_i - x_j| (X row-major n x dim):
+ *   dL/dx_i = sum_j (G_ij + G_ji) (x_i - x_j) / D_ij,  terms with D_ij = 0 are 0.
+ * G is n x n, G[i*n + j] = dL/dD_ij. */
+int orc_dist_backward(const float *X, int64_t n, int64_t dim, const double *G,
+                      double *dX) {
+#pragma omp parallel for schedule(dynamic, 4) num_threads(orc_get_threads())
+  for (int64_t i = 0; i < n; i++) {
+    for (int64_t k = 0; k < dim; k++) dX[i * dim + k] = 0.0;
+    for (int64_t j = 0; j < n; j++) {
+      if (j == i) continue;
+      double d2 = 0.0;
+      for (int64_t k = 0; k < dim; k++) {
+        double t = (double)X[i * dim + k] - (double)X[j * dim + k];
+        d2 += t * t;
+      }
+      double d = sqrt(d2);
+      if (d == 0.0) continue;
+      double w = (G[i * n + j] + G[j * n + i]) / d;
+      for (int64_t k = 0; k < dim; k++)
+        dX[i * dim + k] += w * ((double)X[i * dim + k] - (double)X[j * dim + k]);
+    }
+  }
+  return 0;
+}
+
+/* MDS stress against targets delta (R dist layout, entry (i > j) at
+ * n*j - j*(j+1)/2 + i - j - 1): L = sum_{i<j} (D_ij - delta_ij)^2 and
+ * dL/dx_i = sum_{j != i} 2 (D_ij - delta_ij) (x_i - x_j) / D_ij. */
+int orc_mds_stress(const float *X, int64_t n, int64_t dim, const float *delta,
+                   double *loss, double *dX) {
+  double total = 0.0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : total) num_threads(orc_get_threads())
+  for (int64_t i = 0; i < n; i++) {
+    if (dX)
+      for (int64_t k = 0; k < dim; k++) dX[i * dim + k] = 0.0;
+    for (int64_t j = 0; j < n; j++) {
+      if (j == i) continue;
+      double d2 = 0.0;
+      for (int64_t k = 0; k < dim; k++) {
+        double t = (double)X[i * dim + k] - (double)X[j * dim + k];
+        d2 += t * t;
+      }
+      double d = sqrt(d2);
+      int64_t a = i > j ? i : j, b = i > j ? j : i;
+      double del = delta[n * b - b * (b + 1) / 2 + a - b - 1];
+      if (j > i) total += (d - del) * (d - del);
+      if (dX && d > 0.0) {
+        double w = 2.0 * (d - del) / d;
+        for (int64_t k = 0; k < dim; k++)
+          dX[i * dim + k] += w * ((double)X[i * dim + k] - (double)X[j * dim + k]);
+      }
+    }
+  }
+  if (loss) *loss = total;
+  return 0;
+}

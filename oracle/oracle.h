@@ -70,6 +70,14 @@ void orc_ttest(const double *pairs, const double *r, int64_t len, double *out);
 void orc_signif(const double *pairs, const double *r, int64_t len,
                 double *out);
 
+/* Adjoints (no counterpart in the reference; see oracle.c). */
+int orc_cor_backward(const float *X, int64_t p, int64_t n, const double *G,
+                     double *dX);
+int orc_dist_backward(const float *X, int64_t n, int64_t dim, const double *G,
+                      double *dX);
+int orc_mds_stress(const float *X, int64_t n, int64_t dim, const float *delta,
+                   double *loss, double *dX);
+
 #ifdef __cplusplus
 }
 #endif
