@@ -334,6 +334,7 @@ def run_ours(args, ranks: Ranks):
     euclid = {}
     if ranks.rank == 0 and not args.skip_euclid:
         euclid = run_euclid(args, lib, g, _lib, stream, dev, headline)
+    others = run_configs(lib, g, _lib, stream, dev, args.steps) if ranks.rank == 0 else {}
 
     if ranks.rank != 0:
         return
@@ -377,6 +378,7 @@ def run_ours(args, ranks: Ranks):
                       "sample": f"{SAMPLE_ROWS} rows x {N_VARS} vs FP64 oracle"},
         "paths": paths,
         "euclid": euclid,
+        "configs": others,
         "cpu_baseline": {"value": SAMPLE_ROWS * P / cpu_dt, "unit": "entries/s", "cores": threads,
                          "kind": "port",
                          "sample": f"FP64 oracle, {SAMPLE_ROWS} rows x {N_VARS} vars x {N_OBS} obs"},
@@ -507,6 +509,100 @@ def run_case(args):
         if c.value:
             res[nm + "_ms"] = ms.value / c.value
     print(json.dumps(res), flush=True)
+
+
+def run_configs(lib, g, _lib, stream, dev, steps):
+    """The other configurations at their stated sizes: all six gpuDist methods
+    on 4000 x 100, gpuCor kendall (500 obs x 1000 integer variables, bit-exact
+    spot check) and pearson (500 x 1000), gpuDist euclidean 2000 x 64 through
+    the host C ABI, and the adjoints (gpuCorBackward 1024 x 4096 with a
+    symmetric 4096 x 4096 upstream; MDS stress on 8192 x 32)."""
+    import torch
+    import oracle
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    rng = np.random.default_rng(21)
+    out = {}
+
+    def ev_time(fn, k):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    k = max(3, steps // 2)
+    # six metrics, 4000 x 100
+    base = torch.from_numpy(rng.standard_normal((4000, 100), dtype=np.float32)).to(dev)
+    bern = torch.from_numpy((rng.random((4000, 100)) < 0.3).astype(np.float32)).to(dev)
+    dout = torch.empty(4000 * 4000, dtype=torch.float32, device=dev)
+    methods = {}
+    for mi, m in enumerate(("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")):
+        pts = bern if m == "binary" else base
+        pw = 3.0 if m == "minkowski" else 2.0
+        fn = lambda: _lib.check(lib.gt_distances_device(vp(pts), 4000, 100, vp(dout), 0, mi,
+                                                        ctypes.c_float(pw), sptr))
+        ms = ev_time(fn, k)
+        methods[m] = {"ms": ms, "entries_per_s": 4000 * 4000 / (ms * 1e-3)}
+    out["dist_4000x100"] = methods
+    # kendall 500 obs x 1000 variables, integers 0..9
+    Xk = rng.integers(0, 10, (1000, 500)).astype(np.float32)
+    dXk = torch.from_numpy(Xk).to(dev)
+    tau = torch.empty((1000, 1000), dtype=torch.float64, device=dev)
+    lib.gt_profile_reset(); lib.gt_profile_enable(1)
+    ms = ev_time(lambda: _lib.check(lib.gt_kendall_device(vp(dXk), 1000, vp(dXk), 1000, 500,
+                                                          vp(tau), sptr)), k)
+    lib.gt_profile_enable(0)
+    cms = ctypes.c_double(); cn = ctypes.c_uint64()
+    lib.gt_profile_kernel_ms(b"kendall_count", ctypes.byref(cms), ctypes.byref(cn))
+    cols = rng.choice(1000, 6, replace=False); rows = rng.choice(1000, 6, replace=False)
+    want, *_ = oracle.kendall(Xk[cols], Xk[rows], same=False)
+    got = tau.cpu().numpy()[np.ix_(rows, cols)]
+    for a in range(6):
+        for b_ in range(6):
+            if rows[a] == cols[b_]:
+                want[a, b_] = 1.0
+    words = (500 // 2) * ((500 + 31) // 32)
+    pairs_tiles = 16 * 17 // 2 * 64 * 64          # 64 x 64 tiles on the upper triangle
+    count_ms = cms.value / max(1, cn.value)
+    out["kendall_500x1000"] = {
+        "ms": ms, "entries_per_s": 1e6 / (ms * 1e-3), "count_kernel_ms": count_ms,
+        "word_pairs_per_s": pairs_tiles * words / (count_ms * 1e-3),
+        "bit_exact_sample": bool(np.array_equal(got, want))}
+    # pearson 500 x 1000 and euclid 2000 x 64 end to end through the host ABI
+    Xp = rng.standard_normal((1000, 500)).astype(np.float32)
+    hc = np.empty((1000, 1000), np.float32); ht = np.empty_like(hc); hp = np.empty_like(hc)
+    fp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        _lib.check(lib.gt_pmcc(0, fp(Xp), 1000, fp(Xp), 1000, 500, fp(hp), fp(hc), fp(ht)))
+    out["pearson_500x1000_e2e"] = {"ms": (time.perf_counter() - t0) / k * 1e3}
+    pts = rng.standard_normal((2000, 64)).astype(np.float32)
+    hd = np.empty((2000, 2000), np.float32)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        _lib.check(lib.gt_distances(fp(pts), 2000, 64, fp(hd), 0, ctypes.c_float(2.0)))
+    out["euclid_2000x64_e2e"] = {"ms": (time.perf_counter() - t0) / k * 1e3}
+    # adjoints
+    Xb = torch.from_numpy(rng.standard_normal((4096, 1024), dtype=np.float32)).to(dev)
+    Gb = torch.from_numpy(rng.standard_normal((4096, 4096), dtype=np.float32)).to(dev)
+    Gb = (Gb + Gb.T) * 0.5
+    dXb = torch.empty_like(Xb)
+    ms = ev_time(lambda: _lib.check(lib.gt_cor_backward_device(vp(Xb), 4096, 1024, vp(Gb),
+                                                               vp(dXb), sptr)), k)
+    out["cor_backward_1024x4096"] = {"ms": ms, "useful_tflops": 2 * 4096 * 4096 * 1024 / (ms * 1e-3) / 1e12}
+    Xm = torch.from_numpy(rng.standard_normal((8192, 32), dtype=np.float32)).to(dev)
+    delta = torch.from_numpy(rng.random(8192 * 8191 // 2, dtype=np.float32) * 8).to(dev)
+    gm = torch.empty_like(Xm)
+    loss = torch.zeros(1, dtype=torch.float64, device=dev)
+    ms = ev_time(lambda: _lib.check(lib.gt_mds_stress_device(vp(Xm), 8192, 32, vp(delta), vp(gm),
+                                                             vp(loss), sptr)), k)
+    out["mds_stress_8192x32"] = {"ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3)}
+    return out
 
 
 def main():

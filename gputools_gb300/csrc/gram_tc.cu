@@ -1,5 +1,6 @@
 // gram_tc.cu -- split-bf16 Gram contractions on tcgen05 tensor cores, for
-// Pearson (gpuCor "everything") and Euclidean distances (gpuDist).
+// Pearson (gpuCor "everything"), Euclidean distances (gpuDist) and the
+// Pearson adjoint's GEMM.
 //
 // Reference: the contraction the reference performs as one n-length dot
 // product per 16-thread block (inst/cuda/correlation.cu:248-292
@@ -7,31 +8,38 @@
 // (inst/cuda/distance.cu:40-78).
 //
 // Operands.  Each value v (Pearson: the normalised column entry
-// z = (x - mean)/||x - mean|| computed in FP64; Euclidean: the raw float
-// coordinate) is split into bf16 parts v = v0 + v1 [+ v2] (round to nearest,
-// each part taken from the FP64 remainder of the previous ones).  The parts
-// live in separate planes [part][row][k] (K contiguous, K padded to a
-// multiple of 64 with zeros).  The Gram entry is the sum of the part
-// products whose order is at most NSPLIT-1:
+// z = (x - mean)/||x - mean|| computed in FP64 and rounded to float;
+// Euclidean: the centred coordinate) is split into bf16 parts
+// v = v0 + v1 [+ v2], each the round-to-nearest bf16 of the remainder of the
+// previous ones.  The parts live in separate planes [part][row][k] (K
+// contiguous, padded to a multiple of 64 with zeros).  The Gram entry is the
+// sum of the part products of total order at most NSPLIT-1:
 //   NSPLIT = 2 ("bf16x3"): v0w0 + v0w1 + v1w0            (~2^-16 relative)
-//   NSPLIT = 3 ("bf16x6"): + v0w2 + v1w1 + v2w0            (~2^-24: float32-exact)
-// accumulated in FP32 in tensor memory.
+//   NSPLIT = 3 ("bf16x6"): + v0w2 + v1w1 + v2w0            (float32-level)
 //
-// Kernel.  Persistent, one CTA per SM, 6 warps:
+// Accumulation.  The tensor core's FP32 accumulation rounds every add toward
+// zero, so its error grows linearly with the number of adds into one
+// accumulator (measured: about 2^-25 |acc| per add).  When CHUNKED, K is
+// split into chunks of `ckb` k-blocks; each chunk starts from zero in TMEM and
+// the epilogue adds it into FP32 registers with round-to-nearest.
+//
+// Kernel.  Persistent, one CTA per SM, 10 warps:
 //   warp 0      TMA producer: 3-D tensor loads (part plane, row block, K) of
-//               the A and B tiles into a STAGES-deep smem ring (128-byte or
-//               64-byte swizzle), completion tracked by mbarriers;
-//   warp 1      allocates 2 x BN TMEM columns (double-buffered 128 x BN FP32
-//               accumulator) and one thread issues tcgen05.mma (M = 128,
-//               N = BN, K = 16) for every part product, committing each stage
-//               back to the producer and each finished tile to the epilogue;
-//   warps 2..5  epilogue: tcgen05.ld of 32-column chunks (one TMEM lane = one
-//               output row per thread) and the fused Pearson / Euclidean
-//               finish, overlapped with the next tile's MMAs.
-// Symmetric problems (cor(x), gpuDist) schedule only the 128 x BN tiles that
-// meet the upper triangle and store each entry and its mirror.
+//               the A (128-row) and B (256-row) tiles into a smem ring
+//               (128- or 64-byte swizzle), completion tracked by mbarriers;
+//   warp 1      allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
+//               and one thread issues tcgen05.mma (M = 128, N = 256, K = 16)
+//               for every part product, committing each smem stage back to
+//               the producer and each finished chunk to the epilogue;
+//   warps 2..9  epilogue: two warps per TMEM lane quarter, 128 columns each;
+//               tcgen05.ld, then the fused Pearson / Euclidean / store finish,
+//               while the MMAs fill the other accumulator.
+// Symmetric problems (cor(x), gpuDist) schedule only the 128 x 256 tiles
+// that meet the upper triangle and store each entry and its mirror.  Each
+// warp writes rows through a padded 32 x 33 shared tile, so both orientations
+// are stored with coalesced 128-byte transactions.
 // Every mbarrier wait is bounded: on timeout the CTA raises an error word,
-// stops, releases its TMEM and exits.
+// drains its in-flight copies and MMAs, releases its TMEM and exits.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_ptx.cuh"
@@ -47,7 +55,9 @@ namespace gt {
 
 namespace {
 
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;                   // 2 control warps + 8 epilogue warps
+constexpr int kEpiWarps = 8;
+constexpr int kBM = 128, kBN = 256;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per barrier wait
 constexpr uint64_t kDrainLimitNs = 200000000ull;  // 0.2 s for in-flight work at exit
 constexpr int kKPad = 64;                         // K padding of the operand planes
@@ -56,14 +66,14 @@ constexpr int kEpiTileFloats = 32 * 33;           // one warp's padded 32 x 32 s
 
 // ----------------------------------------------------------------- tiling
 struct TileSpace {
-  int64_t tr, tc;    // row blocks (128), column blocks (BN)
+  int64_t tr, tc;    // row blocks (128), column blocks (256)
   int64_t j0;        // symmetric: column blocks whose tile count is 2*tj + 2
   int64_t ntiles;
   int symmetric;
 };
 
 // Symmetric problems: column block tj holds row blocks 0 .. min(2 tj + 1, tr-1)
-// (the 128-row blocks that reach the upper triangle of a BN = 256 column block).
+// (the 128-row blocks that reach the upper triangle of a 256-column block).
 __host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t, int64_t &ti,
                                             int64_t &tj) {
   if (!ts.symmetric) {
@@ -85,13 +95,12 @@ __host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t, int6
   }
 }
 
-TileSpace make_tiles(int64_t nr, int64_t nc, int bn, bool symmetric) {
+TileSpace make_tiles(int64_t nr, int64_t nc, bool symmetric) {
   TileSpace ts;
-  ts.tr = cdiv(nr, 128);
-  ts.tc = cdiv(nc, bn);
+  ts.tr = cdiv(nr, kBM);
+  ts.tc = cdiv(nc, kBN);
   ts.symmetric = symmetric ? 1 : 0;
   if (symmetric) {
-    // requires bn == 256: column block tj meets row blocks 0 .. 2 tj + 1
     ts.j0 = ts.tr / 2;
     if (ts.j0 > ts.tc) ts.j0 = ts.tc;
     ts.ntiles = ts.j0 * (ts.j0 + 1) + (ts.tc - ts.j0) * ts.tr;
@@ -102,34 +111,69 @@ TileSpace make_tiles(int64_t nr, int64_t nc, int bn, bool symmetric) {
   return ts;
 }
 
-// ----------------------------------------------------------------- epilogues
+// ----------------------------------------------------------------- finishes
+// Each finish handles a warp's 32 x 32 block: lane = row r (consecutive rows
+// across lanes), g[j] = entry (r, c0 + j); wsm is the warp's staging tile.
+
 __device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
 
-__device__ __forceinline__ float signif(float r, float pairs) {
+// hostSignif's rule (src/correlation.cpp:51-64), t = r sqrt(n-2) / sqrt(1-r^2)
+// with sqrt(n-2) precomputed and a hardware reciprocal square root.
+__device__ __forceinline__ float signif_fast(float r, float sq_nm2) {
   if (r >= 0.999f) return 10000.0f;
-  return r * sqrtf((pairs - 2.f) / (1.f - r * r));
+  return r * sq_nm2 * tc::rsqrt_approx(1.f - r * r);
 }
 
-// Stores 32 consecutive floats of one output row: 128-bit stores when the
-// address allows, scalar otherwise.
-__device__ __forceinline__ void store_row32(float *p, const float (&v)[32]) {
-  if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-    float4 *q = reinterpret_cast<float4 *>(p);
+struct PearsonFinish {
+  float *corr, *ts, *pairs;
+  int64_t ld, nr, nc;
+  float npairs, sq_nm2;
+  int symmetric;
+
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+    const int lane = threadIdx.x & 31;
+    // mirror orientation (lanes hold consecutive rows): coalesced from registers
+    if (symmetric && r < nr) {
 #pragma unroll
-    for (int j = 0; j < 8; j++) q[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-  } else {
+      for (int j = 0; j < 32; j++) {
+        const int64_t c = c0 + j;
+        if (c < nc && r < c) {
+          const float v = clamp_r(g[j]);
+          const int64_t o = c * ld + r;
+          if (corr) corr[o] = v;
+          if (ts) ts[o] = signif_fast(v, sq_nm2);
+          if (pairs) pairs[o] = npairs;
+        }
+      }
+    }
+    // row orientation through the staging tile
 #pragma unroll
-    for (int j = 0; j < 32; j++) p[j] = v[j];
+    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
+    __syncwarp();
+    const int64_t rbase = r - lane;
+    const int64_t c = c0 + lane;
+    int64_t o = rbase * ld + c;
+    for (int i = 0; i < 32; i++, o += ld) {
+      const int64_t ri = rbase + i;
+      if (ri >= nr) break;
+      if (c >= nc || (symmetric && c < ri)) continue;
+      float v = clamp_r(wsm[i * 33 + lane]);
+      if (symmetric && c == ri && v == v) v = 1.f;
+      if (corr) corr[o] = v;
+      if (ts) ts[o] = signif_fast(v, sq_nm2);
+      if (pairs) pairs[o] = npairs;
+    }
+    __syncwarp();
   }
-}
+};
 
 // Operands are the points centred by their column means (distances do not
 // change).  d^2 = |a|^2 + |b|^2 - 2 G with FP32 norms rounded from FP64; an
 // entry whose d^2 is below tau * (|a|^2 + |b|^2), where rounding of the
 // contraction could dominate, is recomputed from the original float points
-// by the warp: float differences, float partial sums of squares per lane,
-// FP64 sum across lanes.  Exact duplicates therefore come out exactly 0.
-struct EuclidEpi {
+// by the warp (float differences and partial sums per lane, FP64 sum across
+// lanes), so exact duplicates come out exactly 0.
+struct EuclidFinish {
   const float *norm2;
   const float *pts;
   float *out;
@@ -140,19 +184,22 @@ struct EuclidEpi {
   __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const int64_t cl = c0 + lane;
+    const float nbl = cl < n ? norm2[cl] : 0.f;
+    const float na = r < n ? norm2[r] : 0.f;
+    // this lane's row uses columns c0 + j with r < c0 + j < n
+    const int64_t lo64 = r + 1 - c0, hi64 = n - c0;
+    const int jlo = lo64 < 0 ? 0 : (lo64 > 32 ? 32 : int(lo64));
+    const int jhi = r >= n ? 0 : (hi64 > 32 ? 32 : (hi64 < 0 ? 0 : int(hi64)));
     float v[32];
     unsigned pend = 0u;
-    const float na = r < n ? norm2[r] : 0.f;
 #pragma unroll
     for (int j = 0; j < 32; j++) {
-      const int64_t c = c0 + j;
-      v[j] = 0.f;
-      if (r < n && c < n && r < c) {
-        const float s = na + norm2[c];
-        const float d2 = fmaf(-2.f, g[j], s);
-        if (d2 < tau * s) pend |= 1u << j;
-        else v[j] = sqrtf(d2);
-      }
+      const float s = na + __shfl_sync(FULL, nbl, j);
+      const float d2 = fmaf(-2.f, g[j], s);
+      const bool valid = (j >= jlo) & (j < jhi);
+      pend |= unsigned(valid & (d2 < tau * s)) << j;
+      v[j] = valid ? tc::sqrt_approx(fmaxf(d2, 0.f)) : 0.f;
     }
     while (true) {
       const unsigned any = __ballot_sync(FULL, pend != 0u);
@@ -160,8 +207,7 @@ struct EuclidEpi {
       const int src = __ffs(int(any)) - 1;
       const int j = __shfl_sync(FULL, __ffs(int(pend)) - 1, src);
       const long long rr = __shfl_sync(FULL, (long long)r, src);
-      const int64_t c = c0 + j;
-      const float *pa = pts + rr * dim, *pb = pts + c * dim;
+      const float *pa = pts + rr * dim, *pb = pts + (c0 + j) * dim;
       float part = 0.f;
       for (int64_t k = lane; k < dim; k += 32) {
         const float d = pa[k] - pb[k];
@@ -171,60 +217,74 @@ struct EuclidEpi {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
       if (lane == src) {
-        const float d2 = float(acc);
+        const float d = sqrtf(float(acc));
 #pragma unroll
         for (int q = 0; q < 32; q++)
-          if (q == j) v[q] = sqrtf(d2);
+          if (q == j) v[q] = d;
         pend &= ~(1u << j);
       }
     }
-    // mirror orientation (lanes hold consecutive rows): coalesced from registers
-    if (layout == GT_LAYOUT_FULL && r < n) {
+    const bool full = layout == GT_LAYOUT_FULL;
+    if (full && r < n) {
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int64_t c = c0 + j;
-        if (c < n && r < c) out[c * n + r] = v[j];
-      }
+      for (int j = 0; j < 32; j++)
+        if (j >= jlo && j < jhi) out[(c0 + j) * n + r] = v[j];
     }
-    // row orientation: transpose the warp's 32 x 32 block through shared memory
 #pragma unroll
     for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = v[j];
     __syncwarp();
-    const int64_t rbase = r - lane;
-    const int64_t c = c0 + lane;
+    const int64_t rbase = r - lane, c = c0 + lane;
+    // offset of (row rbase, column 0): full n*r; R dist n*r - r(r+1)/2 - r - 1
+    int64_t off = full ? rbase * n : n * rbase - rbase * (rbase + 1) / 2 - rbase - 1;
     for (int i = 0; i < 32; i++) {
       const int64_t ri = rbase + i;
       if (ri >= n) break;
-      const float x = wsm[i * 33 + lane];
-      if (c >= n || c < ri) continue;
-      if (layout == GT_LAYOUT_FULL) {
-        out[ri * n + c] = (c == ri) ? 0.f : x;
-      } else if (c > ri) {
-        // R dist vector: entry (i = c, j = ri) at n*ri - ri*(ri+1)/2 + c - ri - 1
-        out[n * ri - ri * (ri + 1) / 2 + c - ri - 1] = x;
+      if (c < n) {
+        if (full) {
+          if (c >= ri) out[off + c] = (c == ri) ? 0.f : wsm[i * 33 + lane];
+        } else if (c > ri) {
+          out[off + c] = wsm[i * 33 + lane];
+        }
       }
+      off += full ? n : n - ri - 2;
+    }
+    __syncwarp();
+  }
+};
+
+// Plain FP32 store of the contraction, C[r*ld + c].
+struct StoreFinish {
+  float *out;
+  int64_t ld, nr, nc;
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
+    __syncwarp();
+    const int64_t rbase = r - lane, c = c0 + lane;
+    for (int i = 0; i < 32; i++) {
+      const int64_t ri = rbase + i;
+      if (ri >= nr) break;
+      if (c < nc) out[ri * ld + c] = wsm[i * 33 + lane];
     }
     __syncwarp();
   }
 };
 
 // ----------------------------------------------------------------- kernel
-template <int NSPLIT, int BN, int BK, int EPI_WARPS>
+template <int NSPLIT, int BK>
 struct TcCfg {
-  static constexpr int BM = 128;
   static constexpr int ROW_BYTES = BK * 2;                // 128 or 64
-  static constexpr int A_TILE = BM * BK * 2;
-  static constexpr int B_TILE = BN * BK * 2;
+  static constexpr int A_TILE = kBM * BK * 2;
+  static constexpr int B_TILE = kBN * BK * 2;
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
-  // per epilogue warp: a 32 x 33 float tile for transposing its stores
-  static constexpr int EPI_BYTES = EPI_WARPS * kEpiTileFloats * 4;
+  static constexpr int EPI_BYTES = kEpiWarps * kEpiTileFloats * 4;
   static constexpr int STAGES_RAW = (kMaxSmem - 1024 - 256 - EPI_BYTES) / STAGE;
   static constexpr int STAGES = STAGES_RAW > 6 ? 6 : STAGES_RAW;
   static constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/ + EPI_BYTES;
   static constexpr int KSTEPS = BK / 16;
   static constexpr int NPROD = NSPLIT == 2 ? 3 : 6;
   static_assert(STAGES >= 2, "need at least two stages");
-  static_assert(2 * BN <= 512, "accumulators exceed TMEM");
 };
 
 template <int NSPLIT>
@@ -239,11 +299,11 @@ __device__ __forceinline__ void product_parts(int p, int &pa, int &pb) {
   }
 }
 
-template <int NSPLIT, int BN, int BK, class Epi>
+template <int NSPLIT, int BK, bool CHUNKED, class Fin>
 __global__ void __launch_bounds__(kTcThreads, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-               TileSpace tiles, int64_t nk, Epi epi, int *err) {
-  using C = TcCfg<NSPLIT, BN, BK, 4>;
+               TileSpace tiles, int64_t nk, int64_t ckb, Fin fin, int *err) {
+  using C = TcCfg<NSPLIT, BK>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -264,7 +324,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     }
     for (int b = 0; b < 2; b++) {
       tc::mbar_init(&accf[b], 1);
-      tc::mbar_init(&acce[b], 4);
+      tc::mbar_init(&acce[b], kEpiWarps);
     }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -274,11 +334,13 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     tc::prefetch_tensormap(&mapA);
     tc::prefetch_tensormap(&mapB);
   }
-  if (warp == 1) tc::tmem_alloc(tmem_slot, 2 * BN);
+  if (warp == 1) tc::tmem_alloc(tmem_slot, 2 * kBN);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  if (!CHUNKED) ckb = nk;
+  const int64_t nchunks = (nk + ckb - 1) / ckb;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -299,15 +361,14 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
             tc::tma_load_3d(st + p * C::A_TILE, &mapA, &full[s], int32_t(kb * BK),
-                            int32_t(ti * C::BM), p);
+                            int32_t(ti * kBM), p);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
             tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, &mapB, &full[s],
-                            int32_t(kb * BK), int32_t(tj * BN), p);
+                            int32_t(kb * BK), int32_t(tj * kBN), p);
         }
       }
-      // drain: wait (bounded) for loads that were issued but not consumed, so
-      // no bulk copy is still writing shared memory when the CTA exits
+      // drain: no bulk copy may still be writing shared memory at exit
       if (*abort_flag) {
         for (int s = 0; s < C::STAGES; s++) {
           const int64_t fills = it / C::STAGES + (s < it % C::STAGES ? 1 : 0);
@@ -319,227 +380,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   } else if (warp == 1) {
     if (lane == 0) {
       // ------------------------------------------------ MMA issuer
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(128, BN);
-      int64_t it = 0, local = 0;
-      for (int64_t t = blockIdx.x; t < tiles.ntiles; t += gridDim.x, local++) {
-        const int buf = int(local & 1);
-        const uint32_t ause = uint32_t(local >> 1);
-        if (!tc::mbar_wait(&acce[buf], (ause & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
-          *abort_flag = 1;
-          break;
-        }
-        tc::tc_fence_after();
-        const uint32_t d = tmem_base + uint32_t(buf * BN);
-        bool ok = true;
-        for (int64_t kb = 0; kb < nk; kb++, it++) {
-          const int s = int(it % C::STAGES);
-          const uint32_t use = uint32_t(it / C::STAGES);
-          if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, kWaitLimitNs)) {
-            ok = false;
-            break;
-          }
-          tc::tc_fence_after();
-          const uint32_t sa = tc::smem_u32(smem + s * C::STAGE);
-          const uint32_t sb = sa + NSPLIT * C::A_TILE;
-#pragma unroll
-          for (int k = 0; k < C::KSTEPS; k++) {
-#pragma unroll
-            for (int p = 0; p < C::NPROD; p++) {
-              int pa, pb;
-              product_parts<NSPLIT>(p, pa, pb);
-              const uint64_t ad = tc::smem_desc_kmajor(sa + pa * C::A_TILE + k * 32, C::ROW_BYTES);
-              const uint64_t bd = tc::smem_desc_kmajor(sb + pb * C::B_TILE + k * 32, C::ROW_BYTES);
-              tc::umma_bf16(d, ad, bd, idesc, (kb | k | p) != 0 ? 1u : 0u);
-            }
-          }
-          tc::umma_commit(&empty[s]);
-        }
-        if (!ok) {
-          *abort_flag = 1;
-          break;
-        }
-        tc::umma_commit(&accf[buf]);
-      }
-      // every MMA issued above has finished before TMEM is released
-      tc::umma_commit(mma_done);
-      tc::mbar_wait_bounded(mma_done, 0u, kDrainLimitNs);
-    }
-    __syncwarp();
-  } else {
-    // -------------------------------------------------- epilogue (warps 2..5)
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
-    int64_t local = 0;
-    for (int64_t t = blockIdx.x; t < tiles.ntiles; t += gridDim.x, local++) {
-      int64_t ti, tj;
-      tile_coords(tiles, t, ti, tj);
-      const int buf = int(local & 1);
-      const uint32_t ause = uint32_t(local >> 1);
-      const bool ok = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
-      if (!__all_sync(0xffffffffu, ok)) {
-        *abort_flag = 1;
-        break;
-      }
-      tc::tc_fence_after();
-      const int64_t r = ti * 128 + q * 32 + lane;
-      const uint32_t tbase = tmem_base + uint32_t(buf * BN) + (uint32_t(q * 32) << 16);
-#pragma unroll 1
-      for (int c = 0; c < BN; c += 32) {
-        float g[32];
-        tc::tmem_ld32(tbase + uint32_t(c), g);
-        epi(r, tj * BN + c, g, epi_smem + (warp - 2) * kEpiTileFloats);
-      }
-      tc::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acce[buf]);
-    }
-  }
-  __syncthreads();
-  if (*abort_flag && threadIdx.x == 0) atomicExch(err, 1);
-  if (warp == 1) {
-    tc::tc_fence_after();
-    tc::tmem_dealloc(tmem_base, 2 * BN);
-  }
-}
-
-// ----------------------------------------------------------------- chunked kernel
-// The tensor core's FP32 accumulation rounds every add toward zero, so its
-// error grows linearly with the number of adds into one accumulator (about
-// 2^-25 |acc| per add).  For the Pearson contraction, K is split into chunks
-// of `ckb` k-blocks: each chunk is accumulated in TMEM from zero, and the
-// epilogue warps add the chunk into FP32 registers with round-to-nearest.
-// Eight epilogue warps (two per TMEM lane quarter, 128 columns each) hold the
-// 128 x 256 running sums; chunks alternate between the two TMEM accumulators
-// so the MMAs of chunk c+1 overlap the epilogue's add of chunk c.
-constexpr int kTcChunkThreads = 320;
-
-// Pearson finish of a warp's 32 x 32 block (lane = row, 32 consecutive
-// columns in registers): r = clamp(G), hostSignif's t-score and the pair
-// count, stored row-wise through the warp's staging tile and, for cor(x),
-// mirrored column-wise; both kinds of store are coalesced.
-struct PearsonFinish {
-  float *corr, *ts, *pairs;
-  int64_t ld, nr, nc;
-  float npairs;
-  int symmetric;
-
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
-    const int lane = threadIdx.x & 31;
-    // mirror orientation (lanes hold consecutive rows): coalesced from registers
-    if (symmetric && r < nr) {
-#pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int64_t c = c0 + j;
-        if (c < nc && r < c) {
-          const float v = clamp_r(g[j]);
-          const int64_t o = c * ld + r;
-          if (corr) corr[o] = v;
-          if (ts) ts[o] = signif(v, npairs);
-          if (pairs) pairs[o] = npairs;
-        }
-      }
-    }
-    // row orientation: transpose the warp's 32 x 32 block through shared memory
-#pragma unroll
-    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-    __syncwarp();
-    const int64_t rbase = r - lane;
-    const int64_t c = c0 + lane;
-    for (int i = 0; i < 32; i++) {
-      const int64_t ri = rbase + i;
-      if (ri >= nr) break;
-      const float x = wsm[i * 33 + lane];
-      if (c >= nc || (symmetric && c < ri)) continue;
-      float v = clamp_r(x);
-      if (symmetric && c == ri && v == v) v = 1.f;
-      const int64_t o = ri * ld + c;
-      if (corr) corr[o] = v;
-      if (ts) ts[o] = signif(v, npairs);
-      if (pairs) pairs[o] = npairs;
-    }
-    __syncwarp();
-  }
-};
-
-template <int NSPLIT, int BN, int BK, class Fin>
-__global__ void __launch_bounds__(kTcChunkThreads, 1)
-gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
-                       const __grid_constant__ CUtensorMap mapB, TileSpace tiles, int64_t nk,
-                       int64_t ckb, Fin fin, int *err) {
-  using C = TcCfg<NSPLIT, BN, BK, 8>;
-  static_assert(BN == 256, "chunked kernel: two epilogue warps of 128 columns per lane quarter");
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                              ~uintptr_t(1023));
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + C::STAGES * C::STAGE);
-  uint64_t *empty = full + C::STAGES;
-  uint64_t *accf = empty + C::STAGES;
-  uint64_t *acce = accf + 2;
-  uint64_t *mma_done = acce + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-  float *epi_smem = reinterpret_cast<float *>(smem + C::STAGES * C::STAGE + 256);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < C::STAGES; s++) {
-      tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1);
-    }
-    for (int b = 0; b < 2; b++) {
-      tc::mbar_init(&accf[b], 1);
-      tc::mbar_init(&acce[b], 8);
-    }
-    tc::mbar_init(mma_done, 1);
-    *abort_flag = 0;
-    tc::fence_barrier_init();
-  }
-  if (warp == 0 && lane == 0) {
-    tc::prefetch_tensormap(&mapA);
-    tc::prefetch_tensormap(&mapB);
-  }
-  if (warp == 1) tc::tmem_alloc(tmem_slot, 2 * BN);
-  tc::tc_fence_before();
-  __syncthreads();
-  tc::tc_fence_after();
-  const uint32_t tmem_base = *tmem_slot;
-  const int64_t nchunks = (nk + ckb - 1) / ckb;
-
-  if (warp == 0) {
-    if (lane == 0) {
-      int64_t it = 0;
-      for (int64_t t = blockIdx.x; t < tiles.ntiles && !*abort_flag; t += gridDim.x) {
-        int64_t ti, tj;
-        tile_coords(tiles, t, ti, tj);
-        for (int64_t kb = 0; kb < nk; kb++, it++) {
-          const int s = int(it % C::STAGES);
-          const uint32_t use = uint32_t(it / C::STAGES);
-          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
-            *abort_flag = 1;
-            break;
-          }
-          uint8_t *st = smem + s * C::STAGE;
-          tc::mbar_arrive_expect_tx(&full[s], C::STAGE);
-#pragma unroll
-          for (int p = 0; p < NSPLIT; p++)
-            tc::tma_load_3d(st + p * C::A_TILE, &mapA, &full[s], int32_t(kb * BK),
-                            int32_t(ti * C::BM), p);
-#pragma unroll
-          for (int p = 0; p < NSPLIT; p++)
-            tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, &mapB, &full[s],
-                            int32_t(kb * BK), int32_t(tj * BN), p);
-        }
-      }
-      if (*abort_flag) {
-        for (int s = 0; s < C::STAGES; s++) {
-          const int64_t fills = it / C::STAGES + (s < it % C::STAGES ? 1 : 0);
-          if (fills > 0) tc::mbar_wait_bounded(&full[s], uint32_t((fills - 1) & 1), kDrainLimitNs);
-        }
-      }
-    }
-    __syncwarp();
-  } else if (warp == 1) {
-    if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(128, BN);
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
       int64_t it = 0, cc = 0;
       bool ok = true;
       for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
@@ -551,8 +392,8 @@ gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
             break;
           }
           tc::tc_fence_after();
-          const uint32_t d = tmem_base + uint32_t(buf * BN);
-          const int64_t kb0 = ch * ckb, kb1 = min(nk, kb0 + ckb);
+          const uint32_t d = tmem_base + uint32_t(buf * kBN);
+          const int64_t kb0 = ch * ckb, kb1 = (kb0 + ckb < nk) ? kb0 + ckb : nk;
           for (int64_t kb = kb0; kb < kb1; kb++, it++) {
             const int s = int(it % C::STAGES);
             const uint32_t use = uint32_t(it / C::STAGES);
@@ -580,23 +421,58 @@ gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
         }
       }
       if (!ok) *abort_flag = 1;
+      // every MMA issued above has finished before TMEM is released
       tc::umma_commit(mma_done);
       tc::mbar_wait_bounded(mma_done, 0u, kDrainLimitNs);
     }
     __syncwarp();
   } else {
     // ------------------------------------------ epilogue (warps 2..9)
-    const int q = warp & 3;                  // TMEM lane quarter
-    const int half = (warp - 2) >> 2;        // column half: 0 or 1
+    const int q = warp & 3;            // TMEM lane quarter
+    const int half = (warp - 2) >> 2;  // column half: 0 or 1
+    float *wsm = epi_smem + (warp - 2) * kEpiTileFloats;
     int64_t cc = 0;
     bool ok = true;
     for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
       int64_t ti, tj;
       tile_coords(tiles, t, ti, tj);
-      float acc[128];
+      const int64_t r = ti * kBM + q * 32 + lane;
+      const int64_t col = tj * kBN + half * 128;
+      if (CHUNKED) {
+        float acc[128];
 #pragma unroll
-      for (int j = 0; j < 128; j++) acc[j] = 0.f;
-      for (int64_t ch = 0; ch < nchunks; ch++, cc++) {
+        for (int j = 0; j < 128; j++) acc[j] = 0.f;
+        for (int64_t ch = 0; ch < nchunks; ch++, cc++) {
+          const int buf = int(cc & 1);
+          const uint32_t ause = uint32_t(cc >> 1);
+          const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
+          if (!__all_sync(0xffffffffu, got)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t tb =
+              tmem_base + uint32_t(buf * kBN + half * 128) + (uint32_t(q * 32) << 16);
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            float g[16];
+            tc::tmem_ld16(tb + uint32_t(16 * i), g);
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc[16 * i + j] += g[j];
+          }
+          tc::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&acce[buf]);
+        }
+        if (!ok) break;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          float g[32];
+#pragma unroll
+          for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
+          fin(r, col + 32 * i, g, wsm);
+        }
+      } else {
         const int buf = int(cc & 1);
         const uint32_t ause = uint32_t(cc >> 1);
         const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
@@ -605,27 +481,17 @@ gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
           break;
         }
         tc::tc_fence_after();
-        const uint32_t tbase =
-            tmem_base + uint32_t(buf * BN + half * 128) + (uint32_t(q * 32) << 16);
-#pragma unroll
+        const uint32_t tb = tmem_base + uint32_t(buf * kBN + half * 128) + (uint32_t(q * 32) << 16);
+#pragma unroll 1
         for (int i = 0; i < 4; i++) {
           float g[32];
-          tc::tmem_ld32(tbase + uint32_t(32 * i), g);
-#pragma unroll
-          for (int j = 0; j < 32; j++) acc[32 * i + j] += g[j];
+          tc::tmem_ld32(tb + uint32_t(32 * i), g);
+          fin(r, col + 32 * i, g, wsm);
         }
         tc::tc_fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&acce[buf]);
-      }
-      if (!ok) break;
-      const int64_t r = ti * 128 + q * 32 + lane;
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        float g[32];
-#pragma unroll
-        for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
-        fin(r, tj * BN + half * 128 + 32 * i, g, epi_smem + (warp - 2) * kEpiTileFloats);
+        cc++;
       }
     }
     if (!ok) *abort_flag = 1;
@@ -634,7 +500,7 @@ gram_tc_chunked_kernel(const __grid_constant__ CUtensorMap mapA,
   if (*abort_flag && threadIdx.x == 0) atomicExch(err, 1);
   if (warp == 1) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem_base, 2 * BN);
+    tc::tmem_dealloc(tmem_base, 2 * kBN);
   }
 }
 
@@ -725,7 +591,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D map over planes [NSPLIT][rows][kpad] of bf16; box {BK, box_rows, 1}.
+// 3-D map over planes [nsplit][rows][kpad] of bf16; box {bk, box_rows, 1}.
 int make_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad, int nsplit,
                    int box_rows, int bk) {
   auto fn = encode_fn();
@@ -751,65 +617,29 @@ int err_word(int **p) {
   return GT_OK;
 }
 
-template <int NSPLIT, int BN, int BK, class Epi>
+template <int NSPLIT, int BK, bool CHUNKED, class Fin>
 int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
-                bool symmetric, const Epi &epi, const char *prof_name, cudaStream_t s) {
-  using C = TcCfg<NSPLIT, BN, BK, 4>;
-  if (symmetric && BN != 256) return fail(GT_EINVAL, "symmetric tiling needs BN = 256");
-  if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
-  CUtensorMap mA, mB;
-  GT_TRY(make_plane_map(&mA, zA, nA, kpad, NSPLIT, 128, BK));
-  GT_TRY(make_plane_map(&mB, zB, nB, kpad, NSPLIT, BN, BK));
-  const TileSpace ts = make_tiles(nA, nB, BN, symmetric);
-  if (ts.ntiles == 0) return GT_OK;
-  int *err = nullptr;
-  GT_TRY(err_word(&err));
-  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  auto kern = gram_tc_kernel<NSPLIT, BN, BK, Epi>;
-  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-  const int64_t grid = ts.ntiles < sm_count() ? ts.ntiles : sm_count();
-  ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), kTcThreads, C::SMEM, s>>>(mA, mB, ts, kpad / BK, epi, err);
-  count_launch();
-  GT_CUDA(cudaGetLastError());
-  return GT_OK;
-}
-
-template <int NSPLIT, int BK, class Fin>
-int launch_gram_chunked(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
-                        bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
-                        cudaStream_t s) {
-  constexpr int BN = 256;
-  using C = TcCfg<NSPLIT, BN, BK, 8>;
+                bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
+                cudaStream_t s) {
+  using C = TcCfg<NSPLIT, BK>;
   if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
   if (ckb < 1) ckb = 1;
   CUtensorMap mA, mB;
-  GT_TRY(make_plane_map(&mA, zA, nA, kpad, NSPLIT, 128, BK));
-  GT_TRY(make_plane_map(&mB, zB, nB, kpad, NSPLIT, BN, BK));
-  const TileSpace ts = make_tiles(nA, nB, BN, symmetric);
+  GT_TRY(make_plane_map(&mA, zA, nA, kpad, NSPLIT, kBM, BK));
+  GT_TRY(make_plane_map(&mB, zB, nB, kpad, NSPLIT, kBN, BK));
+  const TileSpace ts = make_tiles(nA, nB, symmetric);
   if (ts.ntiles == 0) return GT_OK;
   int *err = nullptr;
   GT_TRY(err_word(&err));
   GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  auto kern = gram_tc_chunked_kernel<NSPLIT, BN, BK, Fin>;
+  auto kern = gram_tc_kernel<NSPLIT, BK, CHUNKED, Fin>;
   GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
   const int64_t grid = ts.ntiles < sm_count() ? ts.ntiles : sm_count();
   ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), kTcChunkThreads, C::SMEM, s>>>(mA, mB, ts, kpad / BK, ckb, fin, err);
+  kern<<<unsigned(grid), kTcThreads, C::SMEM, s>>>(mA, mB, ts, kpad / BK, ckb, fin, err);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
-}
-
-// k-blocks per accumulation chunk of the Pearson contraction (0 = one chunk).
-int64_t tc_chunk_kblocks(int bk) {
-  static int64_t elems = -1;
-  if (elems < 0) {
-    const char *e = std::getenv("GT_TC_CHUNK");
-    elems = e ? std::atoll(e) : 256;
-  }
-  if (elems <= 0) return int64_t(1) << 40;
-  return elems / bk > 0 ? elems / bk : 1;
 }
 
 int tc_config() {
@@ -821,25 +651,17 @@ int tc_config() {
   return cfg;
 }
 
-// Plain FP32 store of the contraction, C[r*ld + c] (rows through the warp's
-// staging tile so every store is coalesced).
-struct StoreFinish {
-  float *out;
-  int64_t ld, nr, nc;
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-    __syncwarp();
-    const int64_t rbase = r - lane, c = c0 + lane;
-    for (int i = 0; i < 32; i++) {
-      const int64_t ri = rbase + i;
-      if (ri >= nr) break;
-      if (c < nc) out[ri * ld + c] = wsm[i * 33 + lane];
-    }
-    __syncwarp();
+// k-blocks per accumulation chunk of the Pearson contraction (GT_TC_CHUNK
+// elements, default 256; 0 = a single chunk).
+int64_t tc_chunk_kblocks(int bk) {
+  static int64_t elems = -1;
+  if (elems < 0) {
+    const char *e = std::getenv("GT_TC_CHUNK");
+    elems = e ? std::atoll(e) : 256;
   }
-};
+  if (elems <= 0) return int64_t(1) << 40;
+  return elems / bk > 0 ? elems / bk : 1;
+}
 
 }  // namespace
 
@@ -850,10 +672,10 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
   if (nA == 0 || nB == 0) return GT_OK;
   StoreFinish fin{C, ldc, nA, nB};
   if (nsplit == 3)
-    return launch_gram_chunked<3, 32>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(32),
-                                      fin, "gemm_store", s);
-  return launch_gram_chunked<2, 64>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(64),
+    return launch_gram<3, 32, true>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(32),
                                     fin, "gemm_store", s);
+  return launch_gram<2, 64, true>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(64),
+                                  fin, "gemm_store", s);
 }
 
 int tc_check_error(cudaStream_t s, bool *failed) {
@@ -895,22 +717,23 @@ int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t k
                const PearsonOut &out, cudaStream_t s) {
   if (nA == 0 || nB == 0) return GT_OK;
   if (!out.corr && !out.ts && !out.pairs) return GT_OK;
-  PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs, out.symmetric};
+  PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
+                    std::sqrt(out.npairs - 2.f), out.symmetric};
   const bool sym = out.symmetric != 0;
   if (nsplit == 3)
-    return launch_gram_chunked<3, 32>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
-                                      "pearson_gram", s);
-  if (tc_config() == 32)
-    return launch_gram_chunked<2, 32>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
-                                      "pearson_gram", s);
-  return launch_gram_chunked<2, 64>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64), fin,
+    return launch_gram<3, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
                                     "pearson_gram", s);
+  if (tc_config() == 32)
+    return launch_gram<2, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
+                                    "pearson_gram", s);
+  return launch_gram<2, 64, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64), fin,
+                                  "pearson_gram", s);
 }
 
 int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
               cudaStream_t st) {
   if (dim == 0 || n < 2) return dist_simt(d_pts, n, dim, d_out, layout, GT_EUCLIDEAN, 2.f, st);
-  // Output writes bound this kernel at moderate dim, so the float32-exact
+  // Output writes bound this kernel at moderate dim, so the float32-level
   // 3-way split costs nothing over the 2-way one: always use it.
   constexpr int NS = 3;
   const int64_t kpad = cdiv(dim, kKPad) * kKPad;
@@ -935,8 +758,8 @@ int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
     GT_CUDA(cudaGetLastError());
   }
   // Entries with d^2 below an eighth of |a|^2 + |b|^2 are recomputed exactly.
-  EuclidEpi epi{norm2, d_pts, d_out, n, dim, layout, 0.125f};
-  return launch_gram<NS, 256, 32>(z, n, z, n, kpad, true, epi, "euclid_gram", st);
+  EuclidFinish fin{norm2, d_pts, d_out, n, dim, layout, 0.125f};
+  return launch_gram<NS, 32, false>(z, n, z, n, kpad, true, 0, fin, "euclid_gram", st);
 }
 
 }  // namespace gt
