@@ -602,7 +602,63 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     ms = ev_time(lambda: _lib.check(lib.gt_mds_stress_device(vp(Xm), 8192, 32, vp(delta), vp(gm),
                                                              vp(loss), sptr)), k)
     out["mds_stress_8192x32"] = {"ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3)}
+    del Xb, Gb, dXb, Xm, delta, gm
+    torch.cuda.empty_cache()
+    out["batch"] = run_batches(g, stream, dev, k)
     return out
+
+
+def run_batches(g, stream, dev, k):
+    """2000 independent Pearson problems (variables log-uniform in [16, 4096],
+    observations log-uniform in [50, 2000], N(0,1)) and 500 Kendall problems
+    (200 observations, log-uniform [8, 512] integer variables 0..19), each batch
+    one plan replayed from a CUDA graph."""
+    import torch
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(17)
+    rng = np.random.default_rng(17)
+    res = {}
+    ps = np.exp(rng.uniform(np.log(16), np.log(4096), 2000)).astype(int)
+    ns = np.exp(rng.uniform(np.log(50), np.log(2000), 2000)).astype(int)
+    xs = [torch.randn((int(p), int(n)), generator=gen, device=dev, dtype=torch.float32)
+          for p, n in zip(ps, ns)]
+    entries = float(np.sum(ps.astype(np.float64) ** 2))
+    useful = float(np.sum(2.0 * ps.astype(np.float64) ** 2 * ns))
+    t0 = time.perf_counter()
+    plan = g.BatchPlan(xs, "pearson", autotune=True)
+    build_s = time.perf_counter() - t0
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    plan.launch(stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(k):
+        plan.launch(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    res["pearson_2000"] = {"ms": ms, "entries": entries, "entries_per_s": entries / (ms * 1e-3),
+                           "useful_tflops": useful / (ms * 1e-3) / 1e12, "plan": plan.describe(),
+                           "plan_build_s": build_s, "launches_per_step": "1 graph"}
+    plan.close()
+    del xs
+    torch.cuda.empty_cache()
+    kp = np.exp(rng.uniform(np.log(8), np.log(512), 500)).astype(int)
+    ks = [torch.from_numpy(rng.integers(0, 20, (int(p), 200)).astype(np.float32)).to(dev)
+          for p in kp]
+    plan = g.BatchPlan(ks, "kendall")
+    plan.launch(stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(k):
+        plan.launch(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    kent = float(np.sum(kp.astype(np.float64) ** 2))
+    res["kendall_500"] = {"ms": ms, "entries": kent, "entries_per_s": kent / (ms * 1e-3),
+                          "plan": plan.describe()}
+    plan.close()
+    return res
 
 
 def main():

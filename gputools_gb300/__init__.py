@@ -6,12 +6,12 @@ The compute path is libgputools_gb300.so (hand-written CUDA for sm_103a) and
 its C ABI, include/gputools_gb300.h; this package is the Python mirror of the
 R API over that ABI.
 """
-from .api import (Dist, chooseGpu, distances_device, get_gram_path, getGpuId, gpuCor,
+from .api import (BatchPlan, Dist, chooseGpu, distances_device, get_gram_path, getGpuId, gpuCor,
                   gpuCorBackward, gpuDist, gpuDistBackward, gpuMdsStress, gpuTtest, kendall_device,
                   pmcc_device, pmatch, set_gram_path)
 from ._lib import GpuToolsError, load, last_error
 from .builder import build
 
-__all__ = ["Dist", "chooseGpu", "distances_device", "get_gram_path", "getGpuId", "gpuCor",
+__all__ = ["BatchPlan", "Dist", "chooseGpu", "distances_device", "get_gram_path", "getGpuId", "gpuCor",
            "gpuCorBackward", "gpuDistBackward", "gpuMdsStress", "gpuDist", "gpuTtest", "kendall_device", "pmcc_device", "pmatch", "set_gram_path",
            "GpuToolsError", "load", "last_error", "build"]

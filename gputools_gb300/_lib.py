@@ -69,6 +69,31 @@ SIGNATURES = {
     "RgpuMdsStress": (None, [_vp, _pi, _pi, _vp, _vp, _vp]),
 }
 
+class CorProblem(ctypes.Structure):
+    """gt_cor_problem: one cor(x) of a batch (device pointers)."""
+    _fields_ = [("X", ctypes.c_void_p), ("p", ctypes.c_int64), ("n", ctypes.c_int64),
+                ("corr", ctypes.c_void_p), ("ts", ctypes.c_void_p), ("pairs", ctypes.c_void_p)]
+
+
+class KendallProblem(ctypes.Structure):
+    """gt_kendall_problem: one Kendall cor(x) of a batch (device pointers)."""
+    _fields_ = [("X", ctypes.c_void_p), ("p", ctypes.c_int64), ("n", ctypes.c_int64),
+                ("out", ctypes.c_void_p)]
+
+
+GT_BATCH_NO_GRAPH = 1
+GT_BATCH_AUTOTUNE = 2
+
+SIGNATURES.update({
+    "gt_pmcc_batch_plan_create": (_i, [ctypes.POINTER(CorProblem), _i64, _i,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "gt_kendall_batch_plan_create": (_i, [ctypes.POINTER(KendallProblem), _i64, _i,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "gt_batch_plan_launch": (_i, [_vp, _vp]),
+    "gt_batch_plan_describe": (_cp, [_vp]),
+    "gt_batch_plan_destroy": (None, [_vp]),
+})
+
 _lib = None
 
 

@@ -298,3 +298,70 @@ def gpuMdsStress(points, delta):
     if err:
         raise RuntimeError(err)
     return float(loss[0]), out.astype(np.float64)
+
+
+# ---------------------------------------------------------------------------
+# Batches (no counterpart in the reference).
+
+class BatchPlan:
+    """A batch of independent cor(x) problems (pearson or kendall) prepared
+    once and replayed from a CUDA graph.  Inputs are variable-major CUDA
+    float32 tensors (p, n); outputs are allocated here.  `launch()`
+    recomputes every output from the current contents of the inputs."""
+
+    def __init__(self, inputs, method: str = "pearson", autotune: bool = False,
+                 graph: bool = True):
+        import torch
+        self.method = method
+        self.inputs = list(inputs)
+        lib = load()
+        flags = (0 if graph else _lib.GT_BATCH_NO_GRAPH) | (_lib.GT_BATCH_AUTOTUNE if autotune else 0)
+        self.outputs = []
+        handle = ctypes.c_void_p()
+        if method == "pearson":
+            arr = (_lib.CorProblem * max(1, len(self.inputs)))()
+            for i, x in enumerate(self.inputs):
+                p, n = x.shape
+                o = {k: torch.empty((p, p), dtype=torch.float32, device=x.device)
+                     for k in ("corr", "ts", "pairs")}
+                self.outputs.append(o)
+                arr[i] = _lib.CorProblem(x.data_ptr(), p, n, o["corr"].data_ptr(),
+                                         o["ts"].data_ptr(), o["pairs"].data_ptr())
+            check(lib.gt_pmcc_batch_plan_create(arr, len(self.inputs), flags, ctypes.byref(handle)))
+        elif method == "kendall":
+            arr = (_lib.KendallProblem * max(1, len(self.inputs)))()
+            for i, x in enumerate(self.inputs):
+                p, n = x.shape
+                o = torch.empty((p, p), dtype=torch.float64, device=x.device)
+                self.outputs.append(o)
+                arr[i] = _lib.KendallProblem(x.data_ptr(), p, n, o.data_ptr())
+            check(lib.gt_kendall_batch_plan_create(arr, len(self.inputs), flags,
+                                                   ctypes.byref(handle)))
+        else:
+            raise ValueError("method must be 'pearson' or 'kendall'")
+        self._handle = handle
+
+    def describe(self) -> str:
+        d = load().gt_batch_plan_describe(self._handle)
+        return d.decode() if d else ""
+
+    def launch(self, stream=None):
+        check(load().gt_batch_plan_launch(self._handle, _stream_ptr(stream)))
+        return self.outputs
+
+    def close(self):
+        if self._handle:
+            load().gt_batch_plan_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

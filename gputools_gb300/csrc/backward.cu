@@ -155,17 +155,23 @@ constexpr int kDbRows = 128;   // rows i per CTA (one per thread)
 constexpr int kDbCols = 32;    // points j per shared tile
 
 // mode 0: W_ij = (G_ij + G_ji) / D_ij ; mode 1: MDS, W_ij = 2 (D_ij - delta_ij) / D_ij
+// CTA (ib, js): rows i of block ib against points j of split js.  Writes the
+// split's partial sums sum_j W_ij x_j (pacc) and sum_j W_ij (pw), and its
+// partial loss; a second kernel reduces the splits in a fixed order.
 template <int DMAX, int MODE>
 __global__ void __launch_bounds__(kDbRows)
 dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
-                     const float *__restrict__ aux, float *__restrict__ dX,
-                     double *__restrict__ loss) {
+                     const float *__restrict__ aux, int64_t jchunk, float *__restrict__ pacc,
+                     float *__restrict__ pw, double *__restrict__ ploss) {
   __shared__ float xj[kDbCols][DMAX + 1];
   __shared__ float cf[kDbRows][kDbCols + 1];  // G_ij + G_ji, or delta_ij
   __shared__ double sh[kDbRows / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i0 = int64_t(blockIdx.x) * kDbRows;
   const int64_t i = i0 + tid;
+  const int64_t js = blockIdx.y;
+  const int64_t jbeg = js * jchunk;
+  const int64_t jend = (jbeg + jchunk < n) ? jbeg + jchunk : n;
   float xi[DMAX], acc[DMAX];
 #pragma unroll
   for (int k = 0; k < DMAX; k++) {
@@ -174,39 +180,39 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
   }
   float wsum = 0.f;
   double lsum = 0.0;
-  for (int64_t j0 = 0; j0 < n; j0 += kDbCols) {
+  for (int64_t j0 = jbeg; j0 < jend; j0 += kDbCols) {
     __syncthreads();
     for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
       const int jj = e / DMAX, k = e - jj * DMAX;
       const int64_t j = j0 + jj;
-      xj[jj][k] = (j < n && k < dim) ? X[j * dim + k] : 0.f;
+      xj[jj][k] = (j < jend && k < dim) ? X[j * dim + k] : 0.f;
     }
     if (MODE == 0) {
       // rows i, columns j: lanes along j (row-contiguous)
       for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
         const int64_t gi = i0 + ii, gj = j0 + lane;
-        cf[ii][lane] = (gi < n && gj < n) ? aux[gi * n + gj] : 0.f;
+        cf[ii][lane] = (gi < n && gj < jend) ? aux[gi * n + gj] : 0.f;
       }
       __syncthreads();
       // add G_ji: rows j, lanes along i
       for (int jj = 0; jj < kDbCols; jj++) {
         const int64_t gj = j0 + jj;
-        if (gj < n && i < n) cf[tid][jj] += aux[gj * n + i];
+        if (gj < jend && i < n) cf[tid][jj] += aux[gj * n + i];
       }
     } else {
       // delta in R dist layout: (a > b) at n*b - b*(b+1)/2 + a - b - 1
       for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
         const int64_t gi = i0 + ii, gj = j0 + lane;
-        if (gi < n && gj < n && gj > gi) cf[ii][lane] = aux[n * gi - gi * (gi + 1) / 2 + gj - gi - 1];
+        if (gi < n && gj < jend && gj > gi) cf[ii][lane] = aux[n * gi - gi * (gi + 1) / 2 + gj - gi - 1];
       }
       for (int jj = 0; jj < kDbCols; jj++) {
         const int64_t gj = j0 + jj;
-        if (gj < n && i < n && i > gj) cf[tid][jj] = aux[n * gj - gj * (gj + 1) / 2 + i - gj - 1];
+        if (gj < jend && i < n && i > gj) cf[tid][jj] = aux[n * gj - gj * (gj + 1) / 2 + i - gj - 1];
       }
     }
     __syncthreads();
     if (i < n) {
-      const int jmax = (n - j0 < kDbCols) ? int(n - j0) : kDbCols;
+      const int jmax = (jend - j0 < kDbCols) ? int(jend - j0) : kDbCols;
       for (int jj = 0; jj < jmax; jj++) {
         const int64_t j = j0 + jj;
         float d2 = 0.f;
@@ -232,11 +238,13 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
     }
   }
   if (i < n) {
+    float *pa = pacc + (js * n + i) * dim;
 #pragma unroll
     for (int k = 0; k < DMAX; k++)
-      if (k < dim) dX[i * dim + k] = fmaf(xi[k], wsum, -acc[k]);
+      if (k < dim) pa[k] = acc[k];
+    pw[js * n + i] = wsum;
   }
-  if (MODE == 1 && loss) {
+  if (MODE == 1) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if (lane == 0) sh[warp] = lsum;
@@ -244,25 +252,73 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
     if (tid == 0) {
       double t = 0.0;
       for (int w = 0; w < kDbRows / 32; w++) t += sh[w];
-      atomicAdd(loss, t);
+      ploss[blockIdx.y * gridDim.x + blockIdx.x] = t;
     }
+  }
+}
+
+// dX_i = x_i * sum_s pw[s][i] - sum_s pacc[s][i]; splits added in order.
+__global__ void dist_backward_reduce_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
+                                            int64_t nsplit, const float *__restrict__ pacc,
+                                            const float *__restrict__ pw,
+                                            float *__restrict__ dX) {
+  const int64_t total = n * dim;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t i = e / dim;
+    float w = 0.f, a = 0.f;
+    for (int64_t s = 0; s < nsplit; s++) {
+      w += pw[s * n + i];
+      a += pacc[s * n * dim + e];
+    }
+    dX[e] = fmaf(X[e], w, -a);
+  }
+}
+
+__global__ void loss_reduce_kernel(const double *__restrict__ ploss, int64_t count,
+                                   double *__restrict__ loss) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int64_t i = 0; i < count; i++) t += ploss[i];
+    *loss = t;
   }
 }
 
 template <int MODE>
 int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *aux, float *dX,
                          double *loss, cudaStream_t s) {
-  const unsigned grid = unsigned(cdiv(n, kDbRows));
-  if (dim <= 16)
-    dist_backward_kernel<16, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
-  else if (dim <= 32)
-    dist_backward_kernel<32, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
-  else if (dim <= 64)
-    dist_backward_kernel<64, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, dX, loss);
-  else
+  if (dim > 64)
     return fail(GT_EUNSUPPORTED, "distance adjoint supports at most 64 dimensions (dim=%lld)",
                 (long long)dim);
-  count_launch();
+  const int64_t ib = cdiv(n, kDbRows);
+  int64_t nsplit = cdiv(int64_t(sm_count()) * 4, ib);
+  const int64_t max_split = cdiv(n, kDbCols);
+  if (nsplit > max_split) nsplit = max_split;
+  if (nsplit < 1) nsplit = 1;
+  if (nsplit > 65535) nsplit = 65535;
+  const int64_t jchunk = cdiv(cdiv(n, nsplit), kDbCols) * kDbCols;
+  nsplit = cdiv(n, jchunk);
+  void *pa = nullptr, *pw = nullptr, *pl = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH0, size_t(nsplit) * size_t(n) * size_t(dim) * 4, &pa));
+  GT_TRY(ws_get(WS_SCRATCH1, size_t(nsplit) * size_t(n) * 4, &pw));
+  GT_TRY(ws_get(WS_SCRATCH2, size_t(nsplit) * size_t(ib) * 8, &pl));
+  const dim3 grid(unsigned(ib), unsigned(nsplit), 1u);
+  float *fa = static_cast<float *>(pa), *fw = static_cast<float *>(pw);
+  double *dl = static_cast<double *>(pl);
+  if (dim <= 16)
+    dist_backward_kernel<16, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+  else if (dim <= 32)
+    dist_backward_kernel<32, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+  else
+    dist_backward_kernel<64, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+  int64_t g = cdiv(n * dim, 256);
+  if (g > int64_t(sm_count()) * 8) g = int64_t(sm_count()) * 8;
+  dist_backward_reduce_kernel<<<unsigned(g), 256, 0, s>>>(X, n, dim, nsplit, fa, fw, dX);
+  count_launch(2);
+  if (MODE == 1 && loss) {
+    loss_reduce_kernel<<<1, 32, 0, s>>>(dl, ib * nsplit, loss);
+    count_launch();
+  }
   GT_CUDA(cudaGetLastError());
   return GT_OK;
 }
@@ -347,7 +403,6 @@ extern "C" int gt_mds_stress_device(const float *d_X, int64_t n, int64_t dim,
   if (n == 0 || dim == 0) return GT_OK;
   if (!d_X || !d_delta || !d_dX) return gt::fail(GT_EINVAL, "null device pointer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (d_loss) GT_CUDA(cudaMemsetAsync(d_loss, 0, sizeof(double), s));
   gt::ProfScope prof("mds_stress", s);
   return gt::launch_dist_backward<1>(d_X, n, dim, d_delta, d_dX, d_loss, s);
 }

@@ -21,6 +21,7 @@
 #include "common.cuh"
 #include "allpairs_simt.cuh"
 #include "kernels.cuh"
+#include "stats.cuh"
 
 #include <cmath>
 #include <mutex>
@@ -29,90 +30,32 @@ namespace gt {
 
 namespace {
 
-constexpr int kStatThreads = 256;
+constexpr int kStatThreads = kColStatThreads;
 
-__device__ __forceinline__ double block_sum(double v, double *sh) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x < 32) {
-    t = (l < kStatThreads / 32) ? sh[l] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (l == 0) sh[0] = t;
-  }
-  __syncthreads();
-  return sh[0];
-}
-
-// One CTA per variable: FP64 mean (refined by the mean residual, the
-// corrected two-pass algorithm) and centred sum of squares.
-// use 0: every value counts and any NaN flags the variable;
-// use 1: NaN values are skipped.
 __global__ void __launch_bounds__(kStatThreads)
 colstats_kernel(const float *__restrict__ X, int64_t n, int use, ColStats *__restrict__ out) {
   __shared__ double sh[32];
-  const float *x = X + int64_t(blockIdx.x) * n;
-  double s = 0.0, cnt = 0.0, nan = 0.0;
-  for (int64_t k = threadIdx.x; k < n; k += kStatThreads) {
-    const float v = x[k];
-    if (v != v) { nan += 1.0; continue; }
-    s += double(v);
-    cnt += 1.0;
-  }
-  s = block_sum(s, sh);
-  cnt = block_sum(cnt, sh);
-  nan = block_sum(nan, sh);
-  double mean = cnt > 0.0 ? s / cnt : 0.0;
-  double c = 0.0, ss = 0.0;
-  for (int64_t k = threadIdx.x; k < n; k += kStatThreads) {
-    const float v = x[k];
-    if (v != v) continue;
-    const double d = double(v) - mean;
-    c += d;
-    ss = fma(d, d, ss);
-  }
-  c = block_sum(c, sh);
-  ss = block_sum(ss, sh);
-  if (threadIdx.x == 0) {
-    ColStats st;
-    if (cnt > 0.0) {
-      mean += c / cnt;
-      ss -= c * c / cnt;
-    }
-    st.mean = mean;
-    st.flags = 0;
-    if (use == 0 && nan > 0.0) st.flags |= 1;
-    if (!(ss > 0.0) || cnt < 2.0) st.flags |= 2;
-    st.inv_norm = (st.flags & 2) ? 0.0 : 1.0 / sqrt(ss);
-    out[blockIdx.x] = st;
-  }
+  const ColStats st = colstats_block(X + int64_t(blockIdx.x) * n, n, use, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = st;
 }
 
 // z[v][k] = (x - mean) * inv_norm in float, rows of length ldz (>= n, pad
-// filled with `padv`).  Everything mode: a variable containing NaN or with
-// zero variance becomes all-NaN, so every r involving it is NaN.
+// filled with `padv`), one CTA per variable.  Everything mode: a variable
+// containing NaN or with zero variance becomes all-NaN, so every r involving
+// it is NaN.
 __global__ void normalize_f32_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
                                      int64_t ldz, const ColStats *__restrict__ st, int use,
                                      float padv, float *__restrict__ Z) {
-  const int64_t total = nvar * ldz;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t v = i / ldz, k = i - v * ldz;
-    float z;
-    if (k >= n) {
-      z = padv;
-    } else {
-      const ColStats s = st[v];
-      const float x = X[v * n + k];
-      if (use == 0 && s.flags) z = __int_as_float(0x7fc00000);
-      else z = float((double(x) - s.mean) * s.inv_norm);
-    }
-    Z[i] = z;
+  const int64_t v = blockIdx.x;
+  const ColStats s = st[v];
+  const float *x = X + v * n;
+  float *z = Z + v * ldz;
+  for (int64_t k = threadIdx.x; k < ldz; k += blockDim.x) {
+    float val;
+    if (k >= n) val = padv;
+    else if (use == 0 && s.flags) val = __int_as_float(0x7fc00000);
+    else val = float((double(x[k]) - s.mean) * s.inv_norm);
+    z[k] = val;
   }
 }
 
@@ -223,8 +166,7 @@ int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz,
   colstats_kernel<<<unsigned(nvar), kStatThreads, 0, s>>>(dX, n, use, *st);
   count_launch();
   const float padv = use == 0 ? 0.f : __builtin_nanf("");
-  normalize_f32_kernel<<<grid_for(nvar * ldz, 256), 256, 0, s>>>(dX, nvar, n, ldz, *st, use,
-                                                                   padv, *Z);
+  normalize_f32_kernel<<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, ldz, *st, use, padv, *Z);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
@@ -458,12 +400,11 @@ extern "C" int gt_pmcc_device_noalloc(int use, const float *d_A, int64_t nA, con
   // entries of each row, every statistic), so nothing has to be cleared.
   const float padv = use == GT_EVERYTHING ? 0.f : __builtin_nanf("");
   GT_TRY(launch_colstats(d_A, nA, n, use, sA, s));
-  normalize_f32_kernel<<<grid_for(nA * ldz, 256), 256, 0, s>>>(d_A, nA, n, ldz, sA, use, padv, zA);
+  normalize_f32_kernel<<<unsigned(nA), 256, 0, s>>>(d_A, nA, n, ldz, sA, use, padv, zA);
   count_launch();
   if (!sym) {
     GT_TRY(launch_colstats(d_B, nB, n, use, sB, s));
-    normalize_f32_kernel<<<grid_for(nB * ldz, 256), 256, 0, s>>>(d_B, nB, n, ldz, sB, use, padv,
-                                                                  zB);
+    normalize_f32_kernel<<<unsigned(nB), 256, 0, s>>>(d_B, nB, n, ldz, sB, use, padv, zB);
     count_launch();
   }
   GT_CUDA(cudaGetLastError());

@@ -43,13 +43,19 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_ptx.cuh"
+#include "stats.cuh"
 
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
+#include <functional>
 #include <mutex>
+#include <queue>
+#include <vector>
 
 namespace gt {
 
@@ -299,10 +305,83 @@ __device__ __forceinline__ void product_parts(int p, int &pa, int &pb) {
   }
 }
 
-template <int NSPLIT, int BK, bool CHUNKED, class Fin>
+// ----------------------------------------------------------------- work sources
+// A work source tells every role of the kernel, for the cursor-th tile of
+// this CTA, which tensor maps to load from, the tile's row / column blocks,
+// its number of k-blocks, and the finish to apply.
+struct TileRef {
+  const CUtensorMap *ma, *mb;
+  int64_t ti, tj, nk, prob;
+};
+
+// One problem: maps and finish as kernel parameters, tiles dealt round-robin.
+template <class Fin>
+struct SingleWork {
+  CUtensorMap ma, mb;
+  TileSpace ts;
+  int64_t nk;
+  Fin fin;
+  __device__ bool tile(int64_t cursor, TileRef &ref) const {
+    const int64_t t = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
+    if (t >= ts.ntiles) return false;
+    tile_coords(ts, t, ref.ti, ref.tj);
+    ref.ma = &ma;
+    ref.mb = &mb;
+    ref.nk = nk;
+    ref.prob = 0;
+    return true;
+  }
+  __device__ const Fin &finish(const TileRef &) const { return fin; }
+  __device__ void prefetch() const {
+    tc::prefetch_tensormap(&ma);
+    tc::prefetch_tensormap(&mb);
+  }
+};
+
+__device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ prefix, int64_t n,
+                                                int64_t x) {
+  int64_t lo = 0, hi = n;  // prefix has n + 1 entries; largest i with prefix[i] <= x
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (prefix[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// A batch of cor(x) problems: per-problem maps and finishes in device
+// memory; each CTA walks its own host-balanced list of global tile ids.
+struct alignas(64) PearsonBatchProblem {
+  CUtensorMap map;
+  TileSpace ts;
+  int64_t nk;
+  PearsonFinish fin;
+};
+
+struct PearsonBatchWork {
+  const PearsonBatchProblem *probs;
+  const int64_t *tile_prefix;
+  int64_t nprob;
+  const int64_t *cta_tiles, *cta_off;
+  __device__ bool tile(int64_t cursor, TileRef &ref) const {
+    const int64_t idx = cta_off[blockIdx.x] + cursor;
+    if (idx >= cta_off[blockIdx.x + 1]) return false;
+    const int64_t t = cta_tiles[idx];
+    const int64_t pi = find_segment(tile_prefix, nprob, t);
+    const PearsonBatchProblem &pr = probs[pi];
+    tile_coords(pr.ts, t - tile_prefix[pi], ref.ti, ref.tj);
+    ref.ma = ref.mb = &pr.map;
+    ref.nk = pr.nk;
+    ref.prob = pi;
+    return true;
+  }
+  __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
+  __device__ void prefetch() const {}
+};
+
+template <int NSPLIT, int BK, bool CHUNKED, class Work>
 __global__ void __launch_bounds__(kTcThreads, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-               TileSpace tiles, int64_t nk, int64_t ckb, Fin fin, int *err) {
+gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
   using C = TcCfg<NSPLIT, BK>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -330,26 +409,20 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     *abort_flag = 0;
     tc::fence_barrier_init();
   }
-  if (warp == 0 && lane == 0) {
-    tc::prefetch_tensormap(&mapA);
-    tc::prefetch_tensormap(&mapB);
-  }
+  if (warp == 0 && lane == 0) work.prefetch();
   if (warp == 1) tc::tmem_alloc(tmem_slot, 2 * kBN);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  if (!CHUNKED) ckb = nk;
-  const int64_t nchunks = (nk + ckb - 1) / ckb;
 
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------ TMA producer
       int64_t it = 0;
-      for (int64_t t = blockIdx.x; t < tiles.ntiles && !*abort_flag; t += gridDim.x) {
-        int64_t ti, tj;
-        tile_coords(tiles, t, ti, tj);
-        for (int64_t kb = 0; kb < nk; kb++, it++) {
+      TileRef ref;
+      for (int64_t cur = 0; !*abort_flag && work.tile(cur, ref); cur++) {
+        for (int64_t kb = 0; kb < ref.nk; kb++, it++) {
           const int s = int(it % C::STAGES);
           const uint32_t use = uint32_t(it / C::STAGES);
           if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
@@ -360,12 +433,12 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
           tc::mbar_arrive_expect_tx(&full[s], C::STAGE);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
-            tc::tma_load_3d(st + p * C::A_TILE, &mapA, &full[s], int32_t(kb * BK),
-                            int32_t(ti * kBM), p);
+            tc::tma_load_3d(st + p * C::A_TILE, ref.ma, &full[s], int32_t(kb * BK),
+                            int32_t(ref.ti * kBM), p);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
-            tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, &mapB, &full[s],
-                            int32_t(kb * BK), int32_t(tj * kBN), p);
+            tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, ref.mb, &full[s],
+                            int32_t(kb * BK), int32_t(ref.tj * kBN), p);
         }
       }
       // drain: no bulk copy may still be writing shared memory at exit
@@ -383,8 +456,11 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
       int64_t it = 0, cc = 0;
       bool ok = true;
-      for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
-        for (int64_t ch = 0; ch < nchunks && ok; ch++, cc++) {
+      TileRef ref;
+      for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
+        const int64_t ck = CHUNKED ? ckb : ref.nk;
+        const int64_t nch = (ref.nk + ck - 1) / ck;
+        for (int64_t ch = 0; ch < nch && ok; ch++, cc++) {
           const int buf = int(cc & 1);
           const uint32_t ause = uint32_t(cc >> 1);
           if (!tc::mbar_wait(&acce[buf], (ause & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
@@ -393,7 +469,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
           }
           tc::tc_fence_after();
           const uint32_t d = tmem_base + uint32_t(buf * kBN);
-          const int64_t kb0 = ch * ckb, kb1 = (kb0 + ckb < nk) ? kb0 + ckb : nk;
+          const int64_t kb0 = ch * ck, kb1 = (kb0 + ck < ref.nk) ? kb0 + ck : ref.nk;
           for (int64_t kb = kb0; kb < kb1; kb++, it++) {
             const int s = int(it % C::STAGES);
             const uint32_t use = uint32_t(it / C::STAGES);
@@ -433,16 +509,17 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     float *wsm = epi_smem + (warp - 2) * kEpiTileFloats;
     int64_t cc = 0;
     bool ok = true;
-    for (int64_t t = blockIdx.x; t < tiles.ntiles && ok; t += gridDim.x) {
-      int64_t ti, tj;
-      tile_coords(tiles, t, ti, tj);
-      const int64_t r = ti * kBM + q * 32 + lane;
-      const int64_t col = tj * kBN + half * 128;
+    TileRef ref;
+    for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
+      const auto fin = work.finish(ref);
+      const int64_t r = ref.ti * kBM + q * 32 + lane;
+      const int64_t col = ref.tj * kBN + half * 128;
       if (CHUNKED) {
+        const int64_t nch = (ref.nk + ckb - 1) / ckb;
         float acc[128];
 #pragma unroll
         for (int j = 0; j < 128; j++) acc[j] = 0.f;
-        for (int64_t ch = 0; ch < nchunks; ch++, cc++) {
+        for (int64_t ch = 0; ch < nch; ch++, cc++) {
           const int buf = int(cc & 1);
           const uint32_t ause = uint32_t(cc >> 1);
           const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
@@ -507,29 +584,27 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 // ----------------------------------------------------------------- operands
 // Pearson operand planes: z = (x - mean) * inv_norm in FP64 (rounded to
 // float), NaN rows for variables that are NaN-flagged or constant; k >= n is
-// zero.
+// zero.  One CTA per variable (no per-element index division).
 template <int NSPLIT>
-__global__ void pearson_split_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
-                                     int64_t kpad, const ColStats *__restrict__ st,
-                                     __nv_bfloat16 *__restrict__ Z) {
-  const int64_t total = nvar * kpad;
-  const int64_t plane = total;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t v = i / kpad, k = i - v * kpad;
+__global__ void __launch_bounds__(256)
+pearson_split_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int64_t kpad,
+                     const ColStats *__restrict__ st, __nv_bfloat16 *__restrict__ Z) {
+  const int64_t v = blockIdx.x;
+  const int64_t plane = nvar * kpad;
+  const ColStats s = st[v];
+  const float *x = X + v * n;
+  __nv_bfloat16 *z = Z + v * kpad;
+  for (int64_t k = threadIdx.x; k < kpad; k += blockDim.x) {
     __nv_bfloat16 p[3];
     if (k >= n) {
       p[0] = p[1] = p[2] = __float2bfloat16(0.f);
+    } else if (s.flags) {
+      p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
     } else {
-      const ColStats s = st[v];
-      if (s.flags) {
-        p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
-      } else {
-        tc::split_bf16<NSPLIT>(float((double(X[v * n + k]) - s.mean) * s.inv_norm), p);
-      }
+      tc::split_bf16<NSPLIT>(float((double(x[k]) - s.mean) * s.inv_norm), p);
     }
 #pragma unroll
-    for (int q = 0; q < NSPLIT; q++) Z[q * plane + i] = p[q];
+    for (int q = 0; q < NSPLIT; q++) z[q * plane + k] = p[q];
   }
 }
 
@@ -573,6 +648,54 @@ __global__ void euclid_split_kernel(const float *__restrict__ P, int64_t n, int6
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) norm2[v] = float(acc);
+  }
+}
+
+// Batched Pearson prologue: the variables of every problem, one CTA each.
+struct PearsonBatchInput {
+  const float *X;
+  int64_t p, n, kpad;
+  int64_t plane_off;  // element offset of this problem's planes (NSPLIT x p x kpad)
+  int64_t var_off;    // offset of its variables in the statistics array
+};
+
+__global__ void __launch_bounds__(kColStatThreads)
+pearson_batch_stats_kernel(const PearsonBatchInput *__restrict__ in,
+                           const int64_t *__restrict__ var_prefix, int64_t nprob,
+                           ColStats *__restrict__ st) {
+  __shared__ double sh[32];
+  const int64_t gv = blockIdx.x;
+  const int64_t pi = find_segment(var_prefix, nprob, gv);
+  const PearsonBatchInput b = in[pi];
+  const int64_t v = gv - var_prefix[pi];
+  const ColStats c = colstats_block(b.X + v * b.n, b.n, GT_EVERYTHING, sh);
+  if (threadIdx.x == 0) st[gv] = c;
+}
+
+template <int NSPLIT>
+__global__ void __launch_bounds__(256)
+pearson_batch_split_kernel(const PearsonBatchInput *__restrict__ in,
+                           const int64_t *__restrict__ var_prefix, int64_t nprob,
+                           const ColStats *__restrict__ st, __nv_bfloat16 *__restrict__ planes) {
+  const int64_t gv = blockIdx.x;
+  const int64_t pi = find_segment(var_prefix, nprob, gv);
+  const PearsonBatchInput b = in[pi];
+  const int64_t v = gv - var_prefix[pi];
+  const ColStats s = st[gv];
+  const int64_t plane = b.p * b.kpad;
+  const float *x = b.X + v * b.n;
+  __nv_bfloat16 *z = planes + b.plane_off + v * b.kpad;
+  for (int64_t k = threadIdx.x; k < b.kpad; k += blockDim.x) {
+    __nv_bfloat16 p[3];
+    if (k >= b.n) {
+      p[0] = p[1] = p[2] = __float2bfloat16(0.f);
+    } else if (s.flags) {
+      p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
+    } else {
+      tc::split_bf16<NSPLIT>(float((double(x[k]) - s.mean) * s.inv_norm), p);
+    }
+#pragma unroll
+    for (int q = 0; q < NSPLIT; q++) z[q * plane + k] = p[q];
   }
 }
 
@@ -622,21 +745,24 @@ int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t 
                 bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
                 cudaStream_t s) {
   using C = TcCfg<NSPLIT, BK>;
+  using W = SingleWork<Fin>;
   if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
   if (ckb < 1) ckb = 1;
-  CUtensorMap mA, mB;
-  GT_TRY(make_plane_map(&mA, zA, nA, kpad, NSPLIT, kBM, BK));
-  GT_TRY(make_plane_map(&mB, zB, nB, kpad, NSPLIT, kBN, BK));
-  const TileSpace ts = make_tiles(nA, nB, symmetric);
-  if (ts.ntiles == 0) return GT_OK;
+  W w;
+  GT_TRY(make_plane_map(&w.ma, zA, nA, kpad, NSPLIT, kBM, BK));
+  GT_TRY(make_plane_map(&w.mb, zB, nB, kpad, NSPLIT, kBN, BK));
+  w.ts = make_tiles(nA, nB, symmetric);
+  w.nk = kpad / BK;
+  w.fin = fin;
+  if (w.ts.ntiles == 0) return GT_OK;
   int *err = nullptr;
   GT_TRY(err_word(&err));
   GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  auto kern = gram_tc_kernel<NSPLIT, BK, CHUNKED, Fin>;
+  auto kern = gram_tc_kernel<NSPLIT, BK, CHUNKED, W>;
   GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-  const int64_t grid = ts.ntiles < sm_count() ? ts.ntiles : sm_count();
+  const int64_t grid = w.ts.ntiles < sm_count() ? w.ts.ntiles : sm_count();
   ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), kTcThreads, C::SMEM, s>>>(mA, mB, ts, kpad / BK, ckb, fin, err);
+  kern<<<unsigned(grid), kTcThreads, C::SMEM, s>>>(w, ckb, err);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
@@ -698,15 +824,12 @@ int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, in
   ColStats *st = static_cast<ColStats *>(pst);
   ProfScope prof("pearson_prologue", s);
   GT_TRY(launch_colstats(dX, nvar, n, GT_EVERYTHING, st, s));
-  const int64_t total = nvar * *kpad;
-  int64_t g = cdiv(total, 256);
-  if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
-  if (g < 1) g = 1;
   auto *z = static_cast<__nv_bfloat16 *>(pz);
+  if (nvar > 2147483647LL) return fail(GT_EINVAL, "too many variables");
   if (nsplit == 3)
-    pearson_split_kernel<3><<<unsigned(g), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
+    pearson_split_kernel<3><<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
   else
-    pearson_split_kernel<2><<<unsigned(g), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
+    pearson_split_kernel<2><<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
   count_launch();
   GT_CUDA(cudaGetLastError());
   *Z = pz;
@@ -760,6 +883,152 @@ int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
   // Entries with d^2 below an eighth of |a|^2 + |b|^2 are recomputed exactly.
   EuclidFinish fin{norm2, d_pts, d_out, n, dim, layout, 0.125f};
   return launch_gram<NS, 32, false>(z, n, z, n, kpad, true, 0, fin, "euclid_gram", st);
+}
+
+// Batched cor(x): builds device descriptors (through `alloc`, which the plan
+// owns), balances the tiles over one CTA per SM, and returns the runner that
+// launches prologue + Gram for the whole batch.
+int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit, int bk,
+                          int64_t chunk_elems, const std::function<int(size_t, void **)> &alloc,
+                          std::function<int(cudaStream_t)> *run, int64_t *ntiles_out,
+                          int64_t *nctas_out) {
+  std::vector<PearsonBatchInput> inputs;
+  std::vector<PearsonBatchProblem> descs;
+  std::vector<int64_t> var_prefix{0}, tile_prefix{0}, cost;
+  int64_t plane_elems = 0, vars = 0;
+  // first pass: shapes and offsets
+  for (int64_t i = 0; i < count; i++) {
+    const gt_cor_problem &q = probs[i];
+    if (q.p < 0 || q.n < 0) return fail(GT_EINVAL, "problem %lld: negative size", (long long)i);
+    if (q.p == 0) continue;
+    if (!q.X) return fail(GT_EINVAL, "problem %lld: null input", (long long)i);
+    if (q.n == 0) return fail(GT_EINVAL, "problem %lld: no observations", (long long)i);
+    PearsonBatchInput b;
+    b.X = q.X;
+    b.p = q.p;
+    b.n = q.n;
+    b.kpad = cdiv(q.n, kKPad) * kKPad;
+    b.plane_off = plane_elems;
+    b.var_off = vars;
+    inputs.push_back(b);
+    plane_elems += int64_t(nsplit) * b.p * b.kpad;
+    vars += b.p;
+    var_prefix.push_back(vars);
+  }
+  const int64_t nprob = int64_t(inputs.size());
+  void *d_planes = nullptr, *d_st = nullptr, *d_in = nullptr, *d_vp = nullptr;
+  GT_TRY(alloc(size_t(plane_elems) * 2, &d_planes));
+  GT_TRY(alloc(size_t(vars) * sizeof(ColStats), &d_st));
+  auto *planes = static_cast<__nv_bfloat16 *>(d_planes);
+  int64_t ckb = chunk_elems / bk;
+  if (ckb < 1) ckb = 1;
+  // second pass: tensor maps, tiles, finishes
+  int64_t pidx = 0;
+  for (int64_t i = 0; i < count; i++) {
+    const gt_cor_problem &q = probs[i];
+    if (q.p == 0) continue;
+    const PearsonBatchInput &b = inputs[pidx++];
+    PearsonBatchProblem d;
+    std::memset(&d, 0, sizeof(d));
+    GT_TRY(make_plane_map(&d.map, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk));
+    d.ts = make_tiles(b.p, b.p, true);
+    d.nk = b.kpad / bk;
+    d.fin = PearsonFinish{q.corr, q.ts, q.pairs, b.p, b.p, b.p, float(b.n),
+                          std::sqrt(float(b.n) - 2.f), 1};
+    descs.push_back(d);
+    tile_prefix.push_back(tile_prefix.back() + d.ts.ntiles);
+    const int64_t nch = (d.nk + ckb - 1) / ckb;
+    for (int64_t t = 0; t < d.ts.ntiles; t++) cost.push_back(d.nk + 2 * nch + 4);
+  }
+  const int64_t ntiles = tile_prefix.back();
+  int64_t ncta = sm_count();
+  if (ncta > ntiles) ncta = ntiles;
+  std::vector<int64_t> cta_tiles, cta_off;
+  if (ntiles > 0) {
+    // longest-processing-time first over the CTAs
+    std::vector<int64_t> order(ntiles);
+    for (int64_t t = 0; t < ntiles; t++) order[t] = t;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t c) { return cost[a] > cost[c]; });
+    std::vector<int64_t> load(ncta, 0);
+    std::vector<std::vector<int64_t>> lists(ncta);
+    using Item = std::pair<int64_t, int64_t>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (int64_t c = 0; c < ncta; c++) heap.push({0, c});
+    for (int64_t t : order) {
+      Item it = heap.top();
+      heap.pop();
+      lists[it.second].push_back(t);
+      it.first += cost[t];
+      heap.push(it);
+    }
+    cta_off.assign(ncta + 1, 0);
+    for (int64_t c = 0; c < ncta; c++) {
+      cta_off[c] = int64_t(cta_tiles.size());
+      cta_tiles.insert(cta_tiles.end(), lists[c].begin(), lists[c].end());
+    }
+    cta_off[ncta] = int64_t(cta_tiles.size());
+  }
+  auto upload = [&](const void *src, size_t bytes, void **dst) -> int {
+    GT_TRY(alloc(bytes, dst));
+    if (bytes) GT_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    return GT_OK;
+  };
+  void *d_desc = nullptr, *d_tp = nullptr, *d_ct = nullptr, *d_co = nullptr, *d_err = nullptr;
+  GT_TRY(upload(inputs.data(), inputs.size() * sizeof(PearsonBatchInput), &d_in));
+  GT_TRY(upload(var_prefix.data(), var_prefix.size() * 8, &d_vp));
+  GT_TRY(upload(descs.data(), descs.size() * sizeof(PearsonBatchProblem), &d_desc));
+  GT_TRY(upload(tile_prefix.data(), tile_prefix.size() * 8, &d_tp));
+  GT_TRY(upload(cta_tiles.data(), cta_tiles.size() * 8, &d_ct));
+  GT_TRY(upload(cta_off.data(), cta_off.size() * 8, &d_co));
+  GT_TRY(alloc(256, &d_err));
+  PearsonBatchWork w;
+  w.probs = static_cast<const PearsonBatchProblem *>(d_desc);
+  w.tile_prefix = static_cast<const int64_t *>(d_tp);
+  w.nprob = nprob;
+  w.cta_tiles = static_cast<const int64_t *>(d_ct);
+  w.cta_off = static_cast<const int64_t *>(d_co);
+  auto *in = static_cast<const PearsonBatchInput *>(d_in);
+  auto *vp = static_cast<const int64_t *>(d_vp);
+  auto *st = static_cast<ColStats *>(d_st);
+  auto *err = static_cast<int *>(d_err);
+  const int64_t total_vars = vars;
+  const int ns = nsplit;
+  const int BKc = bk;
+  *ntiles_out = ntiles;
+  *nctas_out = ncta;
+  *run = [=](cudaStream_t s) -> int {
+    GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    if (total_vars == 0) return GT_OK;
+    if (total_vars > 2147483647LL) return fail(GT_EINVAL, "too many variables in the batch");
+    pearson_batch_stats_kernel<<<unsigned(total_vars), kColStatThreads, 0, s>>>(in, vp, nprob, st);
+    if (ns == 3)
+      pearson_batch_split_kernel<3><<<unsigned(total_vars), 256, 0, s>>>(in, vp, nprob, st, planes);
+    else
+      pearson_batch_split_kernel<2><<<unsigned(total_vars), 256, 0, s>>>(in, vp, nprob, st, planes);
+    count_launch(2);
+    if (ncta == 0) return GT_OK;
+    if (ns == 3) {
+      using C = TcCfg<3, 32>;
+      auto k = gram_tc_kernel<3, 32, true, PearsonBatchWork>;
+      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+    } else if (BKc == 32) {
+      using C = TcCfg<2, 32>;
+      auto k = gram_tc_kernel<2, 32, true, PearsonBatchWork>;
+      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+    } else {
+      using C = TcCfg<2, 64>;
+      auto k = gram_tc_kernel<2, 64, true, PearsonBatchWork>;
+      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+    }
+    count_launch();
+    GT_CUDA(cudaGetLastError());
+    return GT_OK;
+  };
+  return GT_OK;
 }
 
 }  // namespace gt

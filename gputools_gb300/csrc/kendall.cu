@@ -20,6 +20,7 @@
 // order, clamped to [-1, 1]; NaN when either variable is constant; exactly 1
 // on the diagonal of cor(x).
 #include "common.cuh"
+#include "kernels.cuh"
 
 #include <cmath>
 
@@ -64,29 +65,20 @@ __global__ void kendall_masks_kernel(const float *__restrict__ X, int64_t nvar, 
   }
 }
 
-// S[r*ld + c] += sum over words of popc(m) - 2 popc(m & (Gr ^ Gc)).
-// Rows r index MR (the Y set), columns c index MC (the X set).
-__global__ void __launch_bounds__(kKT)
-kendall_count_kernel(const uint2 *__restrict__ MR, int64_t nr, const uint2 *__restrict__ MC,
-                     int64_t nc, int64_t K, int64_t kchunk, int symmetric,
-                     unsigned long long *__restrict__ S, int64_t ld) {
-  constexpr int TM = 4, TN = 4, BM = 64, BN = 64;
-  const int ti = blockIdx.y, tj = blockIdx.x;
-  if (symmetric && ti > tj) return;
-  const int64_t row0 = int64_t(ti) * BM, col0 = int64_t(tj) * BN;
-  const int64_t kbeg = int64_t(blockIdx.z) * kchunk;
-  const int64_t kend = min(K, kbeg + kchunk);
-  if (kbeg >= kend) return;
-
-  __shared__ __align__(16) uint2 sR[BM * kKLd];
-  __shared__ __align__(16) uint2 sC[BN * kKLd];
+// Counts of one 64 x 64 tile of variable pairs over words [kbeg, kend):
+// both[i][j] = popc(m), disc[i][j] = popc(m & (Gr ^ Gc)) with m = Ur & Uc,
+// for rows row0 + ty + 16 i of MR and columns col0 + tx + 16 j of MC.
+__device__ __forceinline__ void tile_counts(const uint2 *__restrict__ MR, int64_t nr,
+                                            const uint2 *__restrict__ MC, int64_t nc, int64_t K,
+                                            int64_t row0, int64_t col0, int64_t kbeg,
+                                            int64_t kend, uint2 *sR, uint2 *sC,
+                                            unsigned (&both)[4][4], unsigned (&disc)[4][4]) {
+  constexpr int TM = 4, TN = 4;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  unsigned both[TM][TN], disc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; i++)
 #pragma unroll
     for (int j = 0; j < TN; j++) both[i][j] = disc[i][j] = 0u;
-
   for (int64_t k0 = kbeg; k0 < kend; k0 += kKBK) {
     // 64 rows x 16 words = 512 uint4 (two words each) per operand.
 #pragma unroll
@@ -127,13 +119,42 @@ kendall_count_kernel(const uint2 *__restrict__ MR, int64_t nr, const uint2 *__re
     }
     __syncthreads();
   }
+}
+
+// tau-b = S / (sqrt(Tx) * sqrt(Ty)) in IEEE double, R's evaluation order,
+// clamped to [-1, 1]; NaN when either variable is constant.
+__device__ __forceinline__ double taub(long long S, unsigned long long tx, unsigned long long ty) {
+  if (tx == 0 || ty == 0) return __longlong_as_double(0x7ff8000000000000LL);
+  double r = __ddiv_rn(double(S), __dmul_rn(__dsqrt_rn(double(tx)), __dsqrt_rn(double(ty))));
+  if (r > 1.0) r = 1.0;
+  if (r < -1.0) r = -1.0;
+  return r;
+}
+
+// S[r*ld + c] += sum over words of popc(m) - 2 popc(m & (Gr ^ Gc)).
+// Rows r index MR (the Y set), columns c index MC (the X set).
+__global__ void __launch_bounds__(kKT)
+kendall_count_kernel(const uint2 *__restrict__ MR, int64_t nr, const uint2 *__restrict__ MC,
+                     int64_t nc, int64_t K, int64_t kchunk, int symmetric,
+                     unsigned long long *__restrict__ S, int64_t ld) {
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (symmetric && ti > tj) return;
+  const int64_t row0 = int64_t(ti) * 64, col0 = int64_t(tj) * 64;
+  const int64_t kbeg = int64_t(blockIdx.z) * kchunk;
+  const int64_t kend = min(K, kbeg + kchunk);
+  if (kbeg >= kend) return;
+  __shared__ __align__(16) uint2 sR[64 * kKLd];
+  __shared__ __align__(16) uint2 sC[64 * kKLd];
+  unsigned both[4][4], disc[4][4];
+  tile_counts(MR, nr, MC, nc, K, row0, col0, kbeg, kend, sR, sC, both, disc);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const bool mirror = symmetric && ti != tj;
 #pragma unroll
-  for (int i = 0; i < TM; i++) {
+  for (int i = 0; i < 4; i++) {
     const int64_t r = row0 + ty + 16 * i;
     if (r >= nr) continue;
 #pragma unroll
-    for (int j = 0; j < TN; j++) {
+    for (int j = 0; j < 4; j++) {
       const int64_t c = col0 + tx + 16 * j;
       if (c >= nc) continue;
       const long long sv = (long long)both[i][j] - 2LL * (long long)disc[i][j];
@@ -152,20 +173,7 @@ __global__ void kendall_finish_kernel(const unsigned long long *__restrict__ S,
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
        i += int64_t(gridDim.x) * blockDim.x) {
     const int64_t y = i / nx, x = i - y * nx;
-    double r;
-    if (same && x == y) {
-      r = 1.0;
-    } else {
-      const unsigned long long tx = TX[x], ty = TY[y];
-      if (tx == 0 || ty == 0) {
-        r = __longlong_as_double(0x7ff8000000000000LL);
-      } else {
-        const double s = double((long long)S[i]);
-        r = __ddiv_rn(s, __dmul_rn(__dsqrt_rn(double(tx)), __dsqrt_rn(double(ty))));
-        if (r > 1.0) r = 1.0;
-        if (r < -1.0) r = -1.0;
-      }
-    }
+    const double r = (same && x == y) ? 1.0 : taub((long long)S[i], TX[x], TY[y]);
     out[i] = r;
   }
 }
@@ -233,6 +241,128 @@ int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64
   }
   kendall_finish_kernel<<<grid_cap(nx * ny, 256), 256, 0, s>>>(S, TX, TY, nx, ny, same, d_out);
   count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------- batches
+// Many independent Kendall problems in one pass: one CTA per variable builds
+// its pair masks and untied count; one count launch walks per-CTA lists of
+// 64 x 64 tiles (balanced on the host) across all problems and writes tau-b
+// directly (each tile covers its problem's full pair dimension).
+
+namespace {
+
+__device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ prefix, int64_t n,
+                                                int64_t x) {
+  int64_t lo = 0, hi = n;  // prefix has n + 1 entries; largest i with prefix[i] <= x
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (prefix[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+constexpr int kKbMaskThreads = 128;
+
+__global__ void __launch_bounds__(kKbMaskThreads)
+kendall_batch_masks_kernel(const KendallBatchProblem *__restrict__ P,
+                           const int64_t *__restrict__ var_prefix, int64_t nprob,
+                           uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
+  __shared__ unsigned long long part[kKbMaskThreads / 32];
+  const int64_t gv = blockIdx.x;
+  const int64_t pi = find_segment(var_prefix, nprob, gv);
+  const KendallBatchProblem pr = P[pi];
+  const int64_t v = gv - var_prefix[pi];
+  const float *x = pr.X + v * pr.n;
+  uint2 *mv = M + pr.mask_off + v * pr.K;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  for (int64_t t = warp; t < pr.K; t += kKbMaskThreads / 32) {
+    const int64_t dr = t / pr.Wn, w = t - dr * pr.Wn;
+    const int64_t d = dr + 1;
+    const int64_t i = 32 * w + lane;
+    const bool valid = i < pr.n && (2 * d < pr.n || i < pr.n / 2);
+    bool untied = false, greater = false;
+    if (valid) {
+      int64_t j = i + d;
+      if (j >= pr.n) j -= pr.n;
+      untied = x[j] != x[i];
+      greater = x[j] > x[i];
+    }
+    const unsigned u = __ballot_sync(0xffffffffu, untied);
+    const unsigned g = __ballot_sync(0xffffffffu, greater);
+    if (lane == 0) {
+      mv[t] = make_uint2(u, g);
+      cnt += __popc(u);
+    }
+  }
+  if (lane == 0) part[warp] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < kKbMaskThreads / 32; w++) tot += part[w];
+    T[pr.var_off + v] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(kKT)
+kendall_batch_count_kernel(const KendallBatchProblem *__restrict__ P,
+                           const int64_t *__restrict__ tile_prefix, int64_t nprob,
+                           const int64_t *__restrict__ cta_tiles,
+                           const int64_t *__restrict__ cta_off, const uint2 *__restrict__ M,
+                           const unsigned long long *__restrict__ T) {
+  __shared__ __align__(16) uint2 sR[64 * kKLd];
+  __shared__ __align__(16) uint2 sC[64 * kKLd];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int64_t idx = cta_off[blockIdx.x]; idx < cta_off[blockIdx.x + 1]; idx++) {
+    const int64_t gtile = cta_tiles[idx];
+    const int64_t pi = find_segment(tile_prefix, nprob, gtile);
+    const KendallBatchProblem pr = P[pi];
+    const int64_t lt = gtile - tile_prefix[pi];
+    int64_t tj = int64_t((sqrt(8.0 * double(lt) + 1.0) - 1.0) * 0.5);
+    while ((tj + 1) * (tj + 2) / 2 <= lt) tj++;
+    while (tj * (tj + 1) / 2 > lt) tj--;
+    const int64_t ti = lt - tj * (tj + 1) / 2;  // ti <= tj
+    const uint2 *Mp = M + pr.mask_off;
+    unsigned both[4][4], disc[4][4];
+    const int64_t row0 = ti * 64, col0 = tj * 64;
+    tile_counts(Mp, pr.p, Mp, pr.p, pr.K, row0, col0, 0, pr.K, sR, sC, both, disc);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int64_t r = row0 + ty + 16 * i;
+      if (r >= pr.p) continue;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int64_t c = col0 + tx + 16 * j;
+        if (c >= pr.p) continue;
+        const long long sv = (long long)both[i][j] - 2LL * (long long)disc[i][j];
+        const double tau =
+            (r == c) ? 1.0 : taub(sv, T[pr.var_off + c], T[pr.var_off + r]);
+        pr.out[r * pr.p + c] = tau;
+        if (ti != tj) pr.out[c * pr.p + r] = tau;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+int kendall_batch_launch(const KendallBatchProblem *d_probs, const int64_t *d_var_prefix,
+                         int64_t nprob, int64_t total_vars, const int64_t *d_tile_prefix,
+                         const int64_t *d_cta_tiles, const int64_t *d_cta_off, int64_t ncta,
+                         uint2 *d_masks, unsigned long long *d_T, cudaStream_t s) {
+  if (total_vars > 0) {
+    kendall_batch_masks_kernel<<<unsigned(total_vars), kKbMaskThreads, 0, s>>>(
+        d_probs, d_var_prefix, nprob, d_masks, d_T);
+    count_launch();
+  }
+  if (ncta > 0) {
+    kendall_batch_count_kernel<<<unsigned(ncta), kKT, 0, s>>>(d_probs, d_tile_prefix, nprob,
+                                                             d_cta_tiles, d_cta_off, d_masks, d_T);
+    count_launch();
+  }
   GT_CUDA(cudaGetLastError());
   return GT_OK;
 }

@@ -4,6 +4,9 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
+
+#include "gputools_gb300.h"
 
 namespace gt {
 
@@ -49,5 +52,24 @@ int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64
 // ([part][row][kpad], kpad a multiple of 64), stored as row-major float.
 int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,
                   int nsplit, float *C, int64_t ldc, cudaStream_t s);
+
+// kendall.cu: batched problems.  Masks of problem i start at mask_off
+// (uint2 words, K = Dr * Wn per variable); untied counts at var_off.
+struct KendallBatchProblem {
+  const float *X;  // variable-major p x n
+  int64_t p, n, Dr, Wn, K;
+  int64_t mask_off, var_off;
+  double *out;     // p x p, [y*p + x]
+};
+int kendall_batch_launch(const KendallBatchProblem *d_probs, const int64_t *d_var_prefix,
+                         int64_t nprob, int64_t total_vars, const int64_t *d_tile_prefix,
+                         const int64_t *d_cta_tiles, const int64_t *d_cta_off, int64_t ncta,
+                         uint2 *d_masks, unsigned long long *d_T, cudaStream_t s);
+
+// gram_tc.cu: batched cor(x) on tcgen05 (see pearson_batch_prepare).
+int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit, int bk,
+                          int64_t chunk_elems, const std::function<int(size_t, void **)> &alloc,
+                          std::function<int(cudaStream_t)> *run, int64_t *ntiles_out,
+                          int64_t *nctas_out);
 
 }  // namespace gt

@@ -214,6 +214,43 @@ void RgpuDistBackward(const float *points, const int *numPoints,
 void RgpuMdsStress(const float *points, const int *numPoints, const int *dim,
                    const float *delta, double *loss, float *dX);
 
+/* ---- batches (no counterpart in the reference) --------------------------- */
+
+/* One Pearson problem of a batch: cor(x) of a variable-major p x n device
+ * matrix, outputs p x p on the device (any may be NULL). */
+typedef struct gt_cor_problem {
+  const float *X;
+  int64_t p, n;
+  float *corr, *ts, *pairs;
+} gt_cor_problem;
+
+/* One Kendall problem of a batch: tau-b of cor(x), out p x p doubles. */
+typedef struct gt_kendall_problem {
+  const float *X;
+  int64_t p, n;
+  double *out;
+} gt_kendall_problem;
+
+typedef struct gt_batch_plan gt_batch_plan;
+
+/* Plan flags. */
+#define GT_BATCH_NO_GRAPH 1  /* launch the kernels directly, no CUDA graph   */
+#define GT_BATCH_AUTOTUNE 2  /* time the candidate tile configurations once  */
+
+/* Build a plan for `count` problems on the current device: buffers,
+ * descriptors, a host-balanced tile schedule, and (unless
+ * GT_BATCH_NO_GRAPH) a CUDA graph of the launches.  Creating the plan runs
+ * the batch once.  The problems' pointers must stay valid while the plan is
+ * used; gt_batch_plan_launch recomputes every output from the current
+ * inputs. */
+int gt_pmcc_batch_plan_create(const gt_cor_problem *problems, int64_t count,
+                              int flags, gt_batch_plan **plan);
+int gt_kendall_batch_plan_create(const gt_kendall_problem *problems,
+                                 int64_t count, int flags, gt_batch_plan **plan);
+int gt_batch_plan_launch(gt_batch_plan *plan, void *stream);
+const char *gt_batch_plan_describe(const gt_batch_plan *plan);
+void gt_batch_plan_destroy(gt_batch_plan *plan);
+
 /* Device buffers: t-scores as rtestT. */
 int gt_ttest_device(const float *d_pairs, const float *d_coeffs, int64_t n,
                     float *d_ts, void *stream);

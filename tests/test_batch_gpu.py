@@ -1,0 +1,95 @@
+"""Batched problems (one plan, replayed from a CUDA graph) against the
+single-problem C ABI paths and the oracle.
+
+Pearson: absolute error of r within the bf16x3 tolerance of the Pearson tests
+(2e-5) of the oracle, and equal to the single-problem tensor-core result to
+1e-6.  Kendall: bit-exact against the oracle's tau-b.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _shapes(rng, count, pmax, nmin, nmax):
+    p = np.exp(rng.uniform(np.log(1), np.log(pmax), count)).astype(int)
+    n = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count)).astype(int)
+    return list(zip(p.tolist(), n.tolist()))
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_pearson_batch_matches_single_and_oracle(gpu, oracle_mod, graph):
+    import torch
+    import gputools_gb300 as g
+    rng = np.random.default_rng(31)
+    shapes = _shapes(rng, 40, 600, 3, 900) + [(1, 10), (128, 64), (257, 129), (300, 2)]
+    xs = [rng.standard_normal((p, n)).astype(np.float32) * 2 + 5 for p, n in shapes]
+    dxs = [torch.from_numpy(x).cuda() for x in xs]
+    with g.BatchPlan(dxs, "pearson", graph=graph) as plan:
+        outs = plan.launch()
+        torch.cuda.synchronize()
+        for x, dx, o in zip(xs, dxs, outs):
+            corr = o["corr"].cpu().numpy()
+            want, wp, _ = oracle_mod.pearson(x)
+            ok = ~np.isnan(want)
+            assert np.array_equal(np.isnan(corr), np.isnan(want))
+            if ok.any():
+                assert np.abs(corr[ok] - want[ok]).max() <= 2e-5
+            assert np.all(o["pairs"].cpu().numpy() == x.shape[1])
+            single = g.pmcc_device(dx)["corr"].cpu().numpy()
+            assert np.allclose(corr, single, atol=1e-6, equal_nan=True)
+
+
+def test_pearson_batch_replay_sees_new_inputs(gpu, oracle_mod):
+    import torch
+    import gputools_gb300 as g
+    rng = np.random.default_rng(5)
+    xs = [torch.from_numpy(rng.standard_normal((p, 200)).astype(np.float32)).cuda()
+          for p in (50, 300, 7)]
+    with g.BatchPlan(xs, "pearson") as plan:
+        plan.launch()
+        for x in xs:
+            x.copy_(torch.from_numpy(rng.standard_normal(tuple(x.shape)).astype(np.float32)))
+        outs = plan.launch()
+        torch.cuda.synchronize()
+        for x, o in zip(xs, outs):
+            want, _, _ = oracle_mod.pearson(x.cpu().numpy())
+            assert np.abs(o["corr"].cpu().numpy() - want).max() <= 2e-5
+
+
+def test_pearson_batch_autotune(gpu, tmp_path, monkeypatch):
+    import torch
+    import gputools_gb300 as g
+    monkeypatch.setenv("GT_AUTOTUNE_CACHE", str(tmp_path / "tune.txt"))
+    rng = np.random.default_rng(6)
+    xs = [torch.from_numpy(rng.standard_normal((p, 300)).astype(np.float32)).cuda()
+          for p in (400, 90, 1000)]
+    with g.BatchPlan(xs, "pearson", autotune=True) as plan:
+        assert "tuned" in plan.describe()
+        plan.launch()
+    assert (tmp_path / "tune.txt").exists()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_kendall_batch_bit_exact(gpu, oracle_mod, graph):
+    import torch
+    import gputools_gb300 as g
+    rng = np.random.default_rng(41)
+    shapes = [(p, 200) for p, _ in _shapes(rng, 25, 200, 2, 3)] + [(1, 5), (65, 31), (130, 64), (3, 2)]
+    xs = [rng.integers(0, 20, (p, n)).astype(np.float32) for p, n in shapes]
+    with g.BatchPlan([torch.from_numpy(x).cuda() for x in xs], "kendall", graph=graph) as plan:
+        outs = plan.launch()
+        torch.cuda.synchronize()
+        for x, o in zip(xs, outs):
+            want, *_ = oracle_mod.kendall(x)
+            got = o.cpu().numpy()
+            assert np.array_equal(np.isnan(got), np.isnan(want))
+            assert np.array_equal(got[~np.isnan(got)], want[~np.isnan(want)])
+
+
+def test_batch_rejects_bad_problems(gpu):
+    import torch
+    import gputools_gb300 as g
+    x = torch.zeros((4, 0), dtype=torch.float32, device="cuda")
+    with pytest.raises(g.GpuToolsError, match="no observations"):
+        g.BatchPlan([x], "pearson")
