@@ -26,6 +26,7 @@ GT_LAYOUT_DIST = 1
 GT_GRAM_TC_BF16X3 = 0
 GT_GRAM_TC_BF16X6 = 1
 GT_GRAM_FP32 = 2
+GT_GRAM_TC_F16X3 = 3
 
 # (name, restype, argtypes) of every symbol include/gputools_gb300.h declares.
 _i, _i64, _f, _vp, _cp = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p, ctypes.c_char_p

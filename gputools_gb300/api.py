@@ -230,14 +230,15 @@ def kendall_device(X, Y=None, stream=None):
 
 
 def set_gram_path(path: str) -> None:
-    """"bf16x3" / "bf16x6" (tcgen05 split-bf16) or "fp32" (CUDA cores)."""
+    """"bf16x3" / "bf16x6" (tcgen05 split-bf16), "f16x3" (tcgen05, scaled
+    split-fp16) or "fp32" (CUDA cores)."""
     code = {"bf16x3": _lib.GT_GRAM_TC_BF16X3, "bf16x6": _lib.GT_GRAM_TC_BF16X6,
-            "fp32": _lib.GT_GRAM_FP32}[path]
+            "fp32": _lib.GT_GRAM_FP32, "f16x3": _lib.GT_GRAM_TC_F16X3}[path]
     check(load().gt_set_gram_path(code))
 
 
 def get_gram_path() -> str:
-    return {0: "bf16x3", 1: "bf16x6", 2: "fp32"}[load().gt_get_gram_path()]
+    return {0: "bf16x3", 1: "bf16x6", 2: "fp32", 3: "f16x3"}[load().gt_get_gram_path()]
 
 
 # ---------------------------------------------------------------------------

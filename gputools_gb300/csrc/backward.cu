@@ -47,10 +47,10 @@ __device__ __forceinline__ void put_parts<float>(float *dst, int64_t, int64_t id
 template <>
 __device__ __forceinline__ void put_parts<__nv_bfloat16>(__nv_bfloat16 *dst, int64_t plane,
                                                          int64_t idx, float v, int ns) {
-  __nv_bfloat16 p[3];
-  if (ns == 3) tc::split_bf16<3>(v, p);
-  else tc::split_bf16<2>(v, p);
-  for (int q = 0; q < ns; q++) dst[q * plane + idx] = p[q];
+  uint16_t p[3];
+  if (ns == 3) tc::split_parts<tc::KIND_BF16X6>(v, p);
+  else tc::split_parts<tc::KIND_BF16X3>(v, p);
+  for (int q = 0; q < ns; q++) dst[q * plane + idx] = __ushort_as_bfloat16(p[q]);
 }
 
 // S = G + G^T as rows j, columns i (ld kp >= p, zero padded), float or bf16
@@ -355,7 +355,9 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     cudaError_t e = launch_allpairs_simt<OpDotB, OutStore, 8, 8>(a, OpDotB{}, OutStore{W, n}, s);
     if (e != cudaSuccess) return fail(GT_ECUDA, "adjoint GEMM launch: %s", cudaGetErrorString(e));
   } else {
-    const int ns = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
+    // the adjoint's operands (G + G^T, z^T) are not unit-scaled, so the
+    // f16x3 setting runs as bf16x6, its precision class
+    const int ns = path == GT_GRAM_TC_BF16X3 ? 2 : 3;
     GT_TRY(ws_get(WS_SCRATCH0, size_t(ns) * size_t(p) * size_t(kp) * 2, &pS));
     GT_TRY(ws_get(WS_SCRATCH1, size_t(ns) * size_t(n) * size_t(kp) * 2, &pZ));
     sym_operand_kernel<__nv_bfloat16>

@@ -31,6 +31,7 @@ struct gt_batch_plan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t tiles = 0, ctas = 0;
+  int *err = nullptr;  // device error word of the tensor-core kernel, if any
   double config_ms = 0.0;
   char config[160] = {0};
 };
@@ -98,6 +99,11 @@ int plan_finalize(gt_batch_plan *p, int flags) {
   if (st == GT_OK) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) st = fail(GT_ECUDA, "batch plan first run: %s", cudaGetErrorString(e));
+  }
+  if (st == GT_OK && p->err) {
+    int h = 0;
+    GT_CUDA(cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) st = fail(GT_ETIMEOUT, "batch plan first run: a tensor-core kernel wait timed out");
   }
   if (st == GT_OK && !(flags & GT_BATCH_NO_GRAPH)) {
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -248,20 +254,24 @@ void cache_store(const std::string &key, int v) {
   if (f) f << key << " " << v << "\n";
 }
 
-int build_pearson(const gt_cor_problem *probs, int64_t count, int nsplit, const TileConfig &cfg,
+const char *kind_name(int kind) {
+  return kind == GT_GRAM_TC_BF16X6 ? "bf16x6" : (kind == GT_GRAM_TC_F16X3 ? "f16x3" : "bf16x3");
+}
+
+int build_pearson(const gt_cor_problem *probs, int64_t count, int kind, const TileConfig &cfg,
                   gt_batch_plan **out) {
   auto *p = new gt_batch_plan();
   p->kind = 0;
   cudaGetDevice(&p->device);
   auto alloc = [p](size_t bytes, void **ptr) { return plan_alloc(p, bytes, ptr); };
-  int st = pearson_batch_prepare(probs, count, nsplit, cfg.bk, cfg.chunk, alloc, &p->run,
-                                 &p->tiles, &p->ctas);
+  int st = pearson_batch_prepare(probs, count, kind, cfg.bk, cfg.chunk, alloc, &p->run,
+                                 &p->tiles, &p->ctas, &p->err);
   if (st != GT_OK) {
     plan_free(p);
     return st;
   }
-  std::snprintf(p->config, sizeof(p->config), "bf16x%d %s, %lld tiles on %lld ctas",
-                nsplit == 3 ? 6 : 3, cfg.name, (long long)p->tiles, (long long)p->ctas);
+  std::snprintf(p->config, sizeof(p->config), "%s %s, %lld tiles on %lld ctas", kind_name(kind),
+                cfg.name, (long long)p->tiles, (long long)p->ctas);
   *out = p;
   return GT_OK;
 }
@@ -295,14 +305,14 @@ int pearson_batch_plan(const gt_cor_problem *probs, int64_t count, int flags,
   const int path = gt_get_gram_path();
   if (path == GT_GRAM_FP32)
     return fail(GT_EUNSUPPORTED, "batched Pearson runs on the tensor-core Gram paths");
-  const int nsplit = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
-  const TileConfig *cands = nsplit == 3 ? kX6Configs : kX3Configs;
-  const int ncand = nsplit == 3 ? int(sizeof(kX6Configs) / sizeof(kX6Configs[0]))
-                                : int(sizeof(kX3Configs) / sizeof(kX3Configs[0]));
+  const bool x6 = path == GT_GRAM_TC_BF16X6;
+  const TileConfig *cands = x6 ? kX6Configs : kX3Configs;
+  const int ncand = x6 ? int(sizeof(kX6Configs) / sizeof(kX6Configs[0]))
+                       : int(sizeof(kX3Configs) / sizeof(kX3Configs[0]));
   double work = 0.0;
   for (int64_t i = 0; i < count; i++) work += double(probs[i].p) * double(probs[i].p) * double(probs[i].n);
   char key[128];
-  std::snprintf(key, sizeof(key), "pearson:x%d:%lld:%.3e", nsplit == 3 ? 6 : 3, (long long)count,
+  std::snprintf(key, sizeof(key), "pearson:%s:%lld:%.3e", kind_name(path), (long long)count,
                 work);
   int choice = 0;
   if (flags & GT_BATCH_AUTOTUNE) {
@@ -310,7 +320,7 @@ int pearson_batch_plan(const gt_cor_problem *probs, int64_t count, int flags,
     double best_ms = 0.0;
     for (int c = 0; c < ncand; c++) {
       gt_batch_plan *cand = nullptr;
-      GT_TRY(build_pearson(probs, count, nsplit, cands[c], &cand));
+      GT_TRY(build_pearson(probs, count, path, cands[c], &cand));
       double ms = 0.0;
       int st = time_plan(cand, &ms);
       if (st != GT_OK) {
@@ -343,7 +353,7 @@ int pearson_batch_plan(const gt_cor_problem *probs, int64_t count, int flags,
   const int cached = cache_lookup(key);
   if (cached >= 0 && cached < ncand) choice = cached;
   gt_batch_plan *p = nullptr;
-  GT_TRY(build_pearson(probs, count, nsplit, cands[choice], &p));
+  GT_TRY(build_pearson(probs, count, path, cands[choice], &p));
   int st = plan_finalize(p, flags);
   if (st != GT_OK) {
     plan_free(p);

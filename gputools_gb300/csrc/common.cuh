@@ -64,6 +64,13 @@ class ProfScope {
   cudaEvent_t e0_ = nullptr;
 };
 
+// Device-usable address through which kernels may write the host buffer
+// `host` directly (page-locked memory, reached over NVLink-C2C or PCIe), or
+// nullptr when the buffer must be staged through device memory: pageable
+// pages, even where the GPU can reach them, may be unpopulated and fault one
+// by one.  GT_DIRECT_HOST=0 disables it.
+void *host_direct_ptr(void *host);
+
 // Host-side reads of the device the library runs on.
 int current_device(int *dev);
 int sm_count();

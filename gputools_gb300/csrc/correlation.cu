@@ -30,13 +30,15 @@ namespace gt {
 
 namespace {
 
-constexpr int kStatThreads = kColStatThreads;
+constexpr int kStatThreads = 256;  // eight variables per CTA, one warp each
 
 __global__ void __launch_bounds__(kStatThreads)
-colstats_kernel(const float *__restrict__ X, int64_t n, int use, ColStats *__restrict__ out) {
-  __shared__ double sh[32];
-  const ColStats st = colstats_block(X + int64_t(blockIdx.x) * n, n, use, sh);
-  if (threadIdx.x == 0) out[blockIdx.x] = st;
+colstats_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int use,
+                ColStats *__restrict__ out) {
+  const int64_t v = (int64_t(blockIdx.x) * kStatThreads + threadIdx.x) >> 5;
+  if (v >= nvar) return;  // whole warps
+  const ColStats st = colstats_warp(X + v * n, n, use);
+  if ((threadIdx.x & 31) == 0) out[v] = st;
 }
 
 // z[v][k] = (x - mean) * inv_norm in float, rows of length ldz (>= n, pad
@@ -48,13 +50,14 @@ __global__ void normalize_f32_kernel(const float *__restrict__ X, int64_t nvar, 
                                      float padv, float *__restrict__ Z) {
   const int64_t v = blockIdx.x;
   const ColStats s = st[v];
+  const Centerer cen(s);
   const float *x = X + v * n;
   float *z = Z + v * ldz;
   for (int64_t k = threadIdx.x; k < ldz; k += blockDim.x) {
     float val;
     if (k >= n) val = padv;
     else if (use == 0 && s.flags) val = __int_as_float(0x7fc00000);
-    else val = float((double(x[k]) - s.mean) * s.inv_norm);
+    else val = cen(x[k]);
     z[k] = val;
   }
 }
@@ -163,7 +166,8 @@ int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz,
   *Z = static_cast<float *>(pz);
   *st = static_cast<ColStats *>(pst);
   ProfScope prof("pearson_prologue", s);
-  colstats_kernel<<<unsigned(nvar), kStatThreads, 0, s>>>(dX, n, use, *st);
+  colstats_kernel<<<unsigned(cdiv(nvar, kStatThreads / 32)), kStatThreads, 0, s>>>(dX, nvar, n, use,
+                                                                                 *st);
   count_launch();
   const float padv = use == 0 ? 0.f : __builtin_nanf("");
   normalize_f32_kernel<<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, ldz, *st, use, padv, *Z);
@@ -179,14 +183,15 @@ int launch_colstats(const float *dX, int64_t nvar, int64_t n, int use, ColStats 
                     cudaStream_t s) {
   if (nvar == 0) return GT_OK;
   if (nvar > 2147483647LL) return fail(GT_EINVAL, "too many variables");
-  colstats_kernel<<<unsigned(nvar), kStatThreads, 0, s>>>(dX, n, use, st);
+  colstats_kernel<<<unsigned(cdiv(nvar, kStatThreads / 32)), kStatThreads, 0, s>>>(dX, nvar, n, use,
+                                                                                 st);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
 }
 
 // prologue for the tensor-core path lives in gram_tc.cu
-int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, int slot_z,
+int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int kind, int slot_z,
                         int slot_st, void **Z, int64_t *kpad, cudaStream_t s);
 
 int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t nB, int64_t n,
@@ -195,13 +200,12 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
   PearsonOut po{corr, ts, pairs, nB, float(n), symmetric};
   const int path = gt_get_gram_path();
   if (use == GT_EVERYTHING && path != GT_GRAM_FP32 && n > 0) {
-    const int nsplit = path == GT_GRAM_TC_BF16X6 ? 3 : 2;
     void *zA = nullptr, *zB = nullptr;
     int64_t kpad = 0;
-    GT_TRY(pearson_tc_prologue(dA, nA, n, nsplit, WS_SCRATCH0, WS_SCRATCH2, &zA, &kpad, s));
+    GT_TRY(pearson_tc_prologue(dA, nA, n, path, WS_SCRATCH0, WS_SCRATCH2, &zA, &kpad, s));
     if (symmetric) zB = zA;
-    else GT_TRY(pearson_tc_prologue(dB, nB, n, nsplit, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
-    return pearson_tc(zA, nA, zB, nB, kpad, nsplit, po, s);
+    else GT_TRY(pearson_tc_prologue(dB, nB, n, path, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
+    return pearson_tc(zA, nA, zB, nB, kpad, path, po, s);
   }
   const int64_t ldz = (n + 3) / 4 * 4;
   float *zA = nullptr, *zB = nullptr;
@@ -292,15 +296,19 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
       GT_TRY(gt::same_contents(static_cast<float *>(dA), static_cast<float *>(dB), nA * n, &sym, s));
   }
   if (sym) dB = dA;
-  if (corr) GT_TRY(gt::ws_get(gt::WS_OUT0, outb, &o0));
-  if (ts) GT_TRY(gt::ws_get(gt::WS_OUT1, outb, &o1));
-  if (pairs) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));
+  // outputs the kernels can write in place (no staging copy), else workspace
+  void *h0 = corr ? gt::host_direct_ptr(corr) : nullptr;
+  void *h1 = ts ? gt::host_direct_ptr(ts) : nullptr;
+  void *h2 = pairs ? gt::host_direct_ptr(pairs) : nullptr;
+  if (corr && !(o0 = h0)) GT_TRY(gt::ws_get(gt::WS_OUT0, outb, &o0));
+  if (ts && !(o1 = h1)) GT_TRY(gt::ws_get(gt::WS_OUT1, outb, &o1));
+  if (pairs && !(o2 = h2)) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));
   GT_TRY(gt::pearson_impl(use, static_cast<float *>(dA), nA, static_cast<float *>(dB), nB, n,
                           static_cast<float *>(o2), static_cast<float *>(o0),
                           static_cast<float *>(o1), sym ? 1 : 0, s));
-  if (corr) GT_CUDA(cudaMemcpyAsync(corr, o0, outb, cudaMemcpyDeviceToHost, s));
-  if (ts) GT_CUDA(cudaMemcpyAsync(ts, o1, outb, cudaMemcpyDeviceToHost, s));
-  if (pairs) GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
+  if (corr && !h0) GT_CUDA(cudaMemcpyAsync(corr, o0, outb, cudaMemcpyDeviceToHost, s));
+  if (ts && !h1) GT_CUDA(cudaMemcpyAsync(ts, o1, outb, cudaMemcpyDeviceToHost, s));
+  if (pairs && !h2) GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
   GT_CUDA(cudaStreamSynchronize(s));
   bool failed = false;
   GT_TRY(gt::tc_check_error(s, &failed));

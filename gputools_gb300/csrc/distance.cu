@@ -206,11 +206,13 @@ extern "C" int gt_distances(const float *points, int64_t n, int64_t dim, float *
   cudaStream_t st = gt::lib_stream();
   void *dp = nullptr, *dout = nullptr;
   GT_TRY(gt::ws_get(gt::WS_IN_A, size_t(n) * size_t(dim) * 4, &dp));
-  GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(n) * size_t(n) * 4, &dout));
+  void *direct = gt::host_direct_ptr(out);
+  if (!(dout = direct)) GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(n) * size_t(n) * 4, &dout));
   GT_CUDA(cudaMemcpyAsync(dp, points, size_t(n) * size_t(dim) * 4, cudaMemcpyHostToDevice, st));
   GT_TRY(gt_distances_device(static_cast<float *>(dp), n, dim, static_cast<float *>(dout),
                              GT_LAYOUT_FULL, method, p, st));
-  GT_CUDA(cudaMemcpyAsync(out, dout, size_t(n) * size_t(n) * 4, cudaMemcpyDeviceToHost, st));
+  if (!direct)
+    GT_CUDA(cudaMemcpyAsync(out, dout, size_t(n) * size_t(n) * 4, cudaMemcpyDeviceToHost, st));
   GT_CUDA(cudaStreamSynchronize(st));
   bool failed = false;
   GT_TRY(gt::tc_check_error(st, &failed));

@@ -8,14 +8,18 @@
 // (inst/cuda/distance.cu:40-78).
 //
 // Operands.  Each value v (Pearson: the normalised column entry
-// z = (x - mean)/||x - mean|| computed in FP64 and rounded to float;
-// Euclidean: the centred coordinate) is split into bf16 parts
-// v = v0 + v1 [+ v2], each the round-to-nearest bf16 of the remainder of the
+// z = (x - mean)/||x - mean||; Euclidean: the centred coordinate) is split
+// into 16-bit parts, each the round-to-nearest of the remainder of the
 // previous ones.  The parts live in separate planes [part][row][k] (K
 // contiguous, padded to a multiple of 64 with zeros).  The Gram entry is the
 // sum of the part products of total order at most NSPLIT-1:
-//   NSPLIT = 2 ("bf16x3"): v0w0 + v0w1 + v1w0            (~2^-16 relative)
-//   NSPLIT = 3 ("bf16x6"): + v0w2 + v1w1 + v2w0            (float32-level)
+//   bf16x3: two bf16 parts, v0w0 + v0w1 + v1w0            (~2^-16 relative)
+//   bf16x6: three bf16 parts, + v0w2 + v1w1 + v2w0        (float32-level)
+//   f16x3:  two fp16 parts of v scaled by a power of two (Pearson: 2^14 for
+//           every row, since |z| <= 1; Euclidean: per point, its largest
+//           magnitude into [2^14, 2^15)), three products     (~2^-21)
+// f16x3 costs what bf16x3 costs on the tensor core; the epilogue removes the
+// scales exactly.
 //
 // Accumulation.  The tensor core's FP32 accumulation rounds every add toward
 // zero, so its error grows linearly with the number of adds into one
@@ -61,8 +65,6 @@ namespace gt {
 
 namespace {
 
-constexpr int kTcThreads = 320;                   // 2 control warps + 8 epilogue warps
-constexpr int kEpiWarps = 8;
 constexpr int kBM = 128, kBN = 256;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per barrier wait
 constexpr uint64_t kDrainLimitNs = 200000000ull;  // 0.2 s for in-flight work at exit
@@ -71,41 +73,86 @@ constexpr int kMaxSmem = 232448;                  // dynamic shared memory per C
 constexpr int kEpiTileFloats = 32 * 33;           // one warp's padded 32 x 32 staging tile
 
 // ----------------------------------------------------------------- tiling
+// Symmetric problems schedule, in column block tj, the row blocks
+// 0 .. min(2 tj + 1, tr - 1): the 128-row blocks that reach the upper
+// triangle of a 256-column block.
 struct TileSpace {
   int64_t tr, tc;    // row blocks (128), column blocks (256)
   int64_t j0;        // symmetric: column blocks whose tile count is 2*tj + 2
-  int64_t ntiles;
+  int64_t ntiles;    // below 2^31
+  int64_t group;     // column blocks per band of the tile order (power of two)
+  int group_log2;
   int symmetric;
 };
 
-// Symmetric problems: column block tj holds row blocks 0 .. min(2 tj + 1, tr-1)
-// (the 128-row blocks that reach the upper triangle of a 256-column block).
-__host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t, int64_t &ti,
+// Tile order.  Column blocks are grouped into bands of `group` (a power of
+// two); a band's tiles are consecutive, row block by row block, so the CTAs
+// working at one time share a few operand panels in L2: the band's B panels
+// stay resident while its A panels stream past once per band instead of once
+// per column block.  Every role of every CTA evaluates this per tile, so it
+// runs in 32-bit arithmetic (the host keeps tile counts below 2^31): 64-bit
+// integer division is a long software sequence on the GPU.
+__host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t64, int64_t &ti,
                                             int64_t &tj) {
+  const uint32_t t = uint32_t(t64), tr = uint32_t(ts.tr), tc = uint32_t(ts.tc);
+  const uint32_t G = uint32_t(ts.group), lg = uint32_t(ts.group_log2);
   if (!ts.symmetric) {
-    tj = t / ts.tr;
-    ti = t - tj * ts.tr;
+    const uint32_t c0 = (t / (tr << lg)) << lg;
+    const uint32_t g = (tc - c0) < G ? (tc - c0) : G;
+    const uint32_t u = t - c0 * tr;
+    const uint32_t i = u / g;
+    ti = i;
+    tj = c0 + (u - i * g);
     return;
   }
-  const int64_t head = ts.j0 * (ts.j0 + 1);
+  // column block of t in column-major order, hence its band
+  const uint32_t j0 = uint32_t(ts.j0);
+  const uint32_t head = j0 * (j0 + 1);
+  uint32_t col;
   if (t < head) {
-    int64_t j = int64_t((sqrt(4.0 * double(t) + 1.0) - 1.0) * 0.5);
-    while ((j + 1) * (j + 2) <= t) j++;
-    while (j * (j + 1) > t) j--;
-    tj = j;
-    ti = t - j * (j + 1);
+    // float estimate, corrected in integers
+    int32_t j = int32_t((sqrtf(float(t) * 4.f + 1.f) - 1.f) * 0.5f);
+    if (j < 0) j = 0;
+    while (uint32_t(j + 1) * uint32_t(j + 2) <= t) j++;
+    while (uint32_t(j) * uint32_t(j + 1) > t) j--;
+    col = uint32_t(j);
   } else {
-    const int64_t u = t - head;
-    tj = ts.j0 + u / ts.tr;
-    ti = u - (tj - ts.j0) * ts.tr;
+    col = j0 + (t - head) / tr;
+  }
+  const uint32_t c0 = (col >> lg) << lg;
+  const uint32_t c1 = (c0 + G) < tc ? (c0 + G) : tc;
+  const uint32_t g = c1 - c0;
+  const uint32_t pre = c0 <= j0 ? c0 * (c0 + 1) : head + (c0 - j0) * tr;
+  uint32_t u = t - pre;
+  // rows 0 .. 2 c0 + 1 meet every column block of the band
+  const uint32_t F = (2 * c0 + 2) < tr ? (2 * c0 + 2) : tr;
+  if (u < F * g) {
+    const uint32_t i = u / g;
+    ti = i;
+    tj = c0 + (u - i * g);
+    return;
+  }
+  // row F + w meets the last g - 1 - floor(w / 2) column blocks
+  u -= F * g;
+  for (uint32_t w = 0;; w++) {
+    const uint32_t cnt = g - 1 - w / 2;
+    if (u < cnt) {
+      ti = F + w;
+      tj = c1 - cnt + u;
+      return;
+    }
+    u -= cnt;
   }
 }
 
-TileSpace make_tiles(int64_t nr, int64_t nc, bool symmetric) {
+TileSpace make_tiles(int64_t nr, int64_t nc, bool symmetric, int64_t group) {
   TileSpace ts;
   ts.tr = cdiv(nr, kBM);
   ts.tc = cdiv(nc, kBN);
   ts.symmetric = symmetric ? 1 : 0;
+  ts.group_log2 = 0;
+  while ((int64_t(2) << ts.group_log2) <= group) ts.group_log2++;
+  ts.group = int64_t(1) << ts.group_log2;
   if (symmetric) {
     ts.j0 = ts.tr / 2;
     if (ts.j0 > ts.tc) ts.j0 = ts.tc;
@@ -117,9 +164,31 @@ TileSpace make_tiles(int64_t nr, int64_t nc, bool symmetric) {
   return ts;
 }
 
+// Band width for operand planes of `panel_bytes` per 256-row B panel: as
+// many B panels as fit in about 40 MB of L2, at most 16.
+int64_t band_group(int64_t panel_bytes) {
+  const int64_t g = (int64_t(40) << 20) / (panel_bytes > 0 ? panel_bytes : 1);
+  return g < 1 ? 1 : (g > 16 ? 16 : g);
+}
+
 // ----------------------------------------------------------------- finishes
 // Each finish handles a warp's 32 x 32 block: lane = row r (consecutive rows
-// across lanes), g[j] = entry (r, c0 + j); wsm is the warp's staging tile.
+// across lanes), g[j] = entry (r, c0 + j).  The epilogue context carries the
+// warp's staging tile and the rows / columns of its part of the tile; after
+// the last block of a tile the epilogue calls flush().
+
+constexpr int kEuclidList = 64;  // pending near-zero pairs per epilogue warp
+
+struct EpiCtx {
+  float *wsm;       // 32 x 33 staging tile
+  uint32_t *list;   // kEuclidList entries: (row - rbase) << 8 | (col - col0)
+  float2 *cnrm;     // the warp's columns' {norm, scale} (Euclidean)
+  float2 me;        // this lane's row's {norm, scale} (Euclidean)
+  int nlist;        // warp-uniform
+  int ncols;        // columns per warp (128 or 64)
+  int64_t rbase;    // first row of the warp's 32 rows
+  int64_t col0;     // first column of the warp's columns
+};
 
 __device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
 
@@ -134,17 +203,56 @@ struct PearsonFinish {
   float *corr, *ts, *pairs;
   int64_t ld, nr, nc;
   float npairs, sq_nm2;
+  float gscale;  // removes the operand scales (2^-28 for f16x3, else 1)
   int symmetric;
 
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+  __device__ __forceinline__ void put(float *pc, float *pt, float *pp, float v) const {
+    if (corr) *pc = v;
+    if (ts) *pt = signif_fast(v, sq_nm2);
+    if (pairs) *pp = npairs;
+  }
+
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
+    float *wsm = ctx.wsm;
+    const int64_t rbase = r - lane;
+    // interior block: every entry exists and (symmetric) lies above the diagonal
+    const bool interior = (c0 + 31 < nc) && (symmetric ? (rbase + 31 < c0) : (rbase + 31 < nr));
+    if (interior) {
+      // branch-free stores with pointer increments
+      if (symmetric) {
+        const int64_t o = c0 * ld + r;
+        float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          put(pc, pt, pp, clamp_r(g[j] * gscale));
+          pc += ld;
+          pt += ld;
+          pp += ld;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
+      __syncwarp();
+      const int64_t o = rbase * ld + c0 + lane;
+      float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
+#pragma unroll 8
+      for (int i = 0; i < 32; i++) {
+        put(pc, pt, pp, clamp_r(wsm[i * 33 + lane] * gscale));
+        pc += ld;
+        pt += ld;
+        pp += ld;
+      }
+      __syncwarp();
+      return;
+    }
     // mirror orientation (lanes hold consecutive rows): coalesced from registers
     if (symmetric && r < nr) {
 #pragma unroll
       for (int j = 0; j < 32; j++) {
         const int64_t c = c0 + j;
         if (c < nc && r < c) {
-          const float v = clamp_r(g[j]);
+          const float v = clamp_r(g[j] * gscale);
           const int64_t o = c * ld + r;
           if (corr) corr[o] = v;
           if (ts) ts[o] = signif_fast(v, sq_nm2);
@@ -156,14 +264,13 @@ struct PearsonFinish {
 #pragma unroll
     for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
     __syncwarp();
-    const int64_t rbase = r - lane;
     const int64_t c = c0 + lane;
     int64_t o = rbase * ld + c;
     for (int i = 0; i < 32; i++, o += ld) {
       const int64_t ri = rbase + i;
       if (ri >= nr) break;
       if (c >= nc || (symmetric && c < ri)) continue;
-      float v = clamp_r(wsm[i * 33 + lane]);
+      float v = clamp_r(wsm[i * 33 + lane] * gscale);
       if (symmetric && c == ri && v == v) v = 1.f;
       if (corr) corr[o] = v;
       if (ts) ts[o] = signif_fast(v, sq_nm2);
@@ -171,89 +278,186 @@ struct PearsonFinish {
     }
     __syncwarp();
   }
+  __device__ void begin_tile(int64_t, EpiCtx &) const {}
+  __device__ void flush(EpiCtx &) const {}
 };
 
 // Operands are the points centred by their column means (distances do not
-// change).  d^2 = |a|^2 + |b|^2 - 2 G with FP32 norms rounded from FP64; an
+// change).  d^2 = |a|^2 + |b|^2 - 2 G with float norms (compensated sums); an
 // entry whose d^2 is below tau * (|a|^2 + |b|^2), where rounding of the
-// contraction could dominate, is recomputed from the original float points
-// by the warp (float differences and partial sums per lane, FP64 sum across
-// lanes), so exact duplicates come out exactly 0.
+// contraction could dominate, is recomputed from the original float points:
+// the warp queues such pairs and recomputes four at a time, eight lanes per
+// pair (float differences, squares with their FMA residuals, compensated
+// float-pair sums), overwriting the estimate it stored first.  Exact
+// duplicates come out exactly 0.
 struct EuclidFinish {
-  const float *norm2;
+  const float2 *nrm;  // per point {|c|^2, 2^-s} (s its f16x3 scale exponent, else 0),
+                      // zero padded to a multiple of 256 points
   const float *pts;
   float *out;
   int64_t n, dim;
   int layout;  // GT_LAYOUT_FULL / GT_LAYOUT_DIST
   float tau;
+  int vec4;    // pts 16-byte aligned and dim % 4 == 0
 
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
-    const unsigned FULL = 0xffffffffu;
+  __device__ __forceinline__ int64_t dist_index(int64_t i, int64_t j) const {  // i < j
+    return n * i - i * (i + 1) / 2 - i - 1 + j;
+  }
+
+  // The lane's row values and the warp's column values for this tile.
+  __device__ void begin_tile(int64_t r, EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
-    const int64_t cl = c0 + lane;
-    const float nbl = cl < n ? norm2[cl] : 0.f;
-    const float na = r < n ? norm2[r] : 0.f;
-    // this lane's row uses columns c0 + j with r < c0 + j < n
-    const int64_t lo64 = r + 1 - c0, hi64 = n - c0;
-    const int jlo = lo64 < 0 ? 0 : (lo64 > 32 ? 32 : int(lo64));
-    const int jhi = r >= n ? 0 : (hi64 > 32 ? 32 : (hi64 < 0 ? 0 : int(hi64)));
-    float v[32];
-    unsigned pend = 0u;
-#pragma unroll
-    for (int j = 0; j < 32; j++) {
-      const float s = na + __shfl_sync(FULL, nbl, j);
-      const float d2 = fmaf(-2.f, g[j], s);
-      const bool valid = (j >= jlo) & (j < jhi);
-      pend |= unsigned(valid & (d2 < tau * s)) << j;
-      v[j] = valid ? tc::sqrt_approx(fmaxf(d2, 0.f)) : 0.f;
-    }
-    while (true) {
-      const unsigned any = __ballot_sync(FULL, pend != 0u);
-      if (!any) break;
-      const int src = __ffs(int(any)) - 1;
-      const int j = __shfl_sync(FULL, __ffs(int(pend)) - 1, src);
-      const long long rr = __shfl_sync(FULL, (long long)r, src);
-      const float *pa = pts + rr * dim, *pb = pts + (c0 + j) * dim;
-      float part = 0.f;
-      for (int64_t k = lane; k < dim; k += 32) {
-        const float d = pa[k] - pb[k];
-        part = fmaf(d, d, part);
-      }
-      double acc = double(part);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
-      if (lane == src) {
-        const float d = sqrtf(float(acc));
-#pragma unroll
-        for (int q = 0; q < 32; q++)
-          if (q == j) v[q] = d;
-        pend &= ~(1u << j);
-      }
-    }
-    const bool full = layout == GT_LAYOUT_FULL;
-    if (full && r < n) {
-#pragma unroll
-      for (int j = 0; j < 32; j++)
-        if (j >= jlo && j < jhi) out[(c0 + j) * n + r] = v[j];
-    }
-#pragma unroll
-    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = v[j];
+    ctx.me = nrm[r];
+    for (int k = lane; k < ctx.ncols; k += 32) ctx.cnrm[k] = nrm[ctx.col0 + k];
     __syncwarp();
-    const int64_t rbase = r - lane, c = c0 + lane;
-    // offset of (row rbase, column 0): full n*r; R dist n*r - r(r+1)/2 - r - 1
-    int64_t off = full ? rbase * n : n * rbase - rbase * (rbase + 1) / 2 - rbase - 1;
-    for (int i = 0; i < 32; i++) {
-      const int64_t ri = rbase + i;
-      if (ri >= n) break;
-      if (c < n) {
+  }
+
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
+    const int lane = threadIdx.x & 31;
+    float *wsm = ctx.wsm;
+    const int64_t rbase = r - lane;
+    const float na = ctx.me.x, ra = -2.f * ctx.me.y;
+    // the block's column values (shared-memory broadcasts)
+    const float2 *cv = ctx.cnrm + (c0 - ctx.col0);
+    const bool full = layout == GT_LAYOUT_FULL;
+    // interior block: every row below every column, every column < n
+    const bool interior = (rbase + 31 < c0) && (c0 + 31 < n);
+    unsigned pend = 0u;
+    if (interior) {
+      float *om = out + (c0 * n + r);  // mirror orientation (full layout)
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const float2 cj = cv[j];
+        const float s = na + cj.x;
+        const float d2 = fmaf(ra * cj.y, g[j], s);
+        pend |= (__float_as_uint(fmaf(-tau, s, d2)) >> 31) << j;
+        const float v = tc::sqrt_approx(fmaxf(d2, 0.f));
+        wsm[lane * 33 + j] = v;
         if (full) {
-          if (c >= ri) out[off + c] = (c == ri) ? 0.f : wsm[i * 33 + lane];
-        } else if (c > ri) {
-          out[off + c] = wsm[i * 33 + lane];
+          *om = v;
+          om += n;
         }
       }
-      off += full ? n : n - ri - 2;
+      __syncwarp();
+      float *o = out + ((full ? rbase * n : dist_index(rbase, 0)) + c0 + lane);
+#pragma unroll 8
+      for (int i = 0; i < 32; i++) {
+        *o = wsm[i * 33 + lane];
+        o += full ? n : n - (rbase + i) - 2;
+      }
+    } else {
+      // this lane's row uses columns c0 + j with r < c0 + j < n
+      const int64_t lo64 = r + 1 - c0, hi64 = n - c0;
+      const int jlo = lo64 < 0 ? 0 : (lo64 > 32 ? 32 : int(lo64));
+      const int jhi = r >= n ? 0 : (hi64 > 32 ? 32 : (hi64 < 0 ? 0 : int(hi64)));
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const float2 cj = cv[j];
+        const float s = na + cj.x;
+        const float d2 = fmaf(ra * cj.y, g[j], s);
+        const bool valid = (j >= jlo) & (j < jhi);
+        pend |= unsigned(valid & (d2 < tau * s)) << j;
+        const float v = valid ? tc::sqrt_approx(fmaxf(d2, 0.f)) : 0.f;
+        wsm[lane * 33 + j] = v;
+        if (full && valid) out[(c0 + j) * n + r] = v;
+      }
+      __syncwarp();
+      const int64_t c = c0 + lane;
+      // offset of (row rbase, column 0): full n*r; R dist n*r - r(r+1)/2 - r - 1
+      int64_t off = full ? rbase * n : dist_index(rbase, 0);
+      for (int i = 0; i < 32; i++) {
+        const int64_t ri = rbase + i;
+        if (ri >= n) break;
+        if (c < n) {
+          if (full) {
+            if (c >= ri) out[off + c] = (c == ri) ? 0.f : wsm[i * 33 + lane];
+          } else if (c > ri) {
+            out[off + c] = wsm[i * 33 + lane];
+          }
+        }
+        off += full ? n : n - ri - 2;
+      }
     }
+    __syncwarp();
+    // queue the pairs to recompute (after their estimates are stored)
+    const unsigned FULLM = 0xffffffffu;
+    const uint32_t cofs = uint32_t(c0 - ctx.col0);
+    while (__any_sync(FULLM, pend != 0u)) {
+      const int cnt = __popc(pend);
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULLM, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int total = __shfl_sync(FULLM, incl, 31);
+      const int room = kEuclidList - ctx.nlist;
+      const int start = incl - cnt;
+      int take = room - start;
+      take = take < 0 ? 0 : (take > cnt ? cnt : take);
+      for (int t = 0; t < take; t++) {
+        const int jb = __ffs(int(pend)) - 1;
+        pend &= pend - 1u;
+        ctx.list[ctx.nlist + start + t] = (uint32_t(lane) << 8) | (cofs + uint32_t(jb));
+      }
+      ctx.nlist += total < room ? total : room;
+      if (ctx.nlist == kEuclidList) flush(ctx);
+    }
+  }
+
+  __device__ __forceinline__ static void sq_add(float d, FloatPairSum &acc, float &res) {
+    const float q = d * d;
+    res += fmaf(d, d, -q);
+    acc.add(q);
+  }
+
+  // Recomputes the queued pairs: group of 8 lanes per pair, 4 pairs per round.
+  __device__ void flush(EpiCtx &ctx) const {
+    const unsigned FULLM = 0xffffffffu;
+    const int lane = threadIdx.x & 31, grp = lane >> 3, sub = lane & 7;
+    __syncwarp();
+    for (int b = 0; b < ctx.nlist; b += 4) {
+      const int idx = b + grp;
+      const bool act = idx < ctx.nlist;
+      const uint32_t e = ctx.list[act ? idx : b];
+      const int64_t i = ctx.rbase + int64_t(e >> 8), j = ctx.col0 + int64_t(e & 255u);
+      const float *pa = pts + i * dim, *pb = pts + j * dim;
+      FloatPairSum acc;
+      float res = 0.f;
+      if (vec4) {
+        const float4 *a4 = reinterpret_cast<const float4 *>(pa);
+        const float4 *b4 = reinterpret_cast<const float4 *>(pb);
+        const int64_t d4 = dim >> 2;
+#pragma unroll 4
+        for (int64_t k = sub; k < d4; k += 8) {
+          const float4 x = a4[k], y = b4[k];
+          sq_add(x.x - y.x, acc, res);
+          sq_add(x.y - y.y, acc, res);
+          sq_add(x.z - y.z, acc, res);
+          sq_add(x.w - y.w, acc, res);
+        }
+      } else {
+        for (int64_t k = sub; k < dim; k += 8) sq_add(pa[k] - pb[k], acc, res);
+      }
+      float hi = acc.hi, lo = acc.lo + res;
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(FULLM, hi, o), ol = __shfl_xor_sync(FULLM, lo, o);
+        const float t = hi + oh, bp = t - hi;
+        lo = (lo + ol) + ((hi - (t - bp)) + (oh - bp));
+        hi = t;
+      }
+      if (act && sub == 0) {
+        const float d = sqrtf(hi + lo);
+        if (layout == GT_LAYOUT_FULL) {
+          out[i * n + j] = d;
+          out[j * n + i] = d;
+        } else {
+          out[dist_index(i, j)] = d;
+        }
+      }
+    }
+    ctx.nlist = 0;
     __syncwarp();
   }
 };
@@ -262,12 +466,23 @@ struct EuclidFinish {
 struct StoreFinish {
   float *out;
   int64_t ld, nr, nc;
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], float *wsm) const {
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
+    float *wsm = ctx.wsm;
 #pragma unroll
     for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
     __syncwarp();
     const int64_t rbase = r - lane, c = c0 + lane;
+    if (rbase + 31 < nr && c0 + 31 < nc) {
+      float *o = out + (rbase * ld + c);
+#pragma unroll 8
+      for (int i = 0; i < 32; i++) {
+        *o = wsm[i * 33 + lane];
+        o += ld;
+      }
+      __syncwarp();
+      return;
+    }
     for (int i = 0; i < 32; i++) {
       const int64_t ri = rbase + i;
       if (ri >= nr) break;
@@ -275,16 +490,29 @@ struct StoreFinish {
     }
     __syncwarp();
   }
+  __device__ void begin_tile(int64_t, EpiCtx &) const {}
+  __device__ void flush(EpiCtx &) const {}
 };
 
 // ----------------------------------------------------------------- kernel
-template <int NSPLIT, int BK>
+// LISTS: the unchunked (Euclidean) kernel, whose epilogue is latency-bound:
+// 16 epilogue warps of 64 columns, each with a pending-pair list and its
+// columns' norms in shared memory.  The chunked kernels keep 8 warps of 128
+// columns (their running sums need the registers) and give the shared
+// memory to the stages.
+template <int KIND, int BK, bool LISTS>
 struct TcCfg {
+  static constexpr int NSPLIT = tc::Kind<KIND>::NSPLIT;
+  static constexpr int EPI = LISTS ? 16 : 8;                 // epilogue warps
+  static constexpr int THREADS = 64 + 32 * EPI;              // + producer and MMA warps
+  static constexpr int COLS = 4 * kBN / EPI;                 // columns per epilogue warp
+  static constexpr int NBLK = COLS / 32;                     // 32 x 32 blocks per warp
   static constexpr int ROW_BYTES = BK * 2;                // 128 or 64
   static constexpr int A_TILE = kBM * BK * 2;
   static constexpr int B_TILE = kBN * BK * 2;
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
-  static constexpr int EPI_BYTES = kEpiWarps * kEpiTileFloats * 4;
+  static constexpr int EPI_FLOATS = kEpiTileFloats + (LISTS ? kEuclidList + 2 * COLS : 0);
+  static constexpr int EPI_BYTES = EPI * EPI_FLOATS * 4;
   static constexpr int STAGES_RAW = (kMaxSmem - 1024 - 256 - EPI_BYTES) / STAGE;
   static constexpr int STAGES = STAGES_RAW > 6 ? 6 : STAGES_RAW;
   static constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/ + EPI_BYTES;
@@ -351,8 +579,8 @@ __device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ pref
 
 // A batch of cor(x) problems: per-problem maps and finishes in device
 // memory; each CTA walks its own host-balanced list of global tile ids.
-struct alignas(64) PearsonBatchProblem {
-  CUtensorMap map;
+struct PearsonBatchProblem {  // aligned as CUtensorMap
+  CUtensorMap map_a, map_b;  // 128-row and 256-row boxes over the same planes
   TileSpace ts;
   int64_t nk;
   PearsonFinish fin;
@@ -370,7 +598,8 @@ struct PearsonBatchWork {
     const int64_t pi = find_segment(tile_prefix, nprob, t);
     const PearsonBatchProblem &pr = probs[pi];
     tile_coords(pr.ts, t - tile_prefix[pi], ref.ti, ref.tj);
-    ref.ma = ref.mb = &pr.map;
+    ref.ma = &pr.map_a;
+    ref.mb = &pr.map_b;
     ref.nk = pr.nk;
     ref.prob = pi;
     return true;
@@ -379,10 +608,12 @@ struct PearsonBatchWork {
   __device__ void prefetch() const {}
 };
 
-template <int NSPLIT, int BK, bool CHUNKED, class Work>
-__global__ void __launch_bounds__(kTcThreads, 1)
+template <int KIND, int BK, bool CHUNKED, class Work>
+__global__ void __launch_bounds__(TcCfg<KIND, BK, !CHUNKED>::THREADS, 1)
 gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
-  using C = TcCfg<NSPLIT, BK>;
+  using C = TcCfg<KIND, BK, !CHUNKED>;
+  constexpr int NSPLIT = C::NSPLIT;
+  static_assert(!CHUNKED || C::COLS == 128, "chunked sums hold 128 columns per warp");
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -403,7 +634,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
     }
     for (int b = 0; b < 2; b++) {
       tc::mbar_init(&accf[b], 1);
-      tc::mbar_init(&acce[b], kEpiWarps);
+      tc::mbar_init(&acce[b], C::EPI);
     }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -453,7 +684,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
   } else if (warp == 1) {
     if (lane == 0) {
       // ------------------------------------------------ MMA issuer
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+      constexpr uint32_t idesc = tc::idesc_f32acc(kBM, kBN, tc::Kind<KIND>::AB_FMT);
       int64_t it = 0, cc = 0;
       bool ok = true;
       TileRef ref;
@@ -505,15 +736,24 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
   } else {
     // ------------------------------------------ epilogue (warps 2..9)
     const int q = warp & 3;            // TMEM lane quarter
-    const int half = (warp - 2) >> 2;  // column half: 0 or 1
-    float *wsm = epi_smem + (warp - 2) * kEpiTileFloats;
+    const int part = (warp - 2) >> 2;  // column part: 0 .. EPI/4 - 1
+    EpiCtx ctx;
+    float *mine = epi_smem + (warp - 2) * C::EPI_FLOATS;
+    ctx.wsm = mine;
+    ctx.list = CHUNKED ? nullptr : reinterpret_cast<uint32_t *>(mine + kEpiTileFloats);
+    ctx.cnrm = CHUNKED ? nullptr : reinterpret_cast<float2 *>(mine + kEpiTileFloats + kEuclidList);
+    ctx.ncols = C::COLS;
+    ctx.nlist = 0;
     int64_t cc = 0;
     bool ok = true;
     TileRef ref;
     for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
       const auto fin = work.finish(ref);
       const int64_t r = ref.ti * kBM + q * 32 + lane;
-      const int64_t col = ref.tj * kBN + half * 128;
+      const int64_t col = ref.tj * kBN + part * C::COLS;
+      ctx.rbase = r - lane;
+      ctx.col0 = col;
+      fin.begin_tile(r, ctx);
       if (CHUNKED) {
         const int64_t nch = (ref.nk + ckb - 1) / ckb;
         float acc[128];
@@ -529,7 +769,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
           }
           tc::tc_fence_after();
           const uint32_t tb =
-              tmem_base + uint32_t(buf * kBN + half * 128) + (uint32_t(q * 32) << 16);
+              tmem_base + uint32_t(buf * kBN + part * C::COLS) + (uint32_t(q * 32) << 16);
 #pragma unroll
           for (int i = 0; i < 8; i++) {
             float g[16];
@@ -547,8 +787,9 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
           float g[32];
 #pragma unroll
           for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
-          fin(r, col + 32 * i, g, wsm);
+          fin(r, col + 32 * i, g, ctx);
         }
+        fin.flush(ctx);
       } else {
         const int buf = int(cc & 1);
         const uint32_t ause = uint32_t(cc >> 1);
@@ -558,17 +799,19 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
           break;
         }
         tc::tc_fence_after();
-        const uint32_t tb = tmem_base + uint32_t(buf * kBN + half * 128) + (uint32_t(q * 32) << 16);
+        const uint32_t tb =
+            tmem_base + uint32_t(buf * kBN + part * C::COLS) + (uint32_t(q * 32) << 16);
 #pragma unroll 1
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < C::NBLK; i++) {
           float g[32];
           tc::tmem_ld32(tb + uint32_t(32 * i), g);
-          fin(r, col + 32 * i, g, wsm);
+          fin(r, col + 32 * i, g, ctx);
         }
         tc::tc_fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&acce[buf]);
         cc++;
+        fin.flush(ctx);
       }
     }
     if (!ok) *abort_flag = 1;
@@ -582,121 +825,195 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
 }
 
 // ----------------------------------------------------------------- operands
-// Pearson operand planes: z = (x - mean) * inv_norm in FP64 (rounded to
-// float), NaN rows for variables that are NaN-flagged or constant; k >= n is
-// zero.  One CTA per variable (no per-element index division).
-template <int NSPLIT>
-__global__ void __launch_bounds__(256)
-pearson_split_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int64_t kpad,
-                     const ColStats *__restrict__ st, __nv_bfloat16 *__restrict__ Z) {
-  const int64_t v = blockIdx.x;
-  const int64_t plane = nvar * kpad;
-  const ColStats s = st[v];
-  const float *x = X + v * n;
-  __nv_bfloat16 *z = Z + v * kpad;
-  for (int64_t k = threadIdx.x; k < kpad; k += blockDim.x) {
-    __nv_bfloat16 p[3];
-    if (k >= n) {
-      p[0] = p[1] = p[2] = __float2bfloat16(0.f);
-    } else if (s.flags) {
-      p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
-    } else {
-      tc::split_bf16<NSPLIT>(float((double(x[k]) - s.mean) * s.inv_norm), p);
+// Split planes of one row (a variable or a point): parts of val(k) for
+// k < n, zeros for n <= k < kpad; four consecutive k per lane, stored as one
+// 8-byte word per plane.  `plane` is the element stride between part planes.
+template <int KIND, class Val>
+__device__ __forceinline__ void write_row_planes(int64_t n, int64_t kpad, int64_t plane,
+                                                 uint16_t *__restrict__ z, Val &&val) {
+  constexpr int NS = tc::Kind<KIND>::NSPLIT;
+  const int lane = threadIdx.x & 31;
+  for (int64_t k0 = 4 * int64_t(lane); k0 < kpad; k0 += 128) {
+    uint32_t w[3][2];
+#pragma unroll
+    for (int q = 0; q < 3; q++) w[q][0] = w[q][1] = 0u;
+    if (k0 < n) {
+      float v[4];
+      val(k0, v);
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        uint16_t p[3];
+        tc::split_parts<KIND>(v[e], p);
+        if (k0 + e >= n) p[0] = p[1] = p[2] = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) w[q][e >> 1] |= uint32_t(p[q]) << (16 * (e & 1));
+      }
     }
 #pragma unroll
-    for (int q = 0; q < NSPLIT; q++) z[q * plane + k] = p[q];
+    for (int q = 0; q < NS; q++)
+      *reinterpret_cast<uint2 *>(z + q * plane + k0) = make_uint2(w[q][0], w[q][1]);
   }
 }
 
-// Column sums of the points (FP64), accumulated into sums[] (zeroed first).
-__global__ void euclid_colsum_kernel(const float *__restrict__ P, int64_t n, int64_t dim,
-                                     int64_t per_block, double *__restrict__ sums) {
-  const int64_t d = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (d >= dim) return;
-  const int64_t i0 = blockIdx.y * per_block;
-  const int64_t i1 = min(n, i0 + per_block);
-  double acc = 0.0;
-  for (int64_t i = i0; i < i1; i++) acc += double(P[i * dim + d]);
-  atomicAdd(&sums[d], acc);
+// Pearson planes of variable x (length n) with statistics s: z = (x - mean) *
+// inv_norm (times 2^14 for f16x3), NaN for every k < n of a NaN-flagged or
+// constant variable.
+template <int KIND>
+__device__ __forceinline__ void pearson_row(const float *__restrict__ x, int64_t n, int64_t kpad,
+                                            int64_t plane, const ColStats &s,
+                                            uint16_t *__restrict__ z) {
+  const Centerer cen(s);
+  const float scale = tc::Kind<KIND>::F16 ? 16384.f : 1.f;
+  const bool nanrow = s.flags != 0;
+  const bool vec = (reinterpret_cast<uintptr_t>(x) & 15u) == 0 && (n & 3) == 0;
+  write_row_planes<KIND>(n, kpad, plane, z, [&](int64_t k0, float (&v)[4]) {
+    if (vec) {
+      const float4 t = *reinterpret_cast<const float4 *>(x + k0);
+      v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; e++) v[e] = (k0 + e < n) ? x[k0 + e] : 0.f;
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) v[e] = nanrow ? __int_as_float(0x7fc00000) : cen(v[e]) * scale;
+  });
 }
 
-// Euclidean operand planes of the centred points and their squared norms
-// (FP64, stored rounded to float), one warp per point.
-template <int NSPLIT>
-__global__ void euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t dim,
-                                    int64_t kpad, const double *__restrict__ sums,
-                                    __nv_bfloat16 *__restrict__ Z, float *__restrict__ norm2) {
+// Pearson prologue, fused: one warp per variable computes the statistics and
+// writes the operand planes (and the statistics, when st is not null).
+template <int KIND>
+__global__ void __launch_bounds__(256)
+pearson_prep_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int64_t kpad,
+                    uint16_t *__restrict__ Z, ColStats *__restrict__ st) {
+  const int64_t v = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
+  if (v >= nvar) return;  // whole warps
+  const float *x = X + v * n;
+  const ColStats s = colstats_warp(x, n, GT_EVERYTHING);
+  if (st && (threadIdx.x & 31) == 0) st[v] = s;
+  pearson_row<KIND>(x, n, kpad, nvar * kpad, s, Z + v * kpad);
+}
+
+// Column sums of the points: block (x, y) sums dimensions 32x .. 32x+31 over
+// points 64y .. 64y+63 (8 rows of 32 lanes, compensated float sums, combined
+// in a fixed order), one partial per (point block, dimension).
+constexpr int kColsumPoints = 64;
+__global__ void __launch_bounds__(256)
+euclid_colsum_kernel(const float *__restrict__ P, int64_t n, int64_t dim,
+                     double *__restrict__ partial) {
+  __shared__ float2 sh[8][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t d = int64_t(blockIdx.x) * 32 + tx;
+  const int64_t i0 = int64_t(blockIdx.y) * kColsumPoints;
+  FloatPairSum acc;
+  if (d < dim) {
+#pragma unroll 8
+    for (int i = ty; i < kColsumPoints; i += 8)
+      if (i0 + i < n) acc.add(P[(i0 + i) * dim + d]);
+  }
+  sh[ty][tx] = make_float2(acc.hi, acc.lo);
+  __syncthreads();
+  if (ty == 0 && d < dim) {
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < 8; r++) s += double(sh[r][tx].x) + double(sh[r][tx].y);
+    partial[blockIdx.y * dim + d] = s;
+  }
+}
+
+// Column means as float pairs (hi, lo): one CTA per dimension sums that
+// dimension's partials (strided per thread, then a fixed tree), so the
+// result does not depend on scheduling.
+__global__ void __launch_bounds__(256)
+euclid_mean_kernel(const double *__restrict__ partial, int64_t nblk, int64_t dim, int64_t n,
+                   float2 *__restrict__ mean2) {
+  __shared__ double sh[256];
+  const int64_t d = blockIdx.x;
+  double s = 0.0;
+  for (int64_t b = threadIdx.x; b < nblk; b += 256) s += partial[b * dim + d];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (int(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double m = sh[0] / double(n);
+    const float hi = float(m);
+    mean2[d] = make_float2(hi, float(m - double(hi)));
+  }
+}
+
+// Euclidean operand planes of the centred points, one warp per point: the
+// squared norm (compensated), the largest magnitude (f16x3 scale), then the
+// planes.  nrm[v] = {|c|^2, 2^-s}; rows n .. npad-1 of nrm are zeroed.
+template <int KIND>
+__global__ void __launch_bounds__(256)
+euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_t dim,
+                    int64_t kpad, const float2 *__restrict__ mean2, uint16_t *__restrict__ Z,
+                    float2 *__restrict__ nrm) {
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
   const int64_t plane = n * kpad;
-  const double inv_n = 1.0 / double(n);
-  for (int64_t v = warp; v < n; v += nwarps) {
-    double acc = 0.0;
-    for (int64_t k = lane; k < kpad; k += 32) {
-      __nv_bfloat16 p[3];
-      if (k < dim) {
-        const double x = double(P[v * dim + k]) - sums[k] * inv_n;
-        acc = fma(x, x, acc);
-        tc::split_bf16<NSPLIT>(float(x), p);
-      } else {
-        p[0] = p[1] = p[2] = __float2bfloat16(0.f);
-      }
-#pragma unroll
-      for (int q = 0; q < NSPLIT; q++) Z[q * plane + v * kpad + k] = p[q];
+  for (int64_t v = warp; v < npad; v += nwarps) {
+    if (v >= n) {
+      if (lane == 0) nrm[v] = make_float2(0.f, 0.f);
+      continue;
     }
+    const float *x = P + v * dim;
+    FloatPairSum acc;
+    float res = 0.f, amax = 0.f;
+    for (int64_t k = lane; k < dim; k += 32) {
+      const float2 m = mean2[k];
+      const float c = (x[k] - m.x) - m.y;
+      const float q = c * c;
+      res += fmaf(c, c, -q);
+      acc.add(q);
+      amax = fmaxf(amax, fabsf(c));
+    }
+    float hi = acc.hi, lo = acc.lo + res;
+    warp_pair_sum(hi, lo);
+    amax = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(amax)));
+    const int se = tc::Kind<KIND>::F16 ? tc::f16_scale_exp(amax) : 0;
+    const float scale = tc::exp2i(se);
+    if (lane == 0) nrm[v] = make_float2(hi + lo, tc::exp2i(-se));
+    write_row_planes<KIND>(dim, kpad, plane, Z + v * kpad, [&](int64_t k0, float (&c)[4]) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) norm2[v] = float(acc);
+      for (int e = 0; e < 4; e++) {
+        const int64_t k = k0 + e;
+        if (k < dim) {
+          const float2 m = mean2[k];
+          c[e] = ((x[k] - m.x) - m.y) * scale;
+        } else {
+          c[e] = 0.f;
+        }
+      }
+    });
   }
 }
 
-// Batched Pearson prologue: the variables of every problem, one CTA each.
+// Batched Pearson prologue: the variables of every problem, one warp each.
 struct PearsonBatchInput {
   const float *X;
   int64_t p, n, kpad;
   int64_t plane_off;  // element offset of this problem's planes (NSPLIT x p x kpad)
-  int64_t var_off;    // offset of its variables in the statistics array
+  int64_t var_off;    // offset of its variables in the global variable index
 };
 
-__global__ void __launch_bounds__(kColStatThreads)
-pearson_batch_stats_kernel(const PearsonBatchInput *__restrict__ in,
-                           const int64_t *__restrict__ var_prefix, int64_t nprob,
-                           ColStats *__restrict__ st) {
-  __shared__ double sh[32];
-  const int64_t gv = blockIdx.x;
-  const int64_t pi = find_segment(var_prefix, nprob, gv);
-  const PearsonBatchInput b = in[pi];
-  const int64_t v = gv - var_prefix[pi];
-  const ColStats c = colstats_block(b.X + v * b.n, b.n, GT_EVERYTHING, sh);
-  if (threadIdx.x == 0) st[gv] = c;
-}
-
-template <int NSPLIT>
+template <int KIND>
 __global__ void __launch_bounds__(256)
-pearson_batch_split_kernel(const PearsonBatchInput *__restrict__ in,
-                           const int64_t *__restrict__ var_prefix, int64_t nprob,
-                           const ColStats *__restrict__ st, __nv_bfloat16 *__restrict__ planes) {
-  const int64_t gv = blockIdx.x;
+pearson_batch_prep_kernel(const PearsonBatchInput *__restrict__ in,
+                          const int64_t *__restrict__ var_prefix, int64_t nprob,
+                          int64_t total_vars, uint16_t *__restrict__ planes) {
+  const int64_t gv = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
+  if (gv >= total_vars) return;  // whole warps
   const int64_t pi = find_segment(var_prefix, nprob, gv);
   const PearsonBatchInput b = in[pi];
   const int64_t v = gv - var_prefix[pi];
-  const ColStats s = st[gv];
-  const int64_t plane = b.p * b.kpad;
   const float *x = b.X + v * b.n;
-  __nv_bfloat16 *z = planes + b.plane_off + v * b.kpad;
-  for (int64_t k = threadIdx.x; k < b.kpad; k += blockDim.x) {
-    __nv_bfloat16 p[3];
-    if (k >= b.n) {
-      p[0] = p[1] = p[2] = __float2bfloat16(0.f);
-    } else if (s.flags) {
-      p[0] = p[1] = p[2] = __float2bfloat16(__int_as_float(0x7fc00000));
-    } else {
-      tc::split_bf16<NSPLIT>(float((double(x[k]) - s.mean) * s.inv_norm), p);
-    }
-#pragma unroll
-    for (int q = 0; q < NSPLIT; q++) z[q * plane + k] = p[q];
-  }
+  const ColStats s = colstats_warp(x, b.n, GT_EVERYTHING);
+  pearson_row<KIND>(x, b.n, b.kpad, b.p * b.kpad, s, planes + b.plane_off + v * b.kpad);
 }
 
 // ----------------------------------------------------------------- host side
@@ -714,17 +1031,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D map over planes [nsplit][rows][kpad] of bf16; box {bk, box_rows, 1}.
+// 3-D map over planes [nsplit][rows][kpad] of 16-bit parts; box {bk, box_rows, 1}.
 int make_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad, int nsplit,
-                   int box_rows, int bk) {
+                   int box_rows, int bk, bool f16) {
   auto fn = encode_fn();
   if (!fn) return fail(GT_ECUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[3] = {cuuint64_t(kpad), cuuint64_t(rows), cuuint64_t(nsplit)};
   cuuint64_t strides[2] = {cuuint64_t(kpad * 2), cuuint64_t(rows * kpad * 2)};
   cuuint32_t box[3] = {cuuint32_t(bk), cuuint32_t(box_rows), 1u};
   cuuint32_t estr[3] = {1u, 1u, 1u};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  CUresult r = fn(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+                  const_cast<void *>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
                   bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(GT_ECUDA, "cuTensorMapEncodeTiled failed (%d)", int(r));
@@ -740,29 +1058,32 @@ int err_word(int **p) {
   return GT_OK;
 }
 
-template <int NSPLIT, int BK, bool CHUNKED, class Fin>
+template <int KIND, int BK, bool CHUNKED, class Fin>
 int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
                 bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
                 cudaStream_t s) {
-  using C = TcCfg<NSPLIT, BK>;
+  using C = TcCfg<KIND, BK, !CHUNKED>;
   using W = SingleWork<Fin>;
+  constexpr bool F16 = tc::Kind<KIND>::F16;
   if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
   if (ckb < 1) ckb = 1;
   W w;
-  GT_TRY(make_plane_map(&w.ma, zA, nA, kpad, NSPLIT, kBM, BK));
-  GT_TRY(make_plane_map(&w.mb, zB, nB, kpad, NSPLIT, kBN, BK));
-  w.ts = make_tiles(nA, nB, symmetric);
+  GT_TRY(make_plane_map(&w.ma, zA, nA, kpad, C::NSPLIT, kBM, BK, F16));
+  GT_TRY(make_plane_map(&w.mb, zB, nB, kpad, C::NSPLIT, kBN, BK, F16));
+  w.ts = make_tiles(nA, nB, symmetric, band_group(int64_t(kBN) * kpad * 2 * C::NSPLIT));
+  if (w.ts.ntiles > 2147483647LL) return fail(GT_EINVAL, "problem too large (%lld tiles)",
+                                             (long long)w.ts.ntiles);
   w.nk = kpad / BK;
   w.fin = fin;
   if (w.ts.ntiles == 0) return GT_OK;
   int *err = nullptr;
   GT_TRY(err_word(&err));
   GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  auto kern = gram_tc_kernel<NSPLIT, BK, CHUNKED, W>;
+  auto kern = gram_tc_kernel<KIND, BK, CHUNKED, W>;
   GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
   const int64_t grid = w.ts.ntiles < sm_count() ? w.ts.ntiles : sm_count();
   ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+  kern<<<unsigned(grid), C::THREADS, C::SMEM, s>>>(w, ckb, err);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
@@ -772,7 +1093,7 @@ int tc_config() {
   static int cfg = -1;
   if (cfg < 0) {
     const char *e = std::getenv("GT_TC_BK");
-    cfg = (e && std::atoi(e) == 32) ? 32 : 64;
+    cfg = (e && std::atoi(e) == 64) ? 64 : 32;
   }
   return cfg;
 }
@@ -789,6 +1110,14 @@ int64_t tc_chunk_kblocks(int bk) {
   return elems / bk > 0 ? elems / bk : 1;
 }
 
+int check_kind(int kind) {
+  if (kind != tc::KIND_BF16X3 && kind != tc::KIND_BF16X6 && kind != tc::KIND_F16X3)
+    return fail(GT_EINVAL, "not a tensor-core split (%d)", kind);
+  return GT_OK;
+}
+
+int kind_nsplit(int kind) { return kind == tc::KIND_BF16X6 ? 3 : 2; }
+
 }  // namespace
 
 // C[r][c] = sum_k A_r[k] B_c[k] over split-bf16 planes ([part][row][kpad]),
@@ -798,10 +1127,10 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
   if (nA == 0 || nB == 0) return GT_OK;
   StoreFinish fin{C, ldc, nA, nB};
   if (nsplit == 3)
-    return launch_gram<3, 32, true>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(32),
-                                    fin, "gemm_store", s);
-  return launch_gram<2, 64, true>(planesA, nA, planesB, nB, kpad, false, tc_chunk_kblocks(64),
-                                  fin, "gemm_store", s);
+    return launch_gram<tc::KIND_BF16X6, 32, true>(planesA, nA, planesB, nB, kpad, false,
+                                                  tc_chunk_kblocks(32), fin, "gemm_store", s);
+  return launch_gram<tc::KIND_BF16X3, 64, true>(planesA, nA, planesB, nB, kpad, false,
+                                                tc_chunk_kblocks(64), fin, "gemm_store", s);
 }
 
 int tc_check_error(cudaStream_t s, bool *failed) {
@@ -815,83 +1144,117 @@ int tc_check_error(cudaStream_t s, bool *failed) {
   return GT_OK;
 }
 
-int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int nsplit, int slot_z,
+int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int kind, int slot_z,
                         int slot_st, void **Z, int64_t *kpad, cudaStream_t s) {
+  GT_TRY(check_kind(kind));
   *kpad = cdiv(n, kKPad) * kKPad;
   void *pz = nullptr, *pst = nullptr;
-  GT_TRY(ws_get(slot_z, size_t(nsplit) * size_t(nvar) * size_t(*kpad) * 2, &pz));
+  GT_TRY(ws_get(slot_z, size_t(kind_nsplit(kind)) * size_t(nvar) * size_t(*kpad) * 2, &pz));
   GT_TRY(ws_get(slot_st, size_t(nvar) * sizeof(ColStats), &pst));
-  ColStats *st = static_cast<ColStats *>(pst);
+  auto *st = static_cast<ColStats *>(pst);
+  auto *z = static_cast<uint16_t *>(pz);
+  const int64_t blocks = cdiv(nvar, 8);
+  if (blocks > 2147483647LL) return fail(GT_EINVAL, "too many variables");
   ProfScope prof("pearson_prologue", s);
-  GT_TRY(launch_colstats(dX, nvar, n, GT_EVERYTHING, st, s));
-  auto *z = static_cast<__nv_bfloat16 *>(pz);
-  if (nvar > 2147483647LL) return fail(GT_EINVAL, "too many variables");
-  if (nsplit == 3)
-    pearson_split_kernel<3><<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
+  if (kind == tc::KIND_BF16X6)
+    pearson_prep_kernel<tc::KIND_BF16X6><<<unsigned(blocks), 256, 0, s>>>(dX, nvar, n, *kpad, z, st);
+  else if (kind == tc::KIND_F16X3)
+    pearson_prep_kernel<tc::KIND_F16X3><<<unsigned(blocks), 256, 0, s>>>(dX, nvar, n, *kpad, z, st);
   else
-    pearson_split_kernel<2><<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, *kpad, st, z);
+    pearson_prep_kernel<tc::KIND_BF16X3><<<unsigned(blocks), 256, 0, s>>>(dX, nvar, n, *kpad, z, st);
   count_launch();
   GT_CUDA(cudaGetLastError());
   *Z = pz;
   return GT_OK;
 }
 
-int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int nsplit,
+int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int kind,
                const PearsonOut &out, cudaStream_t s) {
+  GT_TRY(check_kind(kind));
   if (nA == 0 || nB == 0) return GT_OK;
   if (!out.corr && !out.ts && !out.pairs) return GT_OK;
+  const float gscale = kind == tc::KIND_F16X3 ? 1.f / 268435456.f : 1.f;  // 2^-28
   PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
-                    std::sqrt(out.npairs - 2.f), out.symmetric};
+                    std::sqrt(out.npairs - 2.f), gscale, out.symmetric};
   const bool sym = out.symmetric != 0;
-  if (nsplit == 3)
-    return launch_gram<3, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
-                                    "pearson_gram", s);
+  if (kind == tc::KIND_BF16X6)
+    return launch_gram<tc::KIND_BF16X6, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32),
+                                                  fin, "pearson_gram", s);
+  if (kind == tc::KIND_F16X3) {
+    if (tc_config() == 32)
+      return launch_gram<tc::KIND_F16X3, 32, true>(zA, nA, zB, nB, kpad, sym,
+                                                   tc_chunk_kblocks(32), fin, "pearson_gram", s);
+    return launch_gram<tc::KIND_F16X3, 64, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64),
+                                                 fin, "pearson_gram", s);
+  }
   if (tc_config() == 32)
-    return launch_gram<2, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32), fin,
-                                    "pearson_gram", s);
-  return launch_gram<2, 64, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64), fin,
-                                  "pearson_gram", s);
+    return launch_gram<tc::KIND_BF16X3, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32),
+                                                  fin, "pearson_gram", s);
+  return launch_gram<tc::KIND_BF16X3, 64, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(64),
+                                                fin, "pearson_gram", s);
 }
+
+namespace {
+
+template <int KIND>
+int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
+                   float tau, cudaStream_t st) {
+  constexpr int NS = tc::Kind<KIND>::NSPLIT;
+  const int64_t kpad = cdiv(dim, kKPad) * kKPad;
+  const int64_t npad = cdiv(n, kBN) * kBN;
+  const int64_t nblk = cdiv(n, kColsumPoints);
+  void *pz = nullptr, *pn = nullptr, *pp = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n) * size_t(kpad) * 2, &pz));
+  GT_TRY(ws_get(WS_SCRATCH2, size_t(npad) * sizeof(float2), &pn));
+  GT_TRY(ws_get(WS_SCRATCH3, size_t(nblk) * size_t(dim) * 8 + size_t(dim) * sizeof(float2), &pp));
+  auto *z = static_cast<uint16_t *>(pz);
+  auto *nrm = static_cast<float2 *>(pn);
+  auto *partial = static_cast<double *>(pp);
+  auto *mean2 = reinterpret_cast<float2 *>(partial + nblk * dim);
+  {
+    ProfScope prof("euclid_prologue", st);
+    if (nblk > 65535) return fail(GT_EINVAL, "too many points (%lld)", (long long)n);
+    dim3 cg((unsigned)cdiv(dim, 32), (unsigned)nblk, 1u);
+    euclid_colsum_kernel<<<cg, 256, 0, st>>>(d_pts, n, dim, partial);
+    euclid_mean_kernel<<<unsigned(dim), 256, 0, st>>>(partial, nblk, dim, n, mean2);
+    int64_t g = cdiv(npad * 32, 256);
+    if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
+    euclid_split_kernel<KIND><<<unsigned(g), 256, 0, st>>>(d_pts, n, npad, dim, kpad, mean2, z,
+                                                           nrm);
+    count_launch(3);
+    GT_CUDA(cudaGetLastError());
+  }
+  const int vec4 = (reinterpret_cast<uintptr_t>(d_pts) & 15u) == 0 && (dim & 3) == 0;
+  EuclidFinish fin{nrm, d_pts, d_out, n, dim, layout, tau, vec4};
+  return launch_gram<KIND, 32, false>(z, n, z, n, kpad, true, 0, fin, "euclid_gram", st);
+}
+
+}  // namespace
 
 int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
               cudaStream_t st) {
   if (dim == 0 || n < 2) return dist_simt(d_pts, n, dim, d_out, layout, GT_EUCLIDEAN, 2.f, st);
-  // Output writes bound this kernel at moderate dim, so the float32-level
-  // 3-way split costs nothing over the 2-way one: always use it.
-  constexpr int NS = 3;
-  const int64_t kpad = cdiv(dim, kKPad) * kKPad;
-  void *pz = nullptr, *pn = nullptr, *psum = nullptr;
-  GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n) * size_t(kpad) * 2, &pz));
-  GT_TRY(ws_get(WS_SCRATCH2, size_t(n) * 4, &pn));
-  GT_TRY(ws_get(WS_SCRATCH3, size_t(dim) * 8, &psum));
-  auto *z = static_cast<__nv_bfloat16 *>(pz);
-  auto *norm2 = static_cast<float *>(pn);
-  auto *sums = static_cast<double *>(psum);
-  {
-    ProfScope prof("euclid_prologue", st);
-    GT_CUDA(cudaMemsetAsync(sums, 0, size_t(dim) * 8, st));
-    const int64_t per_block = 2048;
-    dim3 cg((unsigned)cdiv(dim, 128), (unsigned)cdiv(n, per_block), 1u);
-    euclid_colsum_kernel<<<cg, 128, 0, st>>>(d_pts, n, dim, per_block, sums);
-    count_launch();
-    int64_t g = cdiv(n * 32, 256);
-    if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
-    euclid_split_kernel<NS><<<unsigned(g), 256, 0, st>>>(d_pts, n, dim, kpad, sums, z, norm2);
-    count_launch();
-    GT_CUDA(cudaGetLastError());
-  }
-  // Entries with d^2 below an eighth of |a|^2 + |b|^2 are recomputed exactly.
-  EuclidFinish fin{norm2, d_pts, d_out, n, dim, layout, 0.125f};
-  return launch_gram<NS, 32, false>(z, n, z, n, kpad, true, 0, fin, "euclid_gram", st);
+  // The 3-product split of bf16 loses too much for distances, so the bf16
+  // paths use bf16x6.  Entries with d^2 below tau (|a|^2 + |b|^2) are
+  // recomputed exactly: tau = 1/8 for bf16x6 (float32-level products), 1/4
+  // for f16x3 (~2^-21 products).
+  if (gt_get_gram_path() == GT_GRAM_TC_F16X3)
+    return euclid_tc_kind<tc::KIND_F16X3>(d_pts, n, dim, d_out, layout, 0.25f, st);
+  return euclid_tc_kind<tc::KIND_BF16X6>(d_pts, n, dim, d_out, layout, 0.125f, st);
 }
 
 // Batched cor(x): builds device descriptors (through `alloc`, which the plan
 // owns), balances the tiles over one CTA per SM, and returns the runner that
 // launches prologue + Gram for the whole batch.
-int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit, int bk,
+int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, int bk,
                           int64_t chunk_elems, const std::function<int(size_t, void **)> &alloc,
                           std::function<int(cudaStream_t)> *run, int64_t *ntiles_out,
-                          int64_t *nctas_out) {
+                          int64_t *nctas_out, int **err_out) {
+  GT_TRY(check_kind(kind));
+  if (bk != 32 && bk != 64) return fail(GT_EINVAL, "bad k-block (%d)", bk);
+  if (kind == tc::KIND_BF16X6) bk = 32;
+  const int nsplit = kind_nsplit(kind);
+  const bool f16 = kind == tc::KIND_F16X3;
   std::vector<PearsonBatchInput> inputs;
   std::vector<PearsonBatchProblem> descs;
   std::vector<int64_t> var_prefix{0}, tile_prefix{0}, cost;
@@ -916,12 +1279,12 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit
     var_prefix.push_back(vars);
   }
   const int64_t nprob = int64_t(inputs.size());
-  void *d_planes = nullptr, *d_st = nullptr, *d_in = nullptr, *d_vp = nullptr;
+  void *d_planes = nullptr, *d_in = nullptr, *d_vp = nullptr;
   GT_TRY(alloc(size_t(plane_elems) * 2, &d_planes));
-  GT_TRY(alloc(size_t(vars) * sizeof(ColStats), &d_st));
-  auto *planes = static_cast<__nv_bfloat16 *>(d_planes);
+  auto *planes = static_cast<uint16_t *>(d_planes);
   int64_t ckb = chunk_elems / bk;
   if (ckb < 1) ckb = 1;
+  const float gscale = f16 ? 1.f / 268435456.f : 1.f;
   // second pass: tensor maps, tiles, finishes
   int64_t pidx = 0;
   for (int64_t i = 0; i < count; i++) {
@@ -930,11 +1293,12 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit
     const PearsonBatchInput &b = inputs[pidx++];
     PearsonBatchProblem d;
     std::memset(&d, 0, sizeof(d));
-    GT_TRY(make_plane_map(&d.map, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk));
-    d.ts = make_tiles(b.p, b.p, true);
+    GT_TRY(make_plane_map(&d.map_a, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk, f16));
+    GT_TRY(make_plane_map(&d.map_b, planes + b.plane_off, b.p, b.kpad, nsplit, kBN, bk, f16));
+    d.ts = make_tiles(b.p, b.p, true, 1);
     d.nk = b.kpad / bk;
     d.fin = PearsonFinish{q.corr, q.ts, q.pairs, b.p, b.p, b.p, float(b.n),
-                          std::sqrt(float(b.n) - 2.f), 1};
+                          std::sqrt(float(b.n) - 2.f), gscale, 1};
     descs.push_back(d);
     tile_prefix.push_back(tile_prefix.back() + d.ts.ntiles);
     const int64_t nch = (d.nk + ckb - 1) / ckb;
@@ -950,7 +1314,6 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit
     for (int64_t t = 0; t < ntiles; t++) order[t] = t;
     std::stable_sort(order.begin(), order.end(),
                      [&](int64_t a, int64_t c) { return cost[a] > cost[c]; });
-    std::vector<int64_t> load(ncta, 0);
     std::vector<std::vector<int64_t>> lists(ncta);
     using Item = std::pair<int64_t, int64_t>;
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
@@ -990,39 +1353,50 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit
   w.cta_off = static_cast<const int64_t *>(d_co);
   auto *in = static_cast<const PearsonBatchInput *>(d_in);
   auto *vp = static_cast<const int64_t *>(d_vp);
-  auto *st = static_cast<ColStats *>(d_st);
   auto *err = static_cast<int *>(d_err);
+  *err_out = err;
   const int64_t total_vars = vars;
-  const int ns = nsplit;
   const int BKc = bk;
   *ntiles_out = ntiles;
   *nctas_out = ncta;
   *run = [=](cudaStream_t s) -> int {
     GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     if (total_vars == 0) return GT_OK;
-    if (total_vars > 2147483647LL) return fail(GT_EINVAL, "too many variables in the batch");
-    pearson_batch_stats_kernel<<<unsigned(total_vars), kColStatThreads, 0, s>>>(in, vp, nprob, st);
-    if (ns == 3)
-      pearson_batch_split_kernel<3><<<unsigned(total_vars), 256, 0, s>>>(in, vp, nprob, st, planes);
+    const int64_t blocks = cdiv(total_vars, 8);
+    if (blocks > 2147483647LL) return fail(GT_EINVAL, "too many variables in the batch");
+    if (kind == tc::KIND_BF16X6)
+      pearson_batch_prep_kernel<tc::KIND_BF16X6>
+          <<<unsigned(blocks), 256, 0, s>>>(in, vp, nprob, total_vars, planes);
+    else if (kind == tc::KIND_F16X3)
+      pearson_batch_prep_kernel<tc::KIND_F16X3>
+          <<<unsigned(blocks), 256, 0, s>>>(in, vp, nprob, total_vars, planes);
     else
-      pearson_batch_split_kernel<2><<<unsigned(total_vars), 256, 0, s>>>(in, vp, nprob, st, planes);
-    count_launch(2);
+      pearson_batch_prep_kernel<tc::KIND_BF16X3>
+          <<<unsigned(blocks), 256, 0, s>>>(in, vp, nprob, total_vars, planes);
+    count_launch();
     if (ncta == 0) return GT_OK;
-    if (ns == 3) {
-      using C = TcCfg<3, 32>;
-      auto k = gram_tc_kernel<3, 32, true, PearsonBatchWork>;
-      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
-    } else if (BKc == 32) {
-      using C = TcCfg<2, 32>;
-      auto k = gram_tc_kernel<2, 32, true, PearsonBatchWork>;
-      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+    auto launch = [&](auto kern, int smem) -> int {
+      GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      kern<<<unsigned(ncta), TcCfg<tc::KIND_BF16X3, 32, false>::THREADS, smem, s>>>(w, ckb, err);
+      return GT_OK;
+    };
+    if (kind == tc::KIND_BF16X6) {
+      GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X6, 32, true, PearsonBatchWork>,
+                    TcCfg<tc::KIND_BF16X6, 32, false>::SMEM));
+    } else if (kind == tc::KIND_F16X3) {
+      if (BKc == 32)
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 32, true, PearsonBatchWork>,
+                      TcCfg<tc::KIND_F16X3, 32, false>::SMEM));
+      else
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 64, true, PearsonBatchWork>,
+                      TcCfg<tc::KIND_F16X3, 64, false>::SMEM));
     } else {
-      using C = TcCfg<2, 64>;
-      auto k = gram_tc_kernel<2, 64, true, PearsonBatchWork>;
-      GT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-      k<<<unsigned(ncta), kTcThreads, C::SMEM, s>>>(w, ckb, err);
+      if (BKc == 32)
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 32, true, PearsonBatchWork>,
+                      TcCfg<tc::KIND_BF16X3, 32, false>::SMEM));
+      else
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 64, true, PearsonBatchWork>,
+                      TcCfg<tc::KIND_BF16X3, 64, false>::SMEM));
     }
     count_launch();
     GT_CUDA(cudaGetLastError());

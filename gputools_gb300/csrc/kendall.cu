@@ -407,10 +407,12 @@ extern "C" int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny
       GT_TRY(gt::same_contents(static_cast<float *>(dX), static_cast<float *>(dY), nx * n, &same, s));
   }
   if (same) dY = dX;
-  GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(nx) * size_t(ny) * 8, &dO));
+  void *direct = gt::host_direct_ptr(out);
+  if (!(dO = direct)) GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(nx) * size_t(ny) * 8, &dO));
   GT_TRY(gt::kendall_impl(static_cast<float *>(dX), nx, static_cast<float *>(dY), ny, n,
                           same ? 1 : 0, static_cast<double *>(dO), s));
-  GT_CUDA(cudaMemcpyAsync(out, dO, size_t(nx) * size_t(ny) * 8, cudaMemcpyDeviceToHost, s));
+  if (!direct)
+    GT_CUDA(cudaMemcpyAsync(out, dO, size_t(nx) * size_t(ny) * 8, cudaMemcpyDeviceToHost, s));
   GT_CUDA(cudaStreamSynchronize(s));
   return GT_OK;
 }

@@ -15,12 +15,13 @@ int dist_check_args(int64_t n, int64_t dim, int method, int layout);
 int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout, int method,
               float p, cudaStream_t st);
 
-// euclid_tc.cu: Euclidean distances as a split-bf16 tcgen05 Gram contraction
-// with FP64 norms and an FP64 recomputation of near-zero distances.
+// gram_tc.cu: Euclidean distances as a split tcgen05 Gram contraction (f16x3
+// when the Gram path is f16x3, else bf16x6) with compensated norms and an
+// exact recomputation of near-zero distances.
 int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
               cudaStream_t st);
 
-// Per-variable statistics of the Pearson prologue (FP64).
+// Per-variable statistics of the Pearson prologue.
 struct ColStats {
   double mean;
   double inv_norm;  // 1 / sqrt(sum (x - mean)^2), or 0 for a constant variable
@@ -43,13 +44,14 @@ struct PearsonOut {
   int symmetric;
 };
 
-// Operands for the tensor-core path: for each variable, `nsplit` bf16 rows
-// (hi, lo[, lo2]) of length kpad (multiple of 64), zero padded.
+// Operands for the tensor-core path: for each variable, the 16-bit parts of
+// split `kind` (enum gt_gram_path, not GT_GRAM_FP32) in planes of length kpad
+// (multiple of 64), zero padded.
 int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64_t kpad,
-               int nsplit, const PearsonOut &out, cudaStream_t st);
+               int kind, const PearsonOut &out, cudaStream_t st);
 
-// C[r][c] = sum_k A_r[k] B_c[k] on tcgen05 from split-bf16 planes
-// ([part][row][kpad], kpad a multiple of 64), stored as row-major float.
+// C[r][c] = sum_k A_r[k] B_c[k] on tcgen05 from `nsplit` (2 or 3) split-bf16
+// planes ([part][row][kpad], kpad a multiple of 64), stored as row-major float.
 int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,
                   int nsplit, float *C, int64_t ldc, cudaStream_t s);
 
@@ -67,9 +69,9 @@ int kendall_batch_launch(const KendallBatchProblem *d_probs, const int64_t *d_va
                          uint2 *d_masks, unsigned long long *d_T, cudaStream_t s);
 
 // gram_tc.cu: batched cor(x) on tcgen05 (see pearson_batch_prepare).
-int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int nsplit, int bk,
+int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, int bk,
                           int64_t chunk_elems, const std::function<int(size_t, void **)> &alloc,
                           std::function<int(cudaStream_t)> *run, int64_t *ntiles_out,
-                          int64_t *nctas_out);
+                          int64_t *nctas_out, int **err_out);
 
 }  // namespace gt

@@ -19,7 +19,7 @@ extern "C" void Rf_error(const char *fmt, ...) __attribute__((weak));
 namespace gt {
 namespace {
 
-std::atomic<int> g_gram_path{GT_GRAM_TC_BF16X3};
+std::atomic<int> g_gram_path{GT_GRAM_TC_F16X3};
 
 // src/rinterface.cpp:147-156 getDistEnum: exact names, anything else is
 // euclidean.
@@ -47,7 +47,8 @@ extern "C" {
 
 int gt_set_gram_path(int path) {
   gt::clear_error();
-  if (path != GT_GRAM_TC_BF16X3 && path != GT_GRAM_TC_BF16X6 && path != GT_GRAM_FP32)
+  if (path != GT_GRAM_TC_BF16X3 && path != GT_GRAM_TC_BF16X6 && path != GT_GRAM_FP32 &&
+      path != GT_GRAM_TC_F16X3)
     return gt::fail(GT_EINVAL, "unknown gram path %d", path);
   gt::g_gram_path.store(path);
   return GT_OK;

@@ -8,6 +8,7 @@
 #include "common.cuh"
 
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -108,6 +109,21 @@ cudaStream_t lib_stream() {
   DeviceState &d = g_dev[dev];
   if (!d.stream) cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking);
   return d.stream;
+}
+
+void *host_direct_ptr(void *host) {
+  static int enabled = -1;
+  if (enabled < 0) {
+    const char *e = std::getenv("GT_DIRECT_HOST");
+    enabled = (e && e[0] == '0') ? 0 : 1;
+  }
+  if (!enabled || !host) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 int sm_count() {

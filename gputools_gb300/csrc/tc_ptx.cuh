@@ -4,6 +4,7 @@
 
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -200,25 +201,70 @@ __device__ __forceinline__ uint64_t smem_desc_kmajor(uint32_t saddr, int row_byt
   return d;
 }
 
-// Instruction descriptor: kind::f16, A = B = bf16, D = f32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+// Instruction descriptor: kind::f16, D = f32, A and B K-major and of the same
+// 16-bit type (ab_fmt 0: fp16, 1: bf16).
+__host__ __device__ constexpr uint32_t idesc_f32acc(int M, int N, uint32_t ab_fmt) {
   return (1u << 4)                    // D format f32
-         | (1u << 7)                  // A format bf16
-         | (1u << 10)                 // B format bf16
+         | (ab_fmt << 7)              // A format
+         | (ab_fmt << 10)             // B format
          | (uint32_t(N >> 3) << 17)   // N / 8
          | (uint32_t(M >> 4) << 24);  // M / 16
 }
 
-// Split of a float into NSPLIT bf16 parts, each the round-to-nearest bf16 of
-// the remainder of the previous ones; every remainder is exact in float.
-template <int NSPLIT>
-__device__ __forceinline__ void split_bf16(float z, __nv_bfloat16 (&p)[3]) {
-  float rem = z;
+// Operand encodings of the split planes (the values of enum gt_gram_path):
+//   bf16x3  two bf16 parts (hi, lo), products hi.hi + hi.lo + lo.hi
+//   bf16x6  three bf16 parts, the six products of total order <= 2
+//   f16x3   two fp16 parts of the value times a power of two chosen so that
+//           the largest magnitude lies in [2^14, 2^15); hi carries 11 bits and
+//           lo the next 11, so the three products keep ~2^-22 per element
+//           at the cost of bf16x3.
+constexpr int KIND_BF16X3 = 0, KIND_BF16X6 = 1, KIND_F16X3 = 3;
+
+template <int KIND>
+struct Kind {
+  static constexpr int NSPLIT = KIND == KIND_BF16X6 ? 3 : 2;
+  static constexpr bool F16 = KIND == KIND_F16X3;
+  static constexpr uint32_t AB_FMT = F16 ? 0u : 1u;
+};
+
+// Split of v into the parts of KIND, as raw 16-bit patterns; each part is the
+// round-to-nearest of the remainder of the previous ones (every remainder is
+// exact in float).  For f16x3, v must already carry its power-of-two scale.
+template <int KIND>
+__device__ __forceinline__ void split_parts(float v, uint16_t (&p)[3]) {
+  float rem = v;
+  if (Kind<KIND>::F16) {
 #pragma unroll
-  for (int i = 0; i < NSPLIT; i++) {
-    p[i] = __float2bfloat16_rn(rem);
-    rem -= __bfloat162float(p[i]);
+    for (int i = 0; i < 2; i++) {
+      const __half h = __float2half_rn(rem);
+      p[i] = __half_as_ushort(h);
+      rem -= __half2float(h);
+    }
+    p[2] = 0;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      if (i < Kind<KIND>::NSPLIT) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(rem);
+        p[i] = __bfloat16_as_ushort(h);
+        rem -= __bfloat162float(h);
+      } else {
+        p[i] = 0;
+      }
+    }
   }
+}
+
+// Power of two 2^e, e in [-126, 127], built from its exponent bits.
+__device__ __forceinline__ float exp2i(int e) { return __uint_as_float(uint32_t(e + 127) << 23); }
+
+// Scale exponent that brings the largest magnitude m of a row into
+// [2^14, 2^15) for the f16x3 encoding (0 for m = 0 or non-finite m).
+__device__ __forceinline__ int f16_scale_exp(float m) {
+  if (!(m > 0.f) || !(m <= 3.4e38f)) return 0;
+  const int e = int((__float_as_uint(m) >> 23) & 255u) - 127;  // floor(log2 m), normal m
+  int s = 14 - e;
+  return s > 126 ? 126 : (s < -126 ? -126 : s);
 }
 
 }  // namespace tc

@@ -60,7 +60,8 @@ enum gt_layout { GT_LAYOUT_FULL = 0, GT_LAYOUT_DIST = 1 };
 enum gt_gram_path {
   GT_GRAM_TC_BF16X3 = 0, /* tcgen05, each operand split hi+lo bf16, 3 products */
   GT_GRAM_TC_BF16X6 = 1, /* tcgen05, 3-way bf16 split, 6 products             */
-  GT_GRAM_FP32 = 2       /* plain FP32 CUDA-core path                         */
+  GT_GRAM_FP32 = 2,      /* plain FP32 CUDA-core path                         */
+  GT_GRAM_TC_F16X3 = 3   /* tcgen05, power-of-two scaled hi+lo fp16, 3 products */
 };
 
 /* ======================================================================== *

@@ -4,7 +4,8 @@ holds to FP64 central finite differences.
 
 Error metric: max |gpu - oracle| / max |oracle| over the gradient.
 Tolerances: fp32 and bf16x6 paths 2e-5, bf16x3 2e-4 (its ~2^-16 products),
-distance adjoints (float32 CUDA cores) 2e-5.
+f16x3 2e-5 (the adjoint GEMM's operands are not unit-scaled, so it runs as
+bf16x6), distance adjoints (float32 CUDA cores) 2e-5.
 """
 import ctypes
 
@@ -13,7 +14,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp32": 2e-5, "bf16x6": 2e-5, "bf16x3": 2e-4}
+TOL = {"fp32": 2e-5, "bf16x6": 2e-5, "bf16x3": 2e-4, "f16x3": 2e-5}
 
 
 def rel(got, want):
@@ -34,7 +35,7 @@ def cor_bwd_device(lib, X, G):
     return out.cpu().numpy().astype(np.float64)
 
 
-@pytest.fixture(params=["fp32", "bf16x3", "bf16x6"])
+@pytest.fixture(params=["fp32", "bf16x3", "bf16x6", "f16x3"])
 def path(request, gpu):
     import gputools_gb300 as g
     old = g.get_gram_path()

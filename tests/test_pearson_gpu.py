@@ -6,6 +6,7 @@ Tolerances, per Gram evaluation:
   fp32    2e-6 * sqrt(n / 100) + 1e-6   (float32 accumulation of n products)
   bf16x6  same as fp32                  (3-way bf16 split: float32-exact products)
   bf16x3  2e-5                          (2-way split drops the lo*lo product, ~2^-16)
+  f16x3   same as fp32                  (scaled 2-way fp16 split, ~2^-21 per product)
 pairs must match exactly; t-scores are checked against hostSignif's rule
 applied to the returned r, and against the oracle away from |r| -> 1.
 """
@@ -16,7 +17,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-PATHS = ("fp32", "bf16x3", "bf16x6")
+PATHS = ("fp32", "bf16x3", "bf16x6", "f16x3")
 
 
 def tol(path, n):
