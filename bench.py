@@ -429,22 +429,37 @@ def run_euclid(args, lib, g, _lib, stream, dev, headline):
                        f"(sd {E_SD}), {int(E_DUP*100)}% exact duplicates, R dist layout",
            "entries_per_step": m}
     # the bf16 settings evaluate distances as bf16x6
+    peaks, peaks_kind = load_peaks()
     for pth in ("bf16x6", "f16x3", "fp32") if headline != "fp32" else ("fp32",):
         g.set_gram_path(pth)
         k = max(3, args.steps // 4)
         for _ in range(1):
             step()
         torch.cuda.synchronize()
+        lib.gt_profile_reset()
+        lib.gt_profile_enable(1)
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(k):
             step()
         e1.record(stream)
         torch.cuda.synchronize()
+        lib.gt_profile_enable(0)
         ms = e0.elapsed_time(e1) / k
         rel, zero_ok, nzero = check()
         res[pth] = {"entries_per_s": m / (ms * 1e-3), "ms_per_step": ms, "max_rel_err": rel,
                     "duplicates_exact_zero": zero_ok, "zero_pairs_in_sample": nzero}
+        kms = ctypes.c_double(0); kn = ctypes.c_uint64(0)
+        lib.gt_profile_kernel_ms(b"euclid_gram", ctypes.byref(kms), ctypes.byref(kn))
+        if kn.value and pth != "fp32":
+            kernel_ms = kms.value / kn.value
+            algo = m * 4.0 + n * E_DIM * 4.0  # dist entries written + points read once
+            achieved = algo / (kernel_ms * 1e-3) / 1e9
+            res[pth]["roofline"] = {
+                "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_kind": f"{peaks_kind} copy bandwidth",
+                "kernel": "euclid_gram (tcgen05)", "kernel_ms": kernel_ms,
+                "traffic": load_traffic().get(f"euclid_gram_{pth}")}
     g.set_gram_path(headline)
     del out
     torch.cuda.empty_cache()
