@@ -73,16 +73,20 @@ constexpr int kMaxSmem = 232448;                  // dynamic shared memory per C
 constexpr int kEpiTileFloats = 32 * 33;           // one warp's padded 32 x 32 staging tile
 
 // ----------------------------------------------------------------- tiling
-// Symmetric problems schedule, in column block tj, the row blocks
-// 0 .. min(2 tj + 1, tr - 1): the 128-row blocks that reach the upper
-// triangle of a 256-column block.
+// Tile sets.  kFull: every (row block, column block).  kUpper (symmetric
+// problems whose entries r < c are wanted): column block tj holds row blocks
+// 0 .. min(2 tj + 1, tr - 1), the 128-row blocks that reach the upper
+// triangle of a 256-column block.  kLower (entries c < r): row block ti holds
+// column blocks 0 .. min(ti / 2, tc - 1), enumerated row by row.
+enum TileMode { kFull = 0, kUpper = 1, kLower = 2 };
+
 struct TileSpace {
   int64_t tr, tc;    // row blocks (128), column blocks (256)
-  int64_t j0;        // symmetric: column blocks whose tile count is 2*tj + 2
+  int64_t j0;        // upper: column blocks whose tile count is 2*tj + 2
   int64_t ntiles;    // below 2^31
-  int64_t group;     // column blocks per band of the tile order (power of two)
+  int64_t group;     // upper / full: column blocks per band of the tile order (power of two)
   int group_log2;
-  int symmetric;
+  int symmetric;     // TileMode
 };
 
 // Tile order.  Column blocks are grouped into bands of `group` (a power of
@@ -96,7 +100,28 @@ __host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t64, in
                                             int64_t &tj) {
   const uint32_t t = uint32_t(t64), tr = uint32_t(ts.tr), tc = uint32_t(ts.tc);
   const uint32_t G = uint32_t(ts.group), lg = uint32_t(ts.group_log2);
-  if (!ts.symmetric) {
+  if (ts.symmetric == kLower) {
+    // row pairs (2m, 2m + 1) hold m + 1 tiles each while m + 1 <= tc; rows
+    // from 2 tc on hold tc tiles
+    const uint32_t head = tc * (tc + 1);
+    if (t < head) {
+      int32_t m = int32_t((sqrtf(float(t) * 4.f + 1.f) - 1.f) * 0.5f);
+      if (m < 0) m = 0;
+      while (uint32_t(m + 1) * uint32_t(m + 2) <= t) m++;
+      while (uint32_t(m) * uint32_t(m + 1) > t) m--;
+      const uint32_t u = t - uint32_t(m) * uint32_t(m + 1), w = uint32_t(m) + 1;
+      const uint32_t e = u >= w ? 1u : 0u;
+      ti = 2 * uint32_t(m) + e;
+      tj = u - e * w;
+    } else {
+      const uint32_t u = t - head;
+      const uint32_t i = u / tc;
+      ti = 2 * tc + i;
+      tj = u - i * tc;
+    }
+    return;
+  }
+  if (ts.symmetric == kFull) {
     const uint32_t c0 = (t / (tr << lg)) << lg;
     const uint32_t g = (tc - c0) < G ? (tc - c0) : G;
     const uint32_t u = t - c0 * tr;
@@ -145,15 +170,25 @@ __host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t64, in
   }
 }
 
-TileSpace make_tiles(int64_t nr, int64_t nc, bool symmetric, int64_t group) {
+TileSpace make_tiles(int64_t nr, int64_t nc, int mode, int64_t group) {
   TileSpace ts;
   ts.tr = cdiv(nr, kBM);
   ts.tc = cdiv(nc, kBN);
-  ts.symmetric = symmetric ? 1 : 0;
+  ts.symmetric = mode;
   ts.group_log2 = 0;
   while ((int64_t(2) << ts.group_log2) <= group) ts.group_log2++;
   ts.group = int64_t(1) << ts.group_log2;
-  if (symmetric) {
+  if (mode == kLower) {
+    ts.j0 = 0;
+    ts.group = 1;
+    ts.group_log2 = 0;
+    if (ts.tr <= 2 * ts.tc) {
+      const int64_t m = ts.tr / 2, e = ts.tr % 2;
+      ts.ntiles = m * (m + 1) + e * (m + 1);
+    } else {
+      ts.ntiles = ts.tc * (ts.tc + 1) + (ts.tr - 2 * ts.tc) * ts.tc;
+    }
+  } else if (mode == kUpper) {
     ts.j0 = ts.tr / 2;
     if (ts.j0 > ts.tc) ts.j0 = ts.tc;
     ts.ntiles = ts.j0 * (ts.j0 + 1) + (ts.tc - ts.j0) * ts.tr;
@@ -283,11 +318,16 @@ struct PearsonFinish {
 };
 
 // Operands are the points centred by their column means (distances do not
-// change).  d^2 = |a|^2 + |b|^2 - 2 G with float norms (compensated sums); an
-// entry whose d^2 is below tau * (|a|^2 + |b|^2), where rounding of the
-// contraction could dominate, is recomputed from the original float points:
-// the warp queues such pairs and recomputes four at a time, eight lanes per
-// pair (float differences, squares with their FMA residuals, compensated
+// change).  The kernel runs the lower tile set: TMEM lane = point a, column =
+// point b < a, so for a fixed column the 32 lanes of a warp hold consecutive
+// points a, which are consecutive entries of one row of R's dist layout (and
+// of one row of the full matrix's mirror orientation): those stores go out
+// coalesced straight from registers.
+// d^2 = |a|^2 + |b|^2 - 2 G with float norms (compensated sums); an entry
+// whose d^2 is below tau * (|a|^2 + |b|^2), where rounding of the contraction
+// could dominate, is recomputed from the original float points: the warp
+// queues such pairs and recomputes four at a time, eight lanes per pair
+// (float differences, squares with their FMA residuals, compensated
 // float-pair sums), overwriting the estimate it stored first.  Exact
 // duplicates come out exactly 0.
 struct EuclidFinish {
@@ -304,7 +344,7 @@ struct EuclidFinish {
     return n * i - i * (i + 1) / 2 - i - 1 + j;
   }
 
-  // The lane's row values and the warp's column values for this tile.
+  // The lane's point values and the warp's column values for this tile.
   __device__ void begin_tile(int64_t r, EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
     ctx.me = nrm[r];
@@ -312,6 +352,7 @@ struct EuclidFinish {
     __syncwarp();
   }
 
+  // Block of points a = r (lanes) against b = c0 + k (k = 0..31), b < a.
   __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
     float *wsm = ctx.wsm;
@@ -320,62 +361,58 @@ struct EuclidFinish {
     // the block's column values (shared-memory broadcasts)
     const float2 *cv = ctx.cnrm + (c0 - ctx.col0);
     const bool full = layout == GT_LAYOUT_FULL;
-    // interior block: every row below every column, every column < n
-    const bool interior = (rbase + 31 < c0) && (c0 + 31 < n);
-    unsigned pend = 0u;
+    // interior block: every column below every row, every row < n
+    const bool interior = (c0 + 31 < rbase) && (rbase + 31 < n);
+    unsigned pend = 0u;  // bit 31 - k: entry (r, c0 + k) is recomputed
     if (interior) {
-      float *om = out + (c0 * n + r);  // mirror orientation (full layout)
+      // row c0 + k of the dist layout (or of the full matrix), column r
+      float *o = out + (full ? c0 * n + r : dist_index(c0, r));
+      const int64_t step0 = full ? n : n - c0 - 2;
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const float2 cj = cv[j];
+      for (int k = 0; k < 32; k++) {
+        const float2 cj = cv[k];
         const float s = na + cj.x;
-        const float d2 = fmaf(ra * cj.y, g[j], s);
-        pend |= (__float_as_uint(fmaf(-tau, s, d2)) >> 31) << j;
-        const float v = tc::sqrt_approx(fmaxf(d2, 0.f));
-        wsm[lane * 33 + j] = v;
-        if (full) {
-          *om = v;
-          om += n;
-        }
+        const float d2 = fmaf(ra * cj.y, g[k], s);
+        pend = (pend << 1) | (__float_as_uint(fmaf(-tau, s, d2)) >> 31);
+        const float v = tc::sqrt_approx(fabsf(d2));
+        *o = v;
+        o += full ? step0 : step0 - k;
+        if (full) wsm[lane * 33 + k] = v;
       }
-      __syncwarp();
-      float *o = out + ((full ? rbase * n : dist_index(rbase, 0)) + c0 + lane);
+      if (full) {
+        // row orientation (r, c0 + k) through the staging tile
+        __syncwarp();
+        float *q = out + (rbase * n + c0 + lane);
 #pragma unroll 8
-      for (int i = 0; i < 32; i++) {
-        *o = wsm[i * 33 + lane];
-        o += full ? n : n - (rbase + i) - 2;
+        for (int i = 0; i < 32; i++) {
+          *q = wsm[i * 33 + lane];
+          q += n;
+        }
       }
     } else {
-      // this lane's row uses columns c0 + j with r < c0 + j < n
-      const int64_t lo64 = r + 1 - c0, hi64 = n - c0;
-      const int jlo = lo64 < 0 ? 0 : (lo64 > 32 ? 32 : int(lo64));
-      const int jhi = r >= n ? 0 : (hi64 > 32 ? 32 : (hi64 < 0 ? 0 : int(hi64)));
+      // this lane's row uses columns c0 + k < r, r < n
+      const int64_t hi64 = r - c0;
+      const int khi = r >= n ? 0 : (hi64 > 32 ? 32 : (hi64 < 0 ? 0 : int(hi64)));
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const float2 cj = cv[j];
+      for (int k = 0; k < 32; k++) {
+        const float2 cj = cv[k];
         const float s = na + cj.x;
-        const float d2 = fmaf(ra * cj.y, g[j], s);
-        const bool valid = (j >= jlo) & (j < jhi);
-        pend |= unsigned(valid & (d2 < tau * s)) << j;
-        const float v = valid ? tc::sqrt_approx(fmaxf(d2, 0.f)) : 0.f;
-        wsm[lane * 33 + j] = v;
-        if (full && valid) out[(c0 + j) * n + r] = v;
+        const float d2 = fmaf(ra * cj.y, g[k], s);
+        const bool valid = k < khi;
+        pend = (pend << 1) | unsigned(valid & (d2 < tau * s));
+        const float v = valid ? tc::sqrt_approx(fabsf(d2)) : 0.f;
+        wsm[lane * 33 + k] = v;
+        if (valid) out[full ? (c0 + k) * n + r : dist_index(c0 + k, r)] = v;
       }
-      __syncwarp();
-      const int64_t c = c0 + lane;
-      // offset of (row rbase, column 0): full n*r; R dist n*r - r(r+1)/2 - r - 1
-      int64_t off = full ? rbase * n : dist_index(rbase, 0);
-      for (int i = 0; i < 32; i++) {
-        const int64_t ri = rbase + i;
-        if (ri >= n) break;
-        if (c < n) {
-          if (full) {
-            if (c >= ri) out[off + c] = (c == ri) ? 0.f : wsm[i * 33 + lane];
-          } else if (c > ri) {
-            out[off + c] = wsm[i * 33 + lane];
-          }
+      if (full) {
+        __syncwarp();
+        const int64_t c = c0 + lane;
+        for (int i = 0; i < 32; i++) {
+          const int64_t ri = rbase + i;
+          if (ri >= n) break;
+          if (c < ri) out[ri * n + c] = wsm[i * 33 + lane];
+          else if (c == ri) out[ri * n + c] = 0.f;
         }
-        off += full ? n : n - ri - 2;
       }
     }
     __syncwarp();
@@ -396,9 +433,9 @@ struct EuclidFinish {
       int take = room - start;
       take = take < 0 ? 0 : (take > cnt ? cnt : take);
       for (int t = 0; t < take; t++) {
-        const int jb = __ffs(int(pend)) - 1;
+        const int bit = __ffs(int(pend)) - 1;
         pend &= pend - 1u;
-        ctx.list[ctx.nlist + start + t] = (uint32_t(lane) << 8) | (cofs + uint32_t(jb));
+        ctx.list[ctx.nlist + start + t] = (uint32_t(lane) << 8) | (cofs + uint32_t(31 - bit));
       }
       ctx.nlist += total < room ? total : room;
       if (ctx.nlist == kEuclidList) flush(ctx);
@@ -449,11 +486,12 @@ struct EuclidFinish {
       }
       if (act && sub == 0) {
         const float d = sqrtf(hi + lo);
+        const int64_t lo_i = i < j ? i : j, hi_i = i < j ? j : i;
         if (layout == GT_LAYOUT_FULL) {
           out[i * n + j] = d;
           out[j * n + i] = d;
         } else {
-          out[dist_index(i, j)] = d;
+          out[dist_index(lo_i, hi_i)] = d;
         }
       }
     }
@@ -1060,7 +1098,7 @@ int err_word(int **p) {
 
 template <int KIND, int BK, bool CHUNKED, class Fin>
 int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
-                bool symmetric, int64_t ckb, const Fin &fin, const char *prof_name,
+                int mode, int64_t ckb, const Fin &fin, const char *prof_name,
                 cudaStream_t s) {
   using C = TcCfg<KIND, BK, !CHUNKED>;
   using W = SingleWork<Fin>;
@@ -1070,7 +1108,7 @@ int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t 
   W w;
   GT_TRY(make_plane_map(&w.ma, zA, nA, kpad, C::NSPLIT, kBM, BK, F16));
   GT_TRY(make_plane_map(&w.mb, zB, nB, kpad, C::NSPLIT, kBN, BK, F16));
-  w.ts = make_tiles(nA, nB, symmetric, band_group(int64_t(kBN) * kpad * 2 * C::NSPLIT));
+  w.ts = make_tiles(nA, nB, mode, band_group(int64_t(kBN) * kpad * 2 * C::NSPLIT));
   if (w.ts.ntiles > 2147483647LL) return fail(GT_EINVAL, "problem too large (%lld tiles)",
                                              (long long)w.ts.ntiles);
   w.nk = kpad / BK;
@@ -1127,9 +1165,9 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
   if (nA == 0 || nB == 0) return GT_OK;
   StoreFinish fin{C, ldc, nA, nB};
   if (nsplit == 3)
-    return launch_gram<tc::KIND_BF16X6, 32, true>(planesA, nA, planesB, nB, kpad, false,
+    return launch_gram<tc::KIND_BF16X6, 32, true>(planesA, nA, planesB, nB, kpad, kFull,
                                                   tc_chunk_kblocks(32), fin, "gemm_store", s);
-  return launch_gram<tc::KIND_BF16X3, 64, true>(planesA, nA, planesB, nB, kpad, false,
+  return launch_gram<tc::KIND_BF16X3, 64, true>(planesA, nA, planesB, nB, kpad, kFull,
                                                 tc_chunk_kblocks(64), fin, "gemm_store", s);
 }
 
@@ -1176,7 +1214,7 @@ int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t k
   const float gscale = kind == tc::KIND_F16X3 ? 1.f / 268435456.f : 1.f;  // 2^-28
   PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
                     std::sqrt(out.npairs - 2.f), gscale, out.symmetric};
-  const bool sym = out.symmetric != 0;
+  const int sym = out.symmetric ? kUpper : kFull;
   if (kind == tc::KIND_BF16X6)
     return launch_gram<tc::KIND_BF16X6, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32),
                                                   fin, "pearson_gram", s);
@@ -1226,7 +1264,7 @@ int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int
   }
   const int vec4 = (reinterpret_cast<uintptr_t>(d_pts) & 15u) == 0 && (dim & 3) == 0;
   EuclidFinish fin{nrm, d_pts, d_out, n, dim, layout, tau, vec4};
-  return launch_gram<KIND, 32, false>(z, n, z, n, kpad, true, 0, fin, "euclid_gram", st);
+  return launch_gram<KIND, 32, false>(z, n, z, n, kpad, kLower, 0, fin, "euclid_gram", st);
 }
 
 }  // namespace
@@ -1295,7 +1333,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     std::memset(&d, 0, sizeof(d));
     GT_TRY(make_plane_map(&d.map_a, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk, f16));
     GT_TRY(make_plane_map(&d.map_b, planes + b.plane_off, b.p, b.kpad, nsplit, kBN, bk, f16));
-    d.ts = make_tiles(b.p, b.p, true, 1);
+    d.ts = make_tiles(b.p, b.p, kUpper, 1);
     d.nk = b.kpad / bk;
     d.fin = PearsonFinish{q.corr, q.ts, q.pairs, b.p, b.p, b.p, float(b.n),
                           std::sqrt(float(b.n) - 2.f), gscale, 1};
