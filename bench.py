@@ -595,12 +595,14 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     Xp = rng.standard_normal((1000, 500)).astype(np.float32)
     hc = np.empty((1000, 1000), np.float32); ht = np.empty_like(hc); hp = np.empty_like(hc)
     fp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    _lib.check(lib.gt_pmcc(0, fp(Xp), 1000, fp(Xp), 1000, 500, fp(hp), fp(hc), fp(ht)))  # warm-up
     t0 = time.perf_counter()
     for _ in range(k):
         _lib.check(lib.gt_pmcc(0, fp(Xp), 1000, fp(Xp), 1000, 500, fp(hp), fp(hc), fp(ht)))
     out["pearson_500x1000_e2e"] = {"ms": (time.perf_counter() - t0) / k * 1e3}
     pts = rng.standard_normal((2000, 64)).astype(np.float32)
     hd = np.empty((2000, 2000), np.float32)
+    _lib.check(lib.gt_distances(fp(pts), 2000, 64, fp(hd), 0, ctypes.c_float(2.0)))  # warm-up
     t0 = time.perf_counter()
     for _ in range(k):
         _lib.check(lib.gt_distances(fp(pts), 2000, 64, fp(hd), 0, ctypes.c_float(2.0)))
