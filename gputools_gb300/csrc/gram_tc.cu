@@ -45,6 +45,7 @@
 // Every mbarrier wait is bounded: on timeout the CTA raises an error word,
 // drains its in-flight copies and MMAs, releases its TMEM and exits.
 #include "common.cuh"
+#include "dist_lines.cuh"
 #include "kernels.cuh"
 #include "tc_ptx.cuh"
 #include "stats.cuh"
@@ -214,15 +215,25 @@ int64_t band_group(int64_t panel_bytes) {
 
 constexpr int kEuclidList = 64;  // pending near-zero pairs per epilogue warp
 
+constexpr int kEuclidCols = 64;  // columns per epilogue warp of the Euclidean kernels
+
+// Per-warp state of the epilogue.  Only what changes per tile lives here;
+// the list and the column norms sit at fixed offsets after the staging tile.
 struct EpiCtx {
-  float *wsm;       // 32 x 33 staging tile
-  uint32_t *list;   // kEuclidList entries: (row - rbase) << 8 | (col - col0)
-  float2 *cnrm;     // the warp's columns' {norm, scale} (Euclidean)
+  float *wsm;       // 32 x 33 staging tile, then (Euclidean) the list and column norms
   float2 me;        // this lane's row's {norm, scale} (Euclidean)
-  int nlist;        // warp-uniform
-  int ncols;        // columns per warp (128 or 64)
+  int nlist;        // warp-uniform: entries in the shared-memory list
+  int gcount;       // warp-uniform: entries in the warp's region of a global list
   int64_t rbase;    // first row of the warp's 32 rows
   int64_t col0;     // first column of the warp's columns
+  // kEuclidList entries: (row - rbase) << 8 | (col - col0), or finish-defined
+  __device__ __forceinline__ uint32_t *list() const {
+    return reinterpret_cast<uint32_t *>(wsm + kEpiTileFloats);
+  }
+  // the warp's kEuclidCols columns' {norm, scale} (Euclidean)
+  __device__ __forceinline__ float2 *cnrm() const {
+    return reinterpret_cast<float2 *>(wsm + kEpiTileFloats + kEuclidList);
+  }
 };
 
 __device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
@@ -314,7 +325,8 @@ struct PearsonFinish {
     __syncwarp();
   }
   __device__ void begin_tile(int64_t, EpiCtx &) const {}
-  __device__ void flush(EpiCtx &) const {}
+  __device__ void end_tile(EpiCtx &) const {}
+  __device__ void drain(EpiCtx &) const {}
 };
 
 // Operands are the points centred by their column means (distances do not
@@ -330,6 +342,97 @@ struct PearsonFinish {
 // (float differences, squares with their FMA residuals, compensated
 // float-pair sums), overwriting the estimate it stored first.  Exact
 // duplicates come out exactly 0.
+// Near-zero pairs of the Euclidean finishes.  A block's pending bits (bit
+// 31 - k: entry (lane's row, column k of the block) is recomputed) go to the
+// warp's list through fin.push(ctx, slot, lane, column offset in the warp's
+// columns); a full list is flushed at once.
+template <class Fin>
+__device__ __forceinline__ void euclid_queue(const Fin &fin, unsigned pend, uint32_t cofs,
+                                             EpiCtx &ctx) {
+  const unsigned FULLM = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  while (__any_sync(FULLM, pend != 0u)) {
+    const int cnt = __popc(pend);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULLM, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(FULLM, incl, 31);
+    const int room = kEuclidList - ctx.nlist;
+    const int start = incl - cnt;
+    int take = room - start;
+    take = take < 0 ? 0 : (take > cnt ? cnt : take);
+    for (int t = 0; t < take; t++) {
+      const int bit = __ffs(int(pend)) - 1;
+      pend &= pend - 1u;
+      fin.push(ctx, ctx.nlist + start + t, lane, cofs + uint32_t(31 - bit));
+    }
+    ctx.nlist += total < room ? total : room;
+    if (ctx.nlist == kEuclidList) fin.flush(ctx);
+  }
+}
+
+__device__ __forceinline__ void sq_add(float d, FloatPairSum &acc, float &res) {
+  const float q = d * d;
+  res += fmaf(d, d, -q);
+  acc.add(q);
+}
+
+// |a_i - a_j|^2 from the float points, compensated: each of the 8 lanes of
+// a group (sub = lane & 7) sums every 8th coordinate difference squared, the
+// group combines the partial pairs; every lane of the group gets the sum.
+__device__ __forceinline__ float pair_sq_dist(const float *__restrict__ pts, int64_t dim, int vec4,
+                                              int64_t i, int64_t j, int sub) {
+  const unsigned FULLM = 0xffffffffu;
+  const float *pa = pts + i * dim, *pb = pts + j * dim;
+  FloatPairSum acc;
+  float res = 0.f;
+  if (vec4) {
+    const float4 *a4 = reinterpret_cast<const float4 *>(pa);
+    const float4 *b4 = reinterpret_cast<const float4 *>(pb);
+    const int64_t d4 = dim >> 2;
+#pragma unroll 4
+    for (int64_t k = sub; k < d4; k += 8) {
+      const float4 x = a4[k], y = b4[k];
+      sq_add(x.x - y.x, acc, res);
+      sq_add(x.y - y.y, acc, res);
+      sq_add(x.z - y.z, acc, res);
+      sq_add(x.w - y.w, acc, res);
+    }
+  } else {
+    for (int64_t k = sub; k < dim; k += 8) sq_add(pa[k] - pb[k], acc, res);
+  }
+  float hi = acc.hi, lo = acc.lo + res;
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(FULLM, hi, o), ol = __shfl_xor_sync(FULLM, lo, o);
+    const float t = hi + oh, bp = t - hi;
+    lo = (lo + ol) + ((hi - (t - bp)) + (oh - bp));
+    hi = t;
+  }
+  return hi + lo;
+}
+
+// Recomputes the queued pairs: a group of 8 lanes per pair, 4 pairs per
+// round.  fin.entry(ctx, slot, i, j) reads a list entry as its pair of points.
+template <class Fin>
+__device__ void euclid_flush(const Fin &fin, EpiCtx &ctx) {
+  const int lane = threadIdx.x & 31, grp = lane >> 3, sub = lane & 7;
+  __syncwarp();
+  for (int b = 0; b < ctx.nlist; b += 4) {
+    const int idx = b + grp;
+    const bool act = idx < ctx.nlist;
+    int64_t i, j;
+    fin.entry(ctx, act ? idx : b, i, j);
+    const float d2 = pair_sq_dist(fin.pts, fin.dim, fin.vec4, i, j, sub);
+    if (act && sub == 0) fin.store_pair(i, j, sqrtf(d2));
+  }
+  ctx.nlist = 0;
+  __syncwarp();
+}
+
 struct EuclidFinish {
   const float2 *nrm;  // per point {|c|^2, 2^-s} (s its f16x3 scale exponent, else 0),
                       // zero padded to a multiple of 256 points
@@ -348,7 +451,7 @@ struct EuclidFinish {
   __device__ void begin_tile(int64_t r, EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
     ctx.me = nrm[r];
-    for (int k = lane; k < ctx.ncols; k += 32) ctx.cnrm[k] = nrm[ctx.col0 + k];
+    for (int k = lane; k < kEuclidCols; k += 32) ctx.cnrm()[k] = nrm[ctx.col0 + k];
     __syncwarp();
   }
 
@@ -359,7 +462,7 @@ struct EuclidFinish {
     const int64_t rbase = r - lane;
     const float na = ctx.me.x, ra = -2.f * ctx.me.y;
     // the block's column values (shared-memory broadcasts)
-    const float2 *cv = ctx.cnrm + (c0 - ctx.col0);
+    const float2 *cv = ctx.cnrm() + (c0 - ctx.col0);
     const bool full = layout == GT_LAYOUT_FULL;
     // interior block: every column below every row, every row < n
     const bool interior = (c0 + 31 < rbase) && (rbase + 31 < n);
@@ -417,86 +520,184 @@ struct EuclidFinish {
     }
     __syncwarp();
     // queue the pairs to recompute (after their estimates are stored)
-    const unsigned FULLM = 0xffffffffu;
-    const uint32_t cofs = uint32_t(c0 - ctx.col0);
-    while (__any_sync(FULLM, pend != 0u)) {
-      const int cnt = __popc(pend);
-      int incl = cnt;
+    euclid_queue(*this, pend, uint32_t(c0 - ctx.col0), ctx);
+  }
+
+  // list entry: lane << 8 | column offset, relative to the current tile
+  __device__ __forceinline__ void push(EpiCtx &ctx, int slot, int lane, uint32_t ofs) const {
+    ctx.list()[slot] = (uint32_t(lane) << 8) | ofs;
+  }
+  __device__ __forceinline__ void entry(const EpiCtx &ctx, int slot, int64_t &i, int64_t &j) const {
+    const uint32_t e = ctx.list()[slot];
+    i = ctx.rbase + int64_t(e >> 8);
+    j = ctx.col0 + int64_t(e & 255u);
+  }
+  __device__ __forceinline__ void store_pair(int64_t i, int64_t j, float d) const {
+    if (layout == GT_LAYOUT_FULL) {
+      out[i * n + j] = d;
+      out[j * n + i] = d;
+    } else {
+      out[i < j ? dist_index(i, j) : dist_index(j, i)] = d;
+    }
+  }
+  __device__ void flush(EpiCtx &ctx) const { euclid_flush(*this, ctx); }
+  __device__ void end_tile(EpiCtx &ctx) const { flush(ctx); }
+  __device__ void drain(EpiCtx &) const {}
+};
+
+// ----------------------------------------------------------------- aligned dist lines
+// The dist layout through aligned lines.  The warp's columns sit in its
+// staging tile, which this finish does not otherwise use: point ids, and the
+// offsets base(c) - base(c_first) of their dist columns from the warp's first
+// column (64 columns of one class span at most 4096 points, so the offsets
+// fit 32 bits), and the base of that first column.  The pending pairs follow
+// them in the staging tile.
+struct EuclidLineFinish {
+  const float2 *nrm;  // per point {|c|^2, 2^-s}
+  const float *pts;
+  float *out;
+  int64_t n, dim;
+  float tau;
+  int vec4;
+  DistLines lines;
+  int2 *pair_list;    // [CTA][epilogue warp][pair_cap] pending pairs (row, column)
+  int *pair_count;    // [CTA][epilogue warp] pairs listed, written at the end
+  int pair_cap, epi;
+
+  __device__ __forceinline__ static int *col_ids(const EpiCtx &ctx) {
+    return reinterpret_cast<int *>(ctx.wsm);
+  }
+  __device__ __forceinline__ static int *col_offs(const EpiCtx &ctx) {
+    return reinterpret_cast<int *>(ctx.wsm) + 64;
+  }
+  __device__ __forceinline__ static int2 *pairs(const EpiCtx &ctx) {
+    return reinterpret_cast<int2 *>(ctx.wsm + 128);  // kEuclidList entries
+  }
+  __device__ __forceinline__ static int64_t *first_base(const EpiCtx &ctx) {
+    return reinterpret_cast<int64_t *>(ctx.wsm + 256);
+  }
+  // this warp's region of the global pair list (epilogue warps follow the
+  // producer and MMA warps)
+  __device__ __forceinline__ int64_t region_index() const {
+    return int64_t(blockIdx.x) * epi + (int(threadIdx.x >> 5) - 2);
+  }
+  __device__ __forceinline__ int2 *region() const { return pair_list + region_index() * pair_cap; }
+  __device__ __forceinline__ int64_t base(int64_t c) const { return n * c - c * (c + 1) / 2 - c - 1; }
+
+  __device__ void begin_tile(int64_t r, EpiCtx &ctx) const {
+    const int lane = threadIdx.x & 31;
+    ctx.me = (r >= 0 && r < n) ? nrm[r] : make_float2(0.f, 0.f);
+    const uint32_t p0 = uint32_t(ctx.col0);
+    const int64_t b0 = base(lines.point32(p0));
+    if (lane == 0) *first_base(ctx) = b0;
+    int *cid = col_ids(ctx);
+    int *cof = col_offs(ctx);
+    for (int k = lane; k < kEuclidCols; k += 32) {
+      const int32_t c = lines.point32(p0 + uint32_t(k));
+      cid[k] = c;
+      cof[k] = c < n ? int(base(c) - b0) : 0;
+      ctx.cnrm()[k] = c < n ? nrm[c] : make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+  }
+
+  // Rows r (lanes) against the block's 32 columns (ascending points).
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
+    const int lane = threadIdx.x & 31;
+    const int off = int(c0 - ctx.col0);
+    const int *cid = col_ids(ctx) + off;
+    const int4 *cof4 = reinterpret_cast<const int4 *>(col_offs(ctx) + off);
+    const float4 *cv4 = reinterpret_cast<const float4 *>(ctx.cnrm() + off);
+    const int64_t rbase = r - lane;
+    const float na = ctx.me.x, ra = -2.f * ctx.me.y;
+    float *const orow = out + (*first_base(ctx) + r);
+    // interior block: every column below every row, every row < n
+    const bool interior = (int64_t(cid[31]) < rbase) && (rbase + 31 < n);
+    unsigned pend = 0u;
+    if (interior) {
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(FULLM, incl, o);
-        if (lane >= o) incl += t;
+      for (int k4 = 0; k4 < 8; k4++) {
+        const int4 o4 = cof4[k4];
+        const float4 ca = cv4[2 * k4], cb = cv4[2 * k4 + 1];
+        const float cn[4] = {ca.x, ca.z, cb.x, cb.z}, cs[4] = {ca.y, ca.w, cb.y, cb.w};
+        const int co[4] = {o4.x, o4.y, o4.z, o4.w};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const float s = na + cn[e];
+          const float d2 = fmaf(ra * cs[e], g[4 * k4 + e], s);
+          pend = (pend << 1) | (__float_as_uint(fmaf(-tau, s, d2)) >> 31);
+          orow[co[e]] = tc::sqrt_approx(fabsf(d2));
+        }
       }
-      const int total = __shfl_sync(FULLM, incl, 31);
-      const int room = kEuclidList - ctx.nlist;
-      const int start = incl - cnt;
-      int take = room - start;
-      take = take < 0 ? 0 : (take > cnt ? cnt : take);
-      for (int t = 0; t < take; t++) {
+    } else {
+#pragma unroll
+      for (int k4 = 0; k4 < 8; k4++) {
+        const int4 o4 = cof4[k4];
+        const float4 ca = cv4[2 * k4], cb = cv4[2 * k4 + 1];
+        const float cn[4] = {ca.x, ca.z, cb.x, cb.z}, cs[4] = {ca.y, ca.w, cb.y, cb.w};
+        const int co[4] = {o4.x, o4.y, o4.z, o4.w};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const float s = na + cn[e];
+          const float d2 = fmaf(ra * cs[e], g[4 * k4 + e], s);
+          const bool valid = (int64_t(cid[4 * k4 + e]) < r) && (r < n);
+          pend = (pend << 1) | unsigned(valid & (d2 < tau * s));
+          if (valid) orow[co[e]] = tc::sqrt_approx(fabsf(d2));
+        }
+      }
+    }
+    __syncwarp();
+    queue(pend, off, ctx);
+  }
+
+  // Pending pairs go to the warp's region of the global list (recomputed by
+  // euclid_fixup_kernel after this kernel); once the region is full, to the
+  // shared-memory list that the warp recomputes itself.
+  __device__ __forceinline__ void queue(unsigned pend, int off, EpiCtx &ctx) const {
+    const unsigned FULLM = 0xffffffffu;
+    if (!__any_sync(FULLM, pend != 0u)) return;
+    const int lane = threadIdx.x & 31;
+    const int cnt = __popc(pend);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULLM, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(FULLM, incl, 31);
+    if (ctx.gcount + total <= pair_cap) {
+      int2 *dst = region() + (ctx.gcount + incl - cnt);
+      const int row = int(ctx.rbase) + lane;
+      const int *cid = col_ids(ctx) + off;
+      while (pend) {
         const int bit = __ffs(int(pend)) - 1;
         pend &= pend - 1u;
-        ctx.list[ctx.nlist + start + t] = (uint32_t(lane) << 8) | (cofs + uint32_t(31 - bit));
+        *dst++ = make_int2(row, cid[31 - bit]);
       }
-      ctx.nlist += total < room ? total : room;
-      if (ctx.nlist == kEuclidList) flush(ctx);
+      ctx.gcount += total;
+      return;
     }
+    euclid_queue(*this, pend, uint32_t(off), ctx);
   }
 
-  __device__ __forceinline__ static void sq_add(float d, FloatPairSum &acc, float &res) {
-    const float q = d * d;
-    res += fmaf(d, d, -q);
-    acc.add(q);
+  // list entry: the absolute pair (row, column), so that pairs wait across
+  // tiles and a warp recomputes only full lists (and its rest at the end)
+  __device__ __forceinline__ void push(EpiCtx &ctx, int slot, int lane, uint32_t ofs) const {
+    pairs(ctx)[slot] = make_int2(int(ctx.rbase) + lane, col_ids(ctx)[ofs]);
   }
-
-  // Recomputes the queued pairs: group of 8 lanes per pair, 4 pairs per round.
-  __device__ void flush(EpiCtx &ctx) const {
-    const unsigned FULLM = 0xffffffffu;
-    const int lane = threadIdx.x & 31, grp = lane >> 3, sub = lane & 7;
-    __syncwarp();
-    for (int b = 0; b < ctx.nlist; b += 4) {
-      const int idx = b + grp;
-      const bool act = idx < ctx.nlist;
-      const uint32_t e = ctx.list[act ? idx : b];
-      const int64_t i = ctx.rbase + int64_t(e >> 8), j = ctx.col0 + int64_t(e & 255u);
-      const float *pa = pts + i * dim, *pb = pts + j * dim;
-      FloatPairSum acc;
-      float res = 0.f;
-      if (vec4) {
-        const float4 *a4 = reinterpret_cast<const float4 *>(pa);
-        const float4 *b4 = reinterpret_cast<const float4 *>(pb);
-        const int64_t d4 = dim >> 2;
-#pragma unroll 4
-        for (int64_t k = sub; k < d4; k += 8) {
-          const float4 x = a4[k], y = b4[k];
-          sq_add(x.x - y.x, acc, res);
-          sq_add(x.y - y.y, acc, res);
-          sq_add(x.z - y.z, acc, res);
-          sq_add(x.w - y.w, acc, res);
-        }
-      } else {
-        for (int64_t k = sub; k < dim; k += 8) sq_add(pa[k] - pb[k], acc, res);
-      }
-      float hi = acc.hi, lo = acc.lo + res;
-#pragma unroll
-      for (int o = 4; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(FULLM, hi, o), ol = __shfl_xor_sync(FULLM, lo, o);
-        const float t = hi + oh, bp = t - hi;
-        lo = (lo + ol) + ((hi - (t - bp)) + (oh - bp));
-        hi = t;
-      }
-      if (act && sub == 0) {
-        const float d = sqrtf(hi + lo);
-        const int64_t lo_i = i < j ? i : j, hi_i = i < j ? j : i;
-        if (layout == GT_LAYOUT_FULL) {
-          out[i * n + j] = d;
-          out[j * n + i] = d;
-        } else {
-          out[dist_index(lo_i, hi_i)] = d;
-        }
-      }
-    }
-    ctx.nlist = 0;
-    __syncwarp();
+  __device__ __forceinline__ void entry(const EpiCtx &ctx, int slot, int64_t &i, int64_t &j) const {
+    const int2 e = pairs(ctx)[slot];
+    i = e.x;
+    j = e.y;
+  }
+  __device__ __forceinline__ void store_pair(int64_t i, int64_t j, float d) const {
+    out[base(j) + i] = d;  // i is the row (the larger point), j the column
+  }
+  __device__ void flush(EpiCtx &ctx) const { euclid_flush(*this, ctx); }
+  __device__ void end_tile(EpiCtx &) const {}
+  __device__ void drain(EpiCtx &ctx) const {
+    if ((threadIdx.x & 31) == 0) pair_count[region_index()] = ctx.gcount;
+    if (ctx.nlist) flush(ctx);
   }
 };
 
@@ -529,7 +730,8 @@ struct StoreFinish {
     __syncwarp();
   }
   __device__ void begin_tile(int64_t, EpiCtx &) const {}
-  __device__ void flush(EpiCtx &) const {}
+  __device__ void end_tile(EpiCtx &) const {}
+  __device__ void drain(EpiCtx &) const {}
 };
 
 // ----------------------------------------------------------------- kernel
@@ -577,7 +779,8 @@ __device__ __forceinline__ void product_parts(int p, int &pa, int &pb) {
 // its number of k-blocks, and the finish to apply.
 struct TileRef {
   const CUtensorMap *ma, *mb;
-  int64_t ti, tj, nk, prob;
+  int64_t row0, col0;  // first operand row of the A and B boxes (A may start below 0)
+  int64_t nk, prob;
 };
 
 // One problem: maps and finish as kernel parameters, tiles dealt round-robin.
@@ -590,7 +793,10 @@ struct SingleWork {
   __device__ bool tile(int64_t cursor, TileRef &ref) const {
     const int64_t t = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
     if (t >= ts.ntiles) return false;
-    tile_coords(ts, t, ref.ti, ref.tj);
+    int64_t ti, tj;
+    tile_coords(ts, t, ti, tj);
+    ref.row0 = ti * kBM;
+    ref.col0 = tj * kBN;
     ref.ma = &ma;
     ref.mb = &mb;
     ref.nk = nk;
@@ -598,6 +804,7 @@ struct SingleWork {
     return true;
   }
   __device__ const Fin &finish(const TileRef &) const { return fin; }
+  __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
   __device__ void prefetch() const {
     tc::prefetch_tensormap(&ma);
     tc::prefetch_tensormap(&mb);
@@ -635,7 +842,10 @@ struct PearsonBatchWork {
     const int64_t t = cta_tiles[idx];
     const int64_t pi = find_segment(tile_prefix, nprob, t);
     const PearsonBatchProblem &pr = probs[pi];
-    tile_coords(pr.ts, t - tile_prefix[pi], ref.ti, ref.tj);
+    int64_t ti, tj;
+    tile_coords(pr.ts, t - tile_prefix[pi], ti, tj);
+    ref.row0 = ti * kBM;
+    ref.col0 = tj * kBN;
     ref.ma = &pr.map_a;
     ref.mb = &pr.map_b;
     ref.nk = pr.nk;
@@ -643,7 +853,32 @@ struct PearsonBatchWork {
     return true;
   }
   __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
+  __device__ void drain(EpiCtx &) const {}
   __device__ void prefetch() const {}
+};
+
+// The dist layout in aligned lines (DistLines, LineTiles).
+struct EuclidLineWork {
+  CUtensorMap ma, mb;
+  int64_t nk;
+  LineTiles lt;
+  EuclidLineFinish fin;
+  __device__ bool tile(int64_t cursor, TileRef &ref) const {
+    const int64_t u = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
+    if (u >= int64_t(lt.ntiles)) return false;
+    lt.decode(uint32_t(u), ref.row0, ref.col0);
+    ref.ma = &ma;
+    ref.mb = &mb;
+    ref.nk = nk;
+    ref.prob = 0;
+    return true;
+  }
+  __device__ const EuclidLineFinish &finish(const TileRef &) const { return fin; }
+  __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
+  __device__ void prefetch() const {
+    tc::prefetch_tensormap(&ma);
+    tc::prefetch_tensormap(&mb);
+  }
 };
 
 template <int KIND, int BK, bool CHUNKED, class Work>
@@ -652,6 +887,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
   using C = TcCfg<KIND, BK, !CHUNKED>;
   constexpr int NSPLIT = C::NSPLIT;
   static_assert(!CHUNKED || C::COLS == 128, "chunked sums hold 128 columns per warp");
+  static_assert(CHUNKED || C::COLS == kEuclidCols, "the list kernels hold 64 columns per warp");
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                               ~uintptr_t(1023));
@@ -703,11 +939,11 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
             tc::tma_load_3d(st + p * C::A_TILE, ref.ma, &full[s], int32_t(kb * BK),
-                            int32_t(ref.ti * kBM), p);
+                            int32_t(ref.row0), p);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
             tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, ref.mb, &full[s],
-                            int32_t(kb * BK), int32_t(ref.tj * kBN), p);
+                            int32_t(kb * BK), int32_t(ref.col0), p);
         }
       }
       // drain: no bulk copy may still be writing shared memory at exit
@@ -778,17 +1014,15 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
     EpiCtx ctx;
     float *mine = epi_smem + (warp - 2) * C::EPI_FLOATS;
     ctx.wsm = mine;
-    ctx.list = CHUNKED ? nullptr : reinterpret_cast<uint32_t *>(mine + kEpiTileFloats);
-    ctx.cnrm = CHUNKED ? nullptr : reinterpret_cast<float2 *>(mine + kEpiTileFloats + kEuclidList);
-    ctx.ncols = C::COLS;
     ctx.nlist = 0;
+    ctx.gcount = 0;
     int64_t cc = 0;
     bool ok = true;
     TileRef ref;
     for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
-      const auto fin = work.finish(ref);
-      const int64_t r = ref.ti * kBM + q * 32 + lane;
-      const int64_t col = ref.tj * kBN + part * C::COLS;
+      const auto &fin = work.finish(ref);
+      const int64_t r = ref.row0 + q * 32 + lane;
+      const int64_t col = ref.col0 + part * C::COLS;
       ctx.rbase = r - lane;
       ctx.col0 = col;
       fin.begin_tile(r, ctx);
@@ -827,7 +1061,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
           for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
           fin(r, col + 32 * i, g, ctx);
         }
-        fin.flush(ctx);
+        fin.end_tile(ctx);
       } else {
         const int buf = int(cc & 1);
         const uint32_t ause = uint32_t(cc >> 1);
@@ -849,9 +1083,10 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&acce[buf]);
         cc++;
-        fin.flush(ctx);
+        fin.end_tile(ctx);
       }
     }
+    if (ok) work.drain(ctx);  // pairs that wait across tiles
     if (!ok) *abort_flag = 1;
   }
   __syncthreads();
@@ -983,20 +1218,27 @@ euclid_mean_kernel(const double *__restrict__ partial, int64_t nblk, int64_t dim
 
 // Euclidean operand planes of the centred points, one warp per point: the
 // squared norm (compensated), the largest magnitude (f16x3 scale), then the
-// planes.  nrm[v] = {|c|^2, 2^-s}; rows n .. npad-1 of nrm are zeroed.
+// planes.  nrm[v] = {|c|^2, 2^-s}; rows n .. npad-1 of nrm are zeroed.  With
+// ZB, the planes also go to row lines.pos(v) of the permuted column operand
+// (npb rows), whose padding rows are zeroed.
 template <int KIND>
 __global__ void __launch_bounds__(256)
 euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_t dim,
                     int64_t kpad, const float2 *__restrict__ mean2, uint16_t *__restrict__ Z,
-                    float2 *__restrict__ nrm) {
+                    float2 *__restrict__ nrm, uint16_t *__restrict__ ZB, int64_t npb,
+                    const DistLines lines) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
-  const int64_t plane = n * kpad;
-  for (int64_t v = warp; v < npad; v += nwarps) {
+  const int64_t plane = n * kpad, planeB = npb * kpad;
+  const int64_t nslot = npad > npb ? npad : npb;
+  for (int64_t v = warp; v < nslot; v += nwarps) {
+    // padding rows of the permuted column operand are zero
+    if (ZB && v < npb && lines.point(v) >= n)
+      write_row_planes<KIND>(0, kpad, planeB, ZB + v * kpad, [](int64_t, float (&)[4]) {});
     if (v >= n) {
-      if (lane == 0) nrm[v] = make_float2(0.f, 0.f);
+      if (v < npad && lane == 0) nrm[v] = make_float2(0.f, 0.f);
       continue;
     }
     const float *x = P + v * dim;
@@ -1016,7 +1258,7 @@ euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_
     const int se = tc::Kind<KIND>::F16 ? tc::f16_scale_exp(amax) : 0;
     const float scale = tc::exp2i(se);
     if (lane == 0) nrm[v] = make_float2(hi + lo, tc::exp2i(-se));
-    write_row_planes<KIND>(dim, kpad, plane, Z + v * kpad, [&](int64_t k0, float (&c)[4]) {
+    auto val = [&](int64_t k0, float (&c)[4]) {
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const int64_t k = k0 + e;
@@ -1027,7 +1269,32 @@ euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_
           c[e] = 0.f;
         }
       }
-    });
+    };
+    write_row_planes<KIND>(dim, kpad, plane, Z + v * kpad, val);
+    if (ZB) write_row_planes<KIND>(dim, kpad, planeB, ZB + lines.pos(v) * kpad, val);
+  }
+}
+
+// Exact distances of the near-zero pairs the aligned-lines Gram kernel
+// listed: block r takes region r (counts[r] pairs (row, column), row >
+// column), 16 pairs per round (8 lanes each), and overwrites their dist
+// entries.  Runs after the Gram kernel on the same stream.
+__global__ void __launch_bounds__(128)
+euclid_fixup_kernel(const float *__restrict__ pts, int64_t n, int64_t dim, int vec4,
+                    float *__restrict__ out, const int2 *__restrict__ pairs,
+                    const int *__restrict__ counts, int cap) {
+  const int lane = threadIdx.x & 31, sub = lane & 7;
+  const int slot0 = (threadIdx.x >> 3);  // 0 .. 15
+  const int2 *list = pairs + int64_t(blockIdx.x) * cap;
+  int cnt = counts[blockIdx.x];
+  cnt = cnt < 0 ? 0 : (cnt > cap ? cap : cnt);
+  for (int b = 0; b < cnt; b += 16) {
+    const int idx = b + slot0;
+    const bool act = idx < cnt;
+    const int2 e = list[act ? idx : b];
+    const bool ok = act && e.y >= 0 && e.y < e.x && int64_t(e.x) < n;
+    const float d2 = pair_sq_dist(pts, dim, vec4, ok ? e.x : 0, ok ? e.y : 0, sub);
+    if (ok && sub == 0) out[n * e.y - int64_t(e.y) * (e.y + 1) / 2 - e.y - 1 + e.x] = sqrtf(d2);
   }
 }
 
@@ -1096,6 +1363,25 @@ int err_word(int **p) {
   return GT_OK;
 }
 
+// Launches the persistent kernel over `ntiles` tiles of work source w.
+template <int KIND, int BK, bool CHUNKED, class W>
+int launch_work(const W &w, int64_t ntiles, int64_t ckb, const char *prof_name,
+                cudaStream_t s) {
+  using C = TcCfg<KIND, BK, !CHUNKED>;
+  if (ntiles == 0) return GT_OK;
+  int *err = nullptr;
+  GT_TRY(err_word(&err));
+  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  auto kern = gram_tc_kernel<KIND, BK, CHUNKED, W>;
+  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+  const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
+  ProfScope prof(prof_name, s);
+  kern<<<unsigned(grid), C::THREADS, C::SMEM, s>>>(w, ckb, err);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
 template <int KIND, int BK, bool CHUNKED, class Fin>
 int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
                 int mode, int64_t ckb, const Fin &fin, const char *prof_name,
@@ -1113,18 +1399,20 @@ int launch_gram(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t 
                                              (long long)w.ts.ntiles);
   w.nk = kpad / BK;
   w.fin = fin;
-  if (w.ts.ntiles == 0) return GT_OK;
-  int *err = nullptr;
-  GT_TRY(err_word(&err));
-  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  auto kern = gram_tc_kernel<KIND, BK, CHUNKED, W>;
-  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-  const int64_t grid = w.ts.ntiles < sm_count() ? w.ts.ntiles : sm_count();
-  ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), C::THREADS, C::SMEM, s>>>(w, ckb, err);
-  count_launch();
-  GT_CUDA(cudaGetLastError());
-  return GT_OK;
+  return launch_work<KIND, BK, CHUNKED>(w, w.ts.ntiles, ckb, prof_name, s);
+}
+
+// Pending near-zero pairs per epilogue warp that the aligned-lines kernel
+// lists for euclid_fixup_kernel (8 KB x 8 per warp); beyond them a warp
+// recomputes its pairs itself.
+constexpr int64_t kPairCap = 8192;
+
+// The aligned-lines tiling pays about 8192 / n extra tiles on the diagonal;
+// it is used from 32768 points on (GT_EUCLID_LINES=1 / 0 forces it on / off).
+bool use_dist_lines(int64_t n) {
+  const char *e = std::getenv("GT_EUCLID_LINES");
+  if (e && *e) return std::atoi(e) != 0;
+  return n >= 32768;
 }
 
 int tc_config() {
@@ -1238,14 +1526,23 @@ template <int KIND>
 int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
                    float tau, cudaStream_t st) {
   constexpr int NS = tc::Kind<KIND>::NSPLIT;
+  constexpr bool F16 = tc::Kind<KIND>::F16;
   const int64_t kpad = cdiv(dim, kKPad) * kKPad;
   const int64_t npad = cdiv(n, kBN) * kBN;
   const int64_t nblk = cdiv(n, kColsumPoints);
+  DistLines lines{};
+  LineTiles lt{};
+  const bool aligned = layout == GT_LAYOUT_DIST && use_dist_lines(n) &&
+                       make_dist_lines(n, reinterpret_cast<uintptr_t>(d_out), &lines) &&
+                       make_line_tiles(n, &lt);
+  // permuted column operand of the aligned lines: 8192 rows per super-block
+  const int64_t npb = aligned ? lt.npb : 0;
   void *pz = nullptr, *pn = nullptr, *pp = nullptr;
-  GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n) * size_t(kpad) * 2, &pz));
+  GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n + npb) * size_t(kpad) * 2, &pz));
   GT_TRY(ws_get(WS_SCRATCH2, size_t(npad) * sizeof(float2), &pn));
   GT_TRY(ws_get(WS_SCRATCH3, size_t(nblk) * size_t(dim) * 8 + size_t(dim) * sizeof(float2), &pp));
   auto *z = static_cast<uint16_t *>(pz);
+  auto *zb = aligned ? z + size_t(NS) * size_t(n) * size_t(kpad) : nullptr;
   auto *nrm = static_cast<float2 *>(pn);
   auto *partial = static_cast<double *>(pp);
   auto *mean2 = reinterpret_cast<float2 *>(partial + nblk * dim);
@@ -1255,16 +1552,41 @@ int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int
     dim3 cg((unsigned)cdiv(dim, 32), (unsigned)nblk, 1u);
     euclid_colsum_kernel<<<cg, 256, 0, st>>>(d_pts, n, dim, partial);
     euclid_mean_kernel<<<unsigned(dim), 256, 0, st>>>(partial, nblk, dim, n, mean2);
-    int64_t g = cdiv(npad * 32, 256);
+    const int64_t slots = npad > npb ? npad : npb;
+    int64_t g = cdiv(slots * 32, 256);
     if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
     euclid_split_kernel<KIND><<<unsigned(g), 256, 0, st>>>(d_pts, n, npad, dim, kpad, mean2, z,
-                                                           nrm);
+                                                           nrm, zb, npb, lines);
     count_launch(3);
     GT_CUDA(cudaGetLastError());
   }
   const int vec4 = (reinterpret_cast<uintptr_t>(d_pts) & 15u) == 0 && (dim & 3) == 0;
-  EuclidFinish fin{nrm, d_pts, d_out, n, dim, layout, tau, vec4};
-  return launch_gram<KIND, 32, false>(z, n, z, n, kpad, kLower, 0, fin, "euclid_gram", st);
+  if (!aligned) {
+    EuclidFinish fin{nrm, d_pts, d_out, n, dim, layout, tau, vec4};
+    return launch_gram<KIND, 32, false>(z, n, z, n, kpad, kLower, 0, fin, "euclid_gram", st);
+  }
+  using C = TcCfg<KIND, 32, true>;
+  const int64_t grid = int64_t(lt.ntiles) < sm_count() ? int64_t(lt.ntiles) : sm_count();
+  const int64_t regions = grid * C::EPI;
+  void *pl = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH1, size_t(regions) * (size_t(kPairCap) * sizeof(int2) + sizeof(int)), &pl));
+  auto *pairs = static_cast<int2 *>(pl);
+  auto *counts = reinterpret_cast<int *>(pairs + regions * kPairCap);
+  GT_CUDA(cudaMemsetAsync(counts, 0, size_t(regions) * sizeof(int), st));
+  EuclidLineWork w;
+  GT_TRY(make_plane_map(&w.ma, z, n, kpad, NS, kBM, 32, F16));
+  GT_TRY(make_plane_map(&w.mb, zb, npb, kpad, NS, kBN, 32, F16));
+  w.nk = kpad / 32;
+  w.lt = lt;
+  w.fin = EuclidLineFinish{nrm, d_pts, d_out, n, dim, tau, vec4, lines, pairs, counts,
+                           int(kPairCap), C::EPI};
+  GT_TRY((launch_work<KIND, 32, false>(w, int64_t(lt.ntiles), 0, "euclid_gram", st)));
+  ProfScope prof("euclid_fixup", st);
+  euclid_fixup_kernel<<<unsigned(regions), 128, 0, st>>>(d_pts, n, dim, vec4, d_out, pairs, counts,
+                                                        int(kPairCap));
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
 }
 
 }  // namespace

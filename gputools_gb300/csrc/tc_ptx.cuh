@@ -53,6 +53,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: a waiting thread sleeps until the phase
+// completes or `hint_ns` passes, instead of polling and taking issue slots
+// from the warps that do the work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+constexpr uint32_t kSleepHintNs = 100000;  // 0.1 ms: well inside every wait limit
+
 // Waits for the phase of `bar` with the given parity.  Gives up (returns
 // false) after `limit_ns` or as soon as *abort becomes non-zero, so a kernel
 // never spins forever on a barrier that will not complete.
@@ -61,7 +79,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, kSleepHintNs)) return true;
     if (*abort) return false;
     if (globaltimer_ns() - t0 > limit_ns) return false;
   }
