@@ -550,32 +550,42 @@ struct EuclidFinish {
 // staging tile, which this finish does not otherwise use: point ids, and the
 // offsets base(c) - base(c_first) of their dist columns from the warp's first
 // column (64 columns of one class span at most 4096 points, so the offsets
-// fit 32 bits), and the base of that first column.  The pending pairs follow
-// them in the staging tile.
+// fit 32 bits), and the base of that first column, all copied from the
+// tables the split kernel writes.  The pending pairs follow them in the
+// staging tile.
 struct EuclidLineFinish {
+  static constexpr int kCols = kEuclidCols;  // columns per epilogue warp
   const float2 *nrm;  // per point {|c|^2, 2^-s}
+  const int4 *colinfo;       // per operand column: point, base offset in its group, norm, scale
+  const int64_t *groupbase;  // per kCols operand columns: base of the group's first point
   const float *pts;
   float *out;
   int64_t n, dim;
   float tau;
   int vec4;
-  DistLines lines;
   int2 *pair_list;    // [CTA][epilogue warp][pair_cap] pending pairs (row, column)
   int *pair_count;    // [CTA][epilogue warp] pairs listed, written at the end
   int pair_cap, epi;
 
+  // the warp's staging tile: point ids, offsets, pending pairs, the first
+  // column's base, the columns' {norm, scale}
   __device__ __forceinline__ static int *col_ids(const EpiCtx &ctx) {
     return reinterpret_cast<int *>(ctx.wsm);
   }
   __device__ __forceinline__ static int *col_offs(const EpiCtx &ctx) {
-    return reinterpret_cast<int *>(ctx.wsm) + 64;
+    return reinterpret_cast<int *>(ctx.wsm) + kCols;
   }
   __device__ __forceinline__ static int2 *pairs(const EpiCtx &ctx) {
-    return reinterpret_cast<int2 *>(ctx.wsm + 128);  // kEuclidList entries
+    return reinterpret_cast<int2 *>(ctx.wsm + 2 * kCols);  // kEuclidList entries
   }
   __device__ __forceinline__ static int64_t *first_base(const EpiCtx &ctx) {
-    return reinterpret_cast<int64_t *>(ctx.wsm + 256);
+    return reinterpret_cast<int64_t *>(ctx.wsm + 2 * kCols + 2 * kEuclidList);
   }
+  __device__ __forceinline__ static float2 *col_nrm(const EpiCtx &ctx) {
+    return reinterpret_cast<float2 *>(ctx.wsm + 2 * kCols + 2 * kEuclidList + 8);
+  }
+  static_assert(2 * kCols + 2 * kEuclidList + 8 + 2 * kCols <= kEpiTileFloats,
+                "the columns fit the staging tile");
   // this warp's region of the global pair list (epilogue warps follow the
   // producer and MMA warps)
   __device__ __forceinline__ int64_t region_index() const {
@@ -587,16 +597,16 @@ struct EuclidLineFinish {
   __device__ void begin_tile(int64_t r, EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
     ctx.me = (r >= 0 && r < n) ? nrm[r] : make_float2(0.f, 0.f);
-    const uint32_t p0 = uint32_t(ctx.col0);
-    const int64_t b0 = base(lines.point32(p0));
-    if (lane == 0) *first_base(ctx) = b0;
+    if (lane == 0) *first_base(ctx) = groupbase[ctx.col0 / kCols];
     int *cid = col_ids(ctx);
     int *cof = col_offs(ctx);
-    for (int k = lane; k < kEuclidCols; k += 32) {
-      const int32_t c = lines.point32(p0 + uint32_t(k));
-      cid[k] = c;
-      cof[k] = c < n ? int(base(c) - b0) : 0;
-      ctx.cnrm()[k] = c < n ? nrm[c] : make_float2(0.f, 0.f);
+    float2 *cn = col_nrm(ctx);
+#pragma unroll
+    for (int k = lane; k < kCols; k += 32) {
+      const int4 ci = colinfo[ctx.col0 + k];
+      cid[k] = ci.x;
+      cof[k] = ci.y;
+      cn[k] = make_float2(__int_as_float(ci.z), __int_as_float(ci.w));
     }
     __syncwarp();
   }
@@ -607,7 +617,7 @@ struct EuclidLineFinish {
     const int off = int(c0 - ctx.col0);
     const int *cid = col_ids(ctx) + off;
     const int4 *cof4 = reinterpret_cast<const int4 *>(col_offs(ctx) + off);
-    const float4 *cv4 = reinterpret_cast<const float4 *>(ctx.cnrm() + off);
+    const float4 *cv4 = reinterpret_cast<const float4 *>(col_nrm(ctx) + off);
     const int64_t rbase = r - lane;
     const float na = ctx.me.x, ra = -2.f * ctx.me.y;
     float *const orow = out + (*first_base(ctx) + r);
@@ -746,7 +756,6 @@ struct TcCfg {
   static constexpr int EPI = LISTS ? 16 : 8;                 // epilogue warps
   static constexpr int THREADS = 64 + 32 * EPI;              // + producer and MMA warps
   static constexpr int COLS = 4 * kBN / EPI;                 // columns per epilogue warp
-  static constexpr int NBLK = COLS / 32;                     // 32 x 32 blocks per warp
   static constexpr int ROW_BYTES = BK * 2;                // 128 or 64
   static constexpr int A_TILE = kBM * BK * 2;
   static constexpr int B_TILE = kBN * BK * 2;
@@ -803,6 +812,7 @@ struct SingleWork {
     ref.prob = 0;
     return true;
   }
+  static constexpr bool kPrefetch = false;
   __device__ const Fin &finish(const TileRef &) const { return fin; }
   __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
   __device__ void prefetch() const {
@@ -852,32 +862,74 @@ struct PearsonBatchWork {
     ref.prob = pi;
     return true;
   }
+  static constexpr bool kPrefetch = false;
   __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
   __device__ void drain(EpiCtx &) const {}
   __device__ void prefetch() const {}
 };
 
-// The dist layout in aligned lines (DistLines, LineTiles).
+// The dist layout in aligned lines (DistLines, LineTiles): the tiles' origins
+// come from a table, so that a lookup is one load the cursor issues a tile
+// ahead.
 struct EuclidLineWork {
   CUtensorMap ma, mb;
   int64_t nk;
-  LineTiles lt;
+  int64_t ntiles;
+  const int2 *tiles;  // (row0, col0) per tile, line_tile_table_kernel
   EuclidLineFinish fin;
   __device__ bool tile(int64_t cursor, TileRef &ref) const {
     const int64_t u = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
-    if (u >= int64_t(lt.ntiles)) return false;
-    lt.decode(uint32_t(u), ref.row0, ref.col0);
+    if (u >= ntiles) return false;
+    const int2 t = tiles[u];
+    ref.row0 = t.x;
+    ref.col0 = t.y;
     ref.ma = &ma;
     ref.mb = &mb;
     ref.nk = nk;
     ref.prob = 0;
     return true;
   }
+  static constexpr bool kPrefetch = true;
   __device__ const EuclidLineFinish &finish(const TileRef &) const { return fin; }
   __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
   __device__ void prefetch() const {
     tc::prefetch_tensormap(&ma);
     tc::prefetch_tensormap(&mb);
+  }
+};
+
+// Walks this CTA's tiles first, first + step, ... of a work source.  With
+// Work::kPrefetch it looks up the next tile while the current one is
+// processed (the lookup is a global load); else it looks each tile up when it
+// is reached, holding no second TileRef.
+template <class Work, bool PREFETCH = Work::kPrefetch>
+struct TileCursor {
+  const Work &work;
+  TileRef nref;
+  int64_t cur;
+  int step;
+  bool have;
+  __device__ TileCursor(const Work &w, int first, int stp) : work(w), cur(first), step(stp) {
+    have = work.tile(cur, nref);
+  }
+  __device__ bool next(TileRef &ref) {
+    if (!have) return false;
+    ref = nref;
+    cur += step;
+    have = work.tile(cur, nref);
+    return true;
+  }
+};
+template <class Work>
+struct TileCursor<Work, false> {
+  const Work &work;
+  int64_t cur;
+  int step;
+  __device__ TileCursor(const Work &w, int first, int stp) : work(w), cur(first), step(stp) {}
+  __device__ bool next(TileRef &ref) {
+    const bool got = work.tile(cur, ref);
+    cur += step;
+    return got;
   }
 };
 
@@ -926,7 +978,8 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
       // ------------------------------------------------ TMA producer
       int64_t it = 0;
       TileRef ref;
-      for (int64_t cur = 0; !*abort_flag && work.tile(cur, ref); cur++) {
+      TileCursor<Work> tiles(work, 0, 1);
+      while (!*abort_flag && tiles.next(ref)) {
         for (int64_t kb = 0; kb < ref.nk; kb++, it++) {
           const int s = int(it % C::STAGES);
           const uint32_t use = uint32_t(it / C::STAGES);
@@ -962,7 +1015,8 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
       int64_t it = 0, cc = 0;
       bool ok = true;
       TileRef ref;
-      for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
+      TileCursor<Work> tiles(work, 0, 1);
+      while (ok && tiles.next(ref)) {
         const int64_t ck = CHUNKED ? ckb : ref.nk;
         const int64_t nch = (ref.nk + ck - 1) / ck;
         for (int64_t ch = 0; ch < nch && ok; ch++, cc++) {
@@ -1016,10 +1070,11 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
     ctx.wsm = mine;
     ctx.nlist = 0;
     ctx.gcount = 0;
-    int64_t cc = 0;
+    int64_t cc = 0;  // accumulator use counter: buffer cc & 1, phase cc >> 1
     bool ok = true;
     TileRef ref;
-    for (int64_t cur = 0; ok && work.tile(cur, ref); cur++) {
+    TileCursor<Work> tiles(work, 0, 1);
+    while (ok && tiles.next(ref)) {
       const auto &fin = work.finish(ref);
       const int64_t r = ref.row0 + q * 32 + lane;
       const int64_t col = ref.col0 + part * C::COLS;
@@ -1074,7 +1129,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
         const uint32_t tb =
             tmem_base + uint32_t(buf * kBN + part * C::COLS) + (uint32_t(q * 32) << 16);
 #pragma unroll 1
-        for (int i = 0; i < C::NBLK; i++) {
+        for (int i = 0; i < C::COLS / 32; i++) {
           float g[32];
           tc::tmem_ld32(tb + uint32_t(32 * i), g);
           fin(r, col + 32 * i, g, ctx);
@@ -1220,13 +1275,15 @@ euclid_mean_kernel(const double *__restrict__ partial, int64_t nblk, int64_t dim
 // squared norm (compensated), the largest magnitude (f16x3 scale), then the
 // planes.  nrm[v] = {|c|^2, 2^-s}; rows n .. npad-1 of nrm are zeroed.  With
 // ZB, the planes also go to row lines.pos(v) of the permuted column operand
-// (npb rows), whose padding rows are zeroed.
+// (npb rows), whose padding rows are zeroed, and the column tables of the
+// aligned-lines finish are written.
 template <int KIND>
 __global__ void __launch_bounds__(256)
 euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_t dim,
                     int64_t kpad, const float2 *__restrict__ mean2, uint16_t *__restrict__ Z,
                     float2 *__restrict__ nrm, uint16_t *__restrict__ ZB, int64_t npb,
-                    const DistLines lines) {
+                    const DistLines lines, int4 *__restrict__ colinfo,
+                    int64_t *__restrict__ groupbase) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
@@ -1234,9 +1291,15 @@ euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_
   const int64_t plane = n * kpad, planeB = npb * kpad;
   const int64_t nslot = npad > npb ? npad : npb;
   for (int64_t v = warp; v < nslot; v += nwarps) {
-    // padding rows of the permuted column operand are zero
-    if (ZB && v < npb && lines.point(v) >= n)
+    // padding rows of the permuted column operand are zero, their column
+    // entries the sentinel point n
+    if (ZB && v < npb && lines.point(v) >= n) {
       write_row_planes<KIND>(0, kpad, planeB, ZB + v * kpad, [](int64_t, float (&)[4]) {});
+      if (lane == 0) {
+        colinfo[v] = make_int4(int(n), 0, 0, 0);
+        if ((v % EuclidLineFinish::kCols) == 0) groupbase[v / EuclidLineFinish::kCols] = 0;
+      }
+    }
     if (v >= n) {
       if (v < npad && lane == 0) nrm[v] = make_float2(0.f, 0.f);
       continue;
@@ -1271,30 +1334,95 @@ euclid_split_kernel(const float *__restrict__ P, int64_t n, int64_t npad, int64_
       }
     };
     write_row_planes<KIND>(dim, kpad, plane, Z + v * kpad, val);
-    if (ZB) write_row_planes<KIND>(dim, kpad, planeB, ZB + lines.pos(v) * kpad, val);
+    if (ZB) {
+      const int64_t p = lines.pos(v);
+      write_row_planes<KIND>(dim, kpad, planeB, ZB + p * kpad, val);
+      if (lane == 0) {
+        // the dist column base of v, relative to its column group's first
+        // point (the group's smallest)
+        constexpr int64_t G = EuclidLineFinish::kCols;
+        const int64_t c0 = lines.point(p / G * G);
+        const int64_t b = n * v - v * (v + 1) / 2 - v - 1;
+        const int64_t b0 = n * c0 - c0 * (c0 + 1) / 2 - c0 - 1;
+        colinfo[p] = make_int4(int(v), int(b - b0), __float_as_int(hi + lo),
+                               __float_as_int(tc::exp2i(-se)));
+        if (p % G == 0) groupbase[p / G] = b0;
+      }
+    }
   }
+}
+
+// (row0, col0) of every aligned-lines tile.
+__global__ void __launch_bounds__(256)
+line_tile_table_kernel(const LineTiles lt, int2 *__restrict__ tab) {
+  const uint32_t u = blockIdx.x * 256u + threadIdx.x;
+  if (u >= lt.ntiles) return;
+  int64_t r0, c0;
+  lt.decode(u, r0, c0);
+  tab[u] = make_int2(int(r0), int(c0));
 }
 
 // Exact distances of the near-zero pairs the aligned-lines Gram kernel
 // listed: block r takes region r (counts[r] pairs (row, column), row >
-// column), 16 pairs per round (8 lanes each), and overwrites their dist
-// entries.  Runs after the Gram kernel on the same stream.
-__global__ void __launch_bounds__(128)
+// column) and overwrites their dist entries, 64 pairs per round (4 lanes
+// each).  Every lane issues all its coordinate loads of a batch before the
+// first use, and the next round's entries load during this round.  Runs
+// after the Gram kernel on the same stream.
+constexpr int kFixupThreads = 256;
+__global__ void __launch_bounds__(kFixupThreads)
 euclid_fixup_kernel(const float *__restrict__ pts, int64_t n, int64_t dim, int vec4,
                     float *__restrict__ out, const int2 *__restrict__ pairs,
                     const int *__restrict__ counts, int cap) {
-  const int lane = threadIdx.x & 31, sub = lane & 7;
-  const int slot0 = (threadIdx.x >> 3);  // 0 .. 15
+  constexpr int PER_ROUND = kFixupThreads / 4;
+  const unsigned FULLM = 0xffffffffu;
+  const int sub = threadIdx.x & 3, slot = threadIdx.x >> 2;
   const int2 *list = pairs + int64_t(blockIdx.x) * cap;
   int cnt = counts[blockIdx.x];
   cnt = cnt < 0 ? 0 : (cnt > cap ? cap : cnt);
-  for (int b = 0; b < cnt; b += 16) {
-    const int idx = b + slot0;
-    const bool act = idx < cnt;
-    const int2 e = list[act ? idx : b];
+  if (cnt == 0) return;
+  int2 e = list[slot < cnt ? slot : 0];
+  for (int b = 0; b < cnt; b += PER_ROUND) {
+    const bool act = b + slot < cnt;
+    const int nb = b + PER_ROUND;
+    const int2 en = nb + slot < cnt ? list[nb + slot] : e;
     const bool ok = act && e.y >= 0 && e.y < e.x && int64_t(e.x) < n;
-    const float d2 = pair_sq_dist(pts, dim, vec4, ok ? e.x : 0, ok ? e.y : 0, sub);
-    if (ok && sub == 0) out[n * e.y - int64_t(e.y) * (e.y + 1) / 2 - e.y - 1 + e.x] = sqrtf(d2);
+    const int64_t i = ok ? e.x : 0, j = ok ? e.y : 0;
+    const float *pa = pts + i * dim, *pb = pts + j * dim;
+    FloatPairSum acc;
+    float res = 0.f;
+    if (vec4) {
+      const float4 *a4 = reinterpret_cast<const float4 *>(pa);
+      const float4 *b4 = reinterpret_cast<const float4 *>(pb);
+      const int64_t d4 = dim >> 2;
+      for (int64_t k0 = sub; k0 < d4; k0 += 32) {
+        float4 x[8], y[8];
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+          const int64_t k = k0 + 4 * it;
+          x[it] = k < d4 ? a4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+          y[it] = k < d4 ? b4[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+          sq_add(x[it].x - y[it].x, acc, res);
+          sq_add(x[it].y - y[it].y, acc, res);
+          sq_add(x[it].z - y[it].z, acc, res);
+          sq_add(x[it].w - y[it].w, acc, res);
+        }
+      }
+    } else {
+      for (int64_t k = sub; k < dim; k += 4) sq_add(pa[k] - pb[k], acc, res);
+    }
+    float hi = acc.hi, lo = acc.lo + res;
+#pragma unroll
+    for (int o = 2; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(FULLM, hi, o), ol = __shfl_xor_sync(FULLM, lo, o);
+      const float t = hi + oh, bp = t - hi;
+      lo = (lo + ol) + ((hi - (t - bp)) + (oh - bp));
+      hi = t;
+    }
+    if (ok && sub == 0) out[n * j - j * (j + 1) / 2 - j - 1 + i] = sqrtf(hi + lo);
+    e = en;
   }
 }
 
@@ -1539,7 +1667,16 @@ int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int
   const int64_t npb = aligned ? lt.npb : 0;
   void *pz = nullptr, *pn = nullptr, *pp = nullptr;
   GT_TRY(ws_get(WS_SCRATCH0, size_t(NS) * size_t(n + npb) * size_t(kpad) * 2, &pz));
-  GT_TRY(ws_get(WS_SCRATCH2, size_t(npad) * sizeof(float2), &pn));
+  // nrm, then (aligned lines) the column tables and the tile table
+  const size_t nrm_bytes = size_t(npad) * sizeof(float2);
+  const size_t ci_bytes = size_t(npb) * sizeof(int4);
+  const size_t gb_bytes = size_t(npb / EuclidLineFinish::kCols) * 8;
+  const size_t tab_bytes = aligned ? size_t(lt.ntiles) * sizeof(int2) : 0;
+  GT_TRY(ws_get(WS_SCRATCH2, nrm_bytes + ci_bytes + gb_bytes + tab_bytes, &pn));
+  auto *colinfo = reinterpret_cast<int4 *>(static_cast<char *>(pn) + nrm_bytes);
+  auto *groupbase = reinterpret_cast<int64_t *>(static_cast<char *>(pn) + nrm_bytes + ci_bytes);
+  auto *tiletab =
+      reinterpret_cast<int2 *>(static_cast<char *>(pn) + nrm_bytes + ci_bytes + gb_bytes);
   GT_TRY(ws_get(WS_SCRATCH3, size_t(nblk) * size_t(dim) * 8 + size_t(dim) * sizeof(float2), &pp));
   auto *z = static_cast<uint16_t *>(pz);
   auto *zb = aligned ? z + size_t(NS) * size_t(n) * size_t(kpad) : nullptr;
@@ -1556,8 +1693,13 @@ int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int
     int64_t g = cdiv(slots * 32, 256);
     if (g > int64_t(sm_count()) * 16) g = int64_t(sm_count()) * 16;
     euclid_split_kernel<KIND><<<unsigned(g), 256, 0, st>>>(d_pts, n, npad, dim, kpad, mean2, z,
-                                                           nrm, zb, npb, lines);
+                                                           nrm, zb, npb, lines, colinfo,
+                                                           groupbase);
     count_launch(3);
+    if (aligned) {
+      line_tile_table_kernel<<<unsigned(cdiv(int64_t(lt.ntiles), 256)), 256, 0, st>>>(lt, tiletab);
+      count_launch();
+    }
     GT_CUDA(cudaGetLastError());
   }
   const int vec4 = (reinterpret_cast<uintptr_t>(d_pts) & 15u) == 0 && (dim & 3) == 0;
@@ -1577,12 +1719,13 @@ int euclid_tc_kind(const float *d_pts, int64_t n, int64_t dim, float *d_out, int
   GT_TRY(make_plane_map(&w.ma, z, n, kpad, NS, kBM, 32, F16));
   GT_TRY(make_plane_map(&w.mb, zb, npb, kpad, NS, kBN, 32, F16));
   w.nk = kpad / 32;
-  w.lt = lt;
-  w.fin = EuclidLineFinish{nrm, d_pts, d_out, n, dim, tau, vec4, lines, pairs, counts,
-                           int(kPairCap), C::EPI};
+  w.ntiles = int64_t(lt.ntiles);
+  w.tiles = tiletab;
+  w.fin = EuclidLineFinish{nrm, colinfo, groupbase, d_pts, d_out, n, dim, tau, vec4, pairs,
+                           counts, int(kPairCap), C::EPI};
   GT_TRY((launch_work<KIND, 32, false>(w, int64_t(lt.ntiles), 0, "euclid_gram", st)));
   ProfScope prof("euclid_fixup", st);
-  euclid_fixup_kernel<<<unsigned(regions), 128, 0, st>>>(d_pts, n, dim, vec4, d_out, pairs, counts,
+  euclid_fixup_kernel<<<unsigned(regions), kFixupThreads, 0, st>>>(d_pts, n, dim, vec4, d_out, pairs, counts,
                                                         int(kPairCap));
   count_launch();
   GT_CUDA(cudaGetLastError());

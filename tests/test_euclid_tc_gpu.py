@@ -165,3 +165,27 @@ def test_lines_super_blocks_sampled(gpu, oracle_mod, path, monkeypatch, n, mode)
         err = np.abs(got - w) / np.maximum(np.abs(w), 1e-30)
         err[(w == 0) & (got == 0)] = 0.0
         assert err.max() <= RTOL, (int(s), float(err.max()), int(other[err.argmax()]))
+
+
+def test_lines_pair_list_overflow(gpu, oracle_mod, path, monkeypatch):
+    """A single tight cluster of 12000 points: every pair is recomputed, more
+    than a warp's region of the pair list holds, so the epilogue warps also
+    recompute pairs themselves; sampled points against the oracle."""
+    import torch
+    import gputools_gb300 as g
+    monkeypatch.setenv("GT_EUCLID_LINES", "1")
+    rng = np.random.default_rng(31)
+    n = 12000
+    pts = (3.0 + 1e-4 * rng.standard_normal((n, 16))).astype(np.float32)
+    d = g.distances_device(torch.from_numpy(pts).cuda(), "euclidean", layout="dist")
+    samples = np.unique(np.concatenate([[0, 1, n - 1, 8191, 8192], rng.integers(0, n, 7)]))
+    want = oracle_mod.dist(pts, "euclidean", 2.0, b=pts[samples])
+    xs = np.arange(n, dtype=np.int64)
+    for k, s in enumerate(samples):
+        other = xs[xs != s]
+        idx = np.where(other < s, dist_base(n, other) + s, dist_base(n, s) + other)
+        got = d[torch.from_numpy(idx).cuda()].cpu().numpy().astype(np.float64)
+        w = want[k, other]
+        err = np.abs(got - w) / np.maximum(np.abs(w), 1e-30)
+        err[(w == 0) & (got == 0)] = 0.0
+        assert err.max() <= RTOL, (int(s), float(err.max()), int(other[err.argmax()]))
