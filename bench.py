@@ -483,11 +483,13 @@ def run_case(args):
     if args.case == "pearson":
         z = rng.standard_normal((p, n), dtype=np.float32)
         X = np.exp(z + np.float32(5.0), dtype=np.float32) + rng.uniform(0, 1e3, (p, 1)).astype(np.float32)
+        if args.nan_frac > 0:
+            X[rng.random(X.shape) < args.nan_frac] = np.nan
         dX = torch.from_numpy(X).to(dev)
         outs = [torch.empty((p, p), dtype=torch.float32, device=dev) for _ in range(3)]
-        fn = lambda: _lib.check(lib.gt_pmcc_device(0, vp(dX), p, vp(dX), p, n, vp(outs[0]),
+        fn = lambda: _lib.check(lib.gt_pmcc_device(args.use, vp(dX), p, vp(dX), p, n, vp(outs[0]),
                                                    vp(outs[1]), vp(outs[2]), sptr))
-        names = ("pearson_prologue", "pearson_gram")
+        names = ("pearson_prologue", "pearson_gram", "pearson_pairwise")
     elif args.case == "euclid":
         centres = rng.standard_normal((1000, 128), dtype=np.float32)
         pts = centres[rng.integers(0, 1000, p)] + np.float32(1e-3) * rng.standard_normal((p, 128), dtype=np.float32)
@@ -519,6 +521,7 @@ def run_case(args):
     torch.cuda.synchronize()
     lib.gt_profile_enable(0)
     res = {"case": args.case, "p": p, "n": n, "path": args.path, "layout": args.layout,
+           "use": args.use, "nan_frac": args.nan_frac,
            "ms_per_step": e0.elapsed_time(e1) / args.steps,
            "bk": os.environ.get("GT_TC_BK", "32"), "chunk": os.environ.get("GT_TC_CHUNK", "256")}
     for nm in names:
@@ -694,6 +697,10 @@ def main():
     ap.add_argument("--n", type=int, default=4096, help="--case: observations")
     ap.add_argument("--path", default="bf16x3", help="--case: gram path")
     ap.add_argument("--layout", default="dist", help="--case euclid: full or dist")
+    ap.add_argument("--use", type=int, default=0,
+                    help="--case pearson: 0 everything, 1 pairwise.complete.obs")
+    ap.add_argument("--nan-frac", type=float, default=0.0,
+                    help="--case pearson: fraction of values set to NaN")
     args = ap.parse_args()
     if args.case:
         run_case(args)

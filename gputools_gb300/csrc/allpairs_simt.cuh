@@ -31,6 +31,7 @@ struct SimtArgs {
   int64_t ldr, ldc, nr, nc, K;
   int symmetric;   // R == C: only tiles ti <= tj, mirror off-diagonal tiles
   int vec_ok;      // strides and base pointers allow float4 loads
+  const int *run_if = nullptr;  // when set, the kernel does nothing unless *run_if != 0
 };
 
 // Loads one BK slab of `rows` rows into registers (float4 per chunk).
@@ -79,6 +80,7 @@ template <class Op, class Out, int TM, int TN>
 __global__ void __launch_bounds__(kSimtThreads)
 allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   constexpr int BM = 16 * TM, BN = 16 * TN, NA = Op::NACC;
+  if (a.run_if && *a.run_if == 0) return;  // a gated launch whose gate is closed
   const int ti = blockIdx.y, tj = blockIdx.x;
   if (a.symmetric && ti > tj) return;
   const int64_t row0 = int64_t(ti) * BM, col0 = int64_t(tj) * BN;

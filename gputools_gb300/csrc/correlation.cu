@@ -12,9 +12,11 @@
 //    z = (x - mean) / ||x - mean||, so r(x, y) = <z_x, z_y>;
 //  * "everything": the Gram contraction runs on tcgen05 tensor cores
 //    (split bf16, gram_tc.cu) or, for GT_GRAM_FP32, on the CUDA-core engine;
-//  * "pairwise.complete.obs": the CUDA-core engine accumulates, per pair, the
-//    six masked sums (count, sums, squares, cross) of the standardised values
-//    and the epilogue forms r in FP64;
+//  * "pairwise.complete.obs": on inputs without a missing value it is the
+//    "everything" result, so the tensor-core path runs (gated on a device
+//    NaN flag); otherwise the CUDA-core engine accumulates, per pair, the six
+//    masked sums (count, sums, squares, cross) of the standardised values and
+//    the epilogue forms r in FP64;
 //  * pairs, r and the t-score (hostSignif's rule, in float as the reference
 //    evaluates it) are written by the same epilogue; cor(x) computes each
 //    unordered pair once and mirrors it.
@@ -34,7 +36,8 @@ constexpr int kStatThreads = 256;  // eight variables per CTA, one warp each
 
 __global__ void __launch_bounds__(kStatThreads)
 colstats_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int use,
-                ColStats *__restrict__ out) {
+                ColStats *__restrict__ out, const int *run_if = nullptr) {
+  if (run_if && *run_if == 0) return;  // a gated launch whose gate is closed
   const int64_t v = (int64_t(blockIdx.x) * kStatThreads + threadIdx.x) >> 5;
   if (v >= nvar) return;  // whole warps
   const ColStats st = colstats_warp(X + v * n, n, use);
@@ -47,7 +50,9 @@ colstats_kernel(const float *__restrict__ X, int64_t nvar, int64_t n, int use,
 // it is NaN.
 __global__ void normalize_f32_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
                                      int64_t ldz, const ColStats *__restrict__ st, int use,
-                                     float padv, float *__restrict__ Z) {
+                                     float padv, float *__restrict__ Z,
+                                     const int *run_if = nullptr) {
+  if (run_if && *run_if == 0) return;  // a gated launch whose gate is closed
   const int64_t v = blockIdx.x;
   const ColStats s = st[v];
   const Centerer cen(s);
@@ -151,6 +156,15 @@ __global__ void differ_kernel(const uint32_t *__restrict__ a, const uint32_t *__
   if (__syncthreads_or(local) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
+// flag |= 1 if any of x[0..count) is NaN.
+__global__ void any_nan_kernel(const float *__restrict__ x, int64_t count, int *flag) {
+  int local = 0;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < count;
+       i += int64_t(gridDim.x) * blockDim.x)
+    local |= (x[i] != x[i]);
+  if (__syncthreads_or(local) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 int grid_for(int64_t work, int threads) {
   const int64_t g = cdiv(work, threads);
   const int64_t cap = int64_t(sm_count()) * 16;
@@ -159,7 +173,8 @@ int grid_for(int64_t work, int threads) {
 
 // Column statistics + normalised float rows for one operand.
 int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz, int slot_z,
-                 int slot_st, float **Z, ColStats **st, cudaStream_t s) {
+                 int slot_st, float **Z, ColStats **st, cudaStream_t s,
+                 const int *run_if = nullptr) {
   void *pz = nullptr, *pst = nullptr;
   GT_TRY(ws_get(slot_z, size_t(nvar) * size_t(ldz) * 4, &pz));
   GT_TRY(ws_get(slot_st, size_t(nvar) * sizeof(ColStats), &pst));
@@ -167,11 +182,32 @@ int prologue_f32(const float *dX, int64_t nvar, int64_t n, int use, int64_t ldz,
   *st = static_cast<ColStats *>(pst);
   ProfScope prof("pearson_prologue", s);
   colstats_kernel<<<unsigned(cdiv(nvar, kStatThreads / 32)), kStatThreads, 0, s>>>(dX, nvar, n, use,
-                                                                                 *st);
+                                                                                 *st, run_if);
   count_launch();
   const float padv = use == 0 ? 0.f : __builtin_nanf("");
-  normalize_f32_kernel<<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, ldz, *st, use, padv, *Z);
+  normalize_f32_kernel<<<unsigned(nvar), 256, 0, s>>>(dX, nvar, n, ldz, *st, use, padv, *Z,
+                                                      run_if);
   count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+// Device flag (bytes 128..131 of the small scratch slot): 1 if a or b holds
+// a NaN.  Asynchronous on s.
+int any_nan_flag(const float *a, int64_t na, const float *b, int64_t nb, int **flag,
+                 cudaStream_t s) {
+  void *pf = nullptr;
+  GT_TRY(ws_get(WS_SCRATCH4, 256, &pf));
+  *flag = static_cast<int *>(pf) + 32;
+  GT_CUDA(cudaMemsetAsync(*flag, 0, sizeof(int), s));
+  if (na > 0) {
+    any_nan_kernel<<<grid_for(na, 256), 256, 0, s>>>(a, na, *flag);
+    count_launch();
+  }
+  if (b && nb > 0) {
+    any_nan_kernel<<<grid_for(nb, 256), 256, 0, s>>>(b, nb, *flag);
+    count_launch();
+  }
   GT_CUDA(cudaGetLastError());
   return GT_OK;
 }
@@ -199,20 +235,31 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
   if (nA == 0 || nB == 0) return GT_OK;
   PearsonOut po{corr, ts, pairs, nB, float(n), symmetric};
   const int path = gt_get_gram_path();
-  if (use == GT_EVERYTHING && path != GT_GRAM_FP32 && n > 0) {
+  const bool tc = path != GT_GRAM_FP32 && n > 0;
+  // pairwise.complete.obs on inputs without a missing value is cor(everything):
+  // a device flag (any NaN in A or B) gates two launches, the tensor-core
+  // path (runs if the flag is clear) and the CUDA-core pairwise kernel (runs
+  // if it is set), so the call stays asynchronous
+  int *nan_flag = nullptr;
+  if (use != GT_EVERYTHING && tc) {
+    GT_TRY(any_nan_flag(dA, nA * n, symmetric ? nullptr : dB, nB * n, &nan_flag, s));
+    po.gate = nan_flag;
+  }
+  if (tc) {
     void *zA = nullptr, *zB = nullptr;
     int64_t kpad = 0;
     GT_TRY(pearson_tc_prologue(dA, nA, n, path, WS_SCRATCH0, WS_SCRATCH2, &zA, &kpad, s));
     if (symmetric) zB = zA;
     else GT_TRY(pearson_tc_prologue(dB, nB, n, path, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
-    return pearson_tc(zA, nA, zB, nB, kpad, path, po, s);
+    GT_TRY(pearson_tc(zA, nA, zB, nB, kpad, path, po, s));
+    if (use == GT_EVERYTHING) return GT_OK;
   }
   const int64_t ldz = (n + 3) / 4 * 4;
   float *zA = nullptr, *zB = nullptr;
   ColStats *sA = nullptr, *sB = nullptr;
-  GT_TRY(prologue_f32(dA, nA, n, use, ldz, WS_SCRATCH0, WS_SCRATCH2, &zA, &sA, s));
+  GT_TRY(prologue_f32(dA, nA, n, use, ldz, WS_SCRATCH0, WS_SCRATCH2, &zA, &sA, s, nan_flag));
   if (symmetric) zB = zA;
-  else GT_TRY(prologue_f32(dB, nB, n, use, ldz, WS_SCRATCH1, WS_SCRATCH3, &zB, &sB, s));
+  else GT_TRY(prologue_f32(dB, nB, n, use, ldz, WS_SCRATCH1, WS_SCRATCH3, &zB, &sB, s, nan_flag));
   SimtArgs a;
   a.R = zA; a.C = zB;
   a.ldr = a.ldc = ldz;
@@ -220,6 +267,7 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
   a.K = ldz;
   a.symmetric = symmetric;
   a.vec_ok = 1;
+  a.run_if = nan_flag;
   cudaError_t e;
   ProfScope prof(use == GT_EVERYTHING ? "pearson_gram" : "pearson_pairwise", s);
   if (use == GT_EVERYTHING) {

@@ -60,6 +60,7 @@
 #include <functional>
 #include <mutex>
 #include <queue>
+#include <type_traits>
 #include <vector>
 
 namespace gt {
@@ -251,6 +252,9 @@ struct PearsonFinish {
   float npairs, sq_nm2;
   float gscale;  // removes the operand scales (2^-28 for f16x3, else 1)
   int symmetric;
+  const int *gate = nullptr;  // when set, the kernel does nothing unless *gate == 0
+
+  __device__ __forceinline__ bool skip() const { return gate && *gate != 0; }
 
   __device__ __forceinline__ void put(float *pc, float *pt, float *pp, float v) const {
     if (corr) *pc = v;
@@ -476,7 +480,8 @@ struct EuclidFinish {
         const float2 cj = cv[k];
         const float s = na + cj.x;
         const float d2 = fmaf(ra * cj.y, g[k], s);
-        pend = (pend << 1) | (__float_as_uint(fmaf(-tau, s, d2)) >> 31);
+        // (pend << 1) | sign of d2 - tau s, in one funnel shift
+        pend = __funnelshift_l(__float_as_uint(fmaf(-tau, s, d2)), pend, 1);
         const float v = tc::sqrt_approx(fabsf(d2));
         *o = v;
         o += full ? step0 : step0 - k;
@@ -635,7 +640,8 @@ struct EuclidLineFinish {
         for (int e = 0; e < 4; e++) {
           const float s = na + cn[e];
           const float d2 = fmaf(ra * cs[e], g[4 * k4 + e], s);
-          pend = (pend << 1) | (__float_as_uint(fmaf(-tau, s, d2)) >> 31);
+          // (pend << 1) | sign of d2 - tau s, in one funnel shift
+          pend = __funnelshift_l(__float_as_uint(fmaf(-tau, s, d2)), pend, 1);
           orow[co[e]] = tc::sqrt_approx(fabsf(d2));
         }
       }
@@ -665,8 +671,22 @@ struct EuclidLineFinish {
   // shared-memory list that the warp recomputes itself.
   __device__ __forceinline__ void queue(unsigned pend, int off, EpiCtx &ctx) const {
     const unsigned FULLM = 0xffffffffu;
-    if (!__any_sync(FULLM, pend != 0u)) return;
+    const unsigned lanes = __ballot_sync(FULLM, pend != 0u);
+    if (!lanes) return;
     const int lane = threadIdx.x & 31;
+    // usual case: at most one pending entry per lane; slots by lane rank
+    if (!__any_sync(FULLM, (pend & (pend - 1u)) != 0u)) {
+      const int total = __popc(lanes);
+      if (ctx.gcount + total <= pair_cap) {
+        if (pend) {
+          const int slot = ctx.gcount + __popc(lanes & ((1u << lane) - 1u));
+          region()[slot] =
+              make_int2(int(ctx.rbase) + lane, col_ids(ctx)[off + 31 - (__ffs(int(pend)) - 1)]);
+        }
+        ctx.gcount += total;
+        return;
+      }
+    }
     const int cnt = __popc(pend);
     int incl = cnt;
 #pragma unroll
@@ -813,6 +833,10 @@ struct SingleWork {
     return true;
   }
   static constexpr bool kPrefetch = false;
+  __device__ bool skip() const {
+    if constexpr (std::is_same<Fin, PearsonFinish>::value) return fin.skip();
+    return false;
+  }
   __device__ const Fin &finish(const TileRef &) const { return fin; }
   __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
   __device__ void prefetch() const {
@@ -863,6 +887,7 @@ struct PearsonBatchWork {
     return true;
   }
   static constexpr bool kPrefetch = false;
+  __device__ bool skip() const { return false; }
   __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
   __device__ void drain(EpiCtx &) const {}
   __device__ void prefetch() const {}
@@ -890,6 +915,7 @@ struct EuclidLineWork {
     return true;
   }
   static constexpr bool kPrefetch = true;
+  __device__ bool skip() const { return false; }
   __device__ const EuclidLineFinish &finish(const TileRef &) const { return fin; }
   __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
   __device__ void prefetch() const {
@@ -937,6 +963,7 @@ template <int KIND, int BK, bool CHUNKED, class Work>
 __global__ void __launch_bounds__(TcCfg<KIND, BK, !CHUNKED>::THREADS, 1)
 gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
   using C = TcCfg<KIND, BK, !CHUNKED>;
+  if (work.skip()) return;  // a gated launch whose gate is closed: before any setup
   constexpr int NSPLIT = C::NSPLIT;
   static_assert(!CHUNKED || C::COLS == 128, "chunked sums hold 128 columns per warp");
   static_assert(CHUNKED || C::COLS == kEuclidCols, "the list kernels hold 64 columns per warp");
@@ -1081,7 +1108,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
       ctx.rbase = r - lane;
       ctx.col0 = col;
       fin.begin_tile(r, ctx);
-      if (CHUNKED) {
+      if constexpr (CHUNKED) {
         const int64_t nch = (ref.nk + ckb - 1) / ckb;
         float acc[128];
 #pragma unroll
@@ -1630,6 +1657,7 @@ int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t k
   const float gscale = kind == tc::KIND_F16X3 ? 1.f / 268435456.f : 1.f;  // 2^-28
   PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
                     std::sqrt(out.npairs - 2.f), gscale, out.symmetric};
+  fin.gate = out.gate;
   const int sym = out.symmetric ? kUpper : kFull;
   if (kind == tc::KIND_BF16X6)
     return launch_gram<tc::KIND_BF16X6, 32, true>(zA, nA, zB, nB, kpad, sym, tc_chunk_kblocks(32),

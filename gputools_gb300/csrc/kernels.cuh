@@ -42,6 +42,7 @@ struct PearsonOut {
   int64_t ld;       // leading dimension of the outputs (nB)
   float npairs;     // value of `pairs` (everything mode: n)
   int symmetric;
+  const int *gate = nullptr;  // tensor-core path: run only if *gate == 0 (device flag)
 };
 
 // Operands for the tensor-core path: for each variable, the 16-bit parts of

@@ -128,6 +128,41 @@ def test_pairwise_complete(gpu, oracle_mod, rng, na, nb, n, frac):
     check_r(corr, wc, 2e-5)
 
 
+@pytest.mark.parametrize("na,nb,n", [(3, 5, 30), (130, 70, 257), (200, 200, 64)])
+def test_pairwise_without_missing_values(gpu, oracle_mod, rng, path, na, nb, n):
+    """pairwise.complete.obs on inputs without a NaN is cor(everything): the
+    tensor-core paths take it (a device NaN flag gates the launches); pairs
+    are n everywhere.  A constant variable still gives NaN."""
+    A = (rng.standard_normal((na, n)) * 3 + 7).astype(np.float32)
+    B = (rng.standard_normal((nb, n)) + 50).astype(np.float32)
+    A[1] = 4.0
+    corr, pairs, ts = rpmcc(gpu, 1, A, B)
+    wc, wp, wt = oracle_mod.pearson(A, B, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, tol(path, n))
+    check_ts(ts, corr, pairs, wt, wc)
+    # cor(x) with the same NaN-free matrix
+    corr, pairs, _ = rpmcc(gpu, 1, A, A.copy())
+    wc, wp, _ = oracle_mod.pearson(A, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, tol(path, n))
+
+
+def test_pairwise_flag_follows_each_call(gpu, oracle_mod, rng, path):
+    """Alternating inputs with and without a NaN on the same sizes: each call
+    takes the right kernel (the flag is recomputed per call)."""
+    A = rng.standard_normal((40, 90)).astype(np.float32)
+    B = rng.standard_normal((50, 90)).astype(np.float32)
+    for k in range(3):
+        Bk = B.copy()
+        if k == 1:
+            Bk[7, 13] = np.nan
+        corr, pairs, _ = rpmcc(gpu, 1, A, Bk)
+        wc, wp, _ = oracle_mod.pearson(A, Bk, use=1)
+        assert np.array_equal(pairs, wp.astype(np.float32))
+        check_r(corr, wc, 2e-5 if k == 1 else tol(path, 90))
+
+
 def test_pairwise_degenerate(gpu, oracle_mod):
     A = np.array([[1, np.nan, 3, 4], [np.nan, np.nan, np.nan, 2], [5, 5, 5, 5]], np.float32)
     corr, pairs, _ = rpmcc(gpu, 1, A, A.copy())
