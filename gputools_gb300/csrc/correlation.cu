@@ -13,10 +13,10 @@
 //  * "everything": the Gram contraction runs on tcgen05 tensor cores
 //    (split bf16, gram_tc.cu) or, for GT_GRAM_FP32, on the CUDA-core engine;
 //  * "pairwise.complete.obs": on inputs without a missing value it is the
-//    "everything" result, so the tensor-core path runs (gated on a device
-//    NaN flag); otherwise the CUDA-core engine accumulates, per pair, the six
-//    masked sums (count, sums, squares, cross) of the standardised values and
-//    the epilogue forms r in FP64;
+//    "everything" result, so that tensor-core path runs (gated on a device
+//    NaN flag); otherwise the masked tensor-core Gram (pairwise_tc.cu) forms
+//    the six sums per pair (count, sums, squares, cross); the FP32 path
+//    accumulates them on the CUDA-core engine; r comes from them in FP64;
 //  * pairs, r and the t-score (hostSignif's rule, in float as the reference
 //    evaluates it) are written by the same epilogue; cor(x) computes each
 //    unordered pair once and mirrors it.
@@ -238,8 +238,9 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
   const bool tc = path != GT_GRAM_FP32 && n > 0;
   // pairwise.complete.obs on inputs without a missing value is cor(everything):
   // a device flag (any NaN in A or B) gates two launches, the tensor-core
-  // path (runs if the flag is clear) and the CUDA-core pairwise kernel (runs
-  // if it is set), so the call stays asynchronous
+  // Gram of everything mode (runs if the flag is clear) and the masked
+  // tensor-core Gram (runs if it is set), so the call stays asynchronous.
+  // The FP32 path keeps the CUDA-core six-sum kernel
   int *nan_flag = nullptr;
   if (use != GT_EVERYTHING && tc) {
     GT_TRY(any_nan_flag(dA, nA * n, symmetric ? nullptr : dB, nB * n, &nan_flag, s));
@@ -253,6 +254,8 @@ int pearson_impl(int use, const float *dA, int64_t nA, const float *dB, int64_t 
     else GT_TRY(pearson_tc_prologue(dB, nB, n, path, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
     GT_TRY(pearson_tc(zA, nA, zB, nB, kpad, path, po, s));
     if (use == GT_EVERYTHING) return GT_OK;
+    // with a missing value: the masked tensor-core Gram (pairwise_tc.cu)
+    return pearson_pairwise_tc(dA, nA, symmetric ? dA : dB, nB, n, po, nan_flag, s);
   }
   const int64_t ldz = (n + 3) / 4 * 4;
   float *zA = nullptr, *zB = nullptr;

@@ -1601,6 +1601,13 @@ int kind_nsplit(int kind) { return kind == tc::KIND_BF16X6 ? 3 : 2; }
 
 }  // namespace
 
+int tc_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad, int nplanes,
+                 int box_rows, int bk, bool f16) {
+  return make_plane_map(map, base, rows, kpad, nplanes, box_rows, bk, f16);
+}
+
+int tc_error_word(int **p) { return err_word(p); }
+
 // C[r][c] = sum_k A_r[k] B_c[k] over split-bf16 planes ([part][row][kpad]),
 // chunked FP32 accumulation, stored as a row-major float matrix.
 int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,

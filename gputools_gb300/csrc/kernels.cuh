@@ -2,6 +2,7 @@
 // of libgputools_gb300 (not part of the C ABI).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <functional>
@@ -20,6 +21,13 @@ int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
 // exact recomputation of near-zero distances.
 int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layout,
               cudaStream_t st);
+
+// gram_tc.cu: a 3-D TMA map over planes [nplanes][rows][kpad] of 16-bit
+// values (box {bk, box_rows, 1}; bk 32 -> 64-byte swizzle, 64 -> 128-byte),
+// and the tensor-core kernels' device error word.
+int tc_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad, int nplanes,
+                 int box_rows, int bk, bool f16);
+int tc_error_word(int **p);
 
 // Per-variable statistics of the Pearson prologue.
 struct ColStats {
@@ -50,6 +58,11 @@ struct PearsonOut {
 // (multiple of 64), zero padded.
 int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64_t kpad,
                int kind, const PearsonOut &out, cudaStream_t st);
+
+// pairwise_tc.cu: pairwise-complete Pearson on the tensor cores (masked
+// Gram of the six sums); every launch gated on the device flag run_if.
+int pearson_pairwise_tc(const float *dA, int64_t nA, const float *dB, int64_t nB, int64_t n,
+                        const PearsonOut &out, const int *run_if, cudaStream_t s);
 
 // C[r][c] = sum_k A_r[k] B_c[k] on tcgen05 from `nsplit` (2 or 3) split-bf16
 // planes ([part][row][kpad], kpad a multiple of 64), stored as row-major float.

@@ -163,6 +163,25 @@ def test_pairwise_flag_follows_each_call(gpu, oracle_mod, rng, path):
         check_r(corr, wc, 2e-5 if k == 1 else tol(path, 90))
 
 
+@pytest.mark.parametrize("frac", [0.01, 0.2])
+def test_pairwise_missing_long_columns(gpu, oracle_mod, rng, path, frac):
+    """Missing values over 4096 observations (16 accumulation chunks on the
+    tensor cores): the same tolerance as cor(everything)."""
+    n = 4096
+    A = (np.exp(rng.standard_normal((150, n)) + 5.0) + rng.uniform(0, 1e3, (150, 1))).astype(np.float32)
+    A[rng.random(A.shape) < frac] = np.nan
+    corr, pairs, ts = rpmcc(gpu, 1, A, A.copy())
+    wc, wp, wt = oracle_mod.pearson(A, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, 2e-5 if path == "bf16x3" else tol(path, n))
+    B = (rng.standard_normal((70, n)) - 3).astype(np.float32)
+    B[rng.random(B.shape) < frac] = np.nan
+    corr, pairs, _ = rpmcc(gpu, 1, A, B)
+    wc, wp, _ = oracle_mod.pearson(A, B, use=1)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    check_r(corr, wc, 2e-5 if path == "bf16x3" else tol(path, n))
+
+
 def test_pairwise_degenerate(gpu, oracle_mod):
     A = np.array([[1, np.nan, 3, 4], [np.nan, np.nan, np.nan, 2], [5, 5, 5, 5]], np.float32)
     corr, pairs, _ = rpmcc(gpu, 1, A, A.copy())
