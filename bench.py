@@ -536,8 +536,9 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     """The other configurations at their stated sizes: all six gpuDist methods
     on 4000 x 100, gpuCor kendall (500 obs x 1000 integer variables, bit-exact
     spot check) and pearson (500 x 1000), gpuDist euclidean 2000 x 64 through
-    the host C ABI, and the adjoints (gpuCorBackward 1024 x 4096 with a
-    symmetric 4096 x 4096 upstream; MDS stress on 8192 x 32)."""
+    the host C ABI, the adjoints (gpuCorBackward 1024 x 4096 with a
+    symmetric 4096 x 4096 upstream; MDS stress on 8192 x 32) and gpuMi
+    (2000 variables x 1000 samples, 10 bins, order 3)."""
     import torch
     import oracle
     sptr = ctypes.c_void_p(stream.cuda_stream)
@@ -626,6 +627,25 @@ def run_configs(lib, g, _lib, stream, dev, steps):
                                                              vp(loss), sptr)), k)
     out["mds_stress_8192x32"] = {"ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3)}
     del Xb, Gb, dXb, Xm, delta, gm
+    # gpuMi: 2000 variables x 1000 samples, 10 bins, cubic B-splines (order 3),
+    # the symmetric all-pairs matrix; tensor cores and the CUDA-core path, and
+    # a spot check of 4 rows against the FP64 oracle
+    Xi = (rng.standard_normal((1, 1000)) + 0.7 * rng.standard_normal((2000, 1000))).astype(np.float32)
+    dXi = torch.from_numpy(Xi).to(dev)
+    mi = torch.empty((2000, 2000), dtype=torch.float32, device=dev)
+    run_mi = lambda: _lib.check(lib.gt_mutual_info_device(10, 3, 1000, vp(dXi), 2000, vp(dXi), 2000,
+                                                          vp(mi), sptr))
+    ms = ev_time(run_mi, k)
+    rows = np.array([0, 999, 1500, 1999])
+    want, _, _ = oracle.bspline_mi(Xi, Xi[rows], bins=10, order=3)
+    err = float(np.max(np.abs(mi.cpu().numpy()[rows].astype(np.float64) - want)))
+    old_path = g.get_gram_path()
+    g.set_gram_path("fp32")
+    ms_cc = ev_time(run_mi, max(1, k // 3))
+    g.set_gram_path(old_path)
+    out["mi_2000x1000_b10_o3"] = {"ms": ms, "pairs_per_s": 2000 * 2000 / (ms * 1e-3),
+                                  "cuda_core_ms": ms_cc, "max_abs_err_sample": err}
+    del dXi, mi
     torch.cuda.empty_cache()
     out["batch"] = run_batches(g, stream, dev, k)
     return out

@@ -38,6 +38,7 @@ SIGNATURES = {
     "Rdistances": (None, [_vp, _pi, _pi, _vp, _pcp, _pf]),
     "rpmcc": (None, [_pi, _vp, _pi, _vp, _pi, _pi, _vp, _vp, _vp]),
     "RgpuKendall": (None, [_vp, _pi, _vp, _pi, _pi, _vp]),
+    "rBSplineMutualInfo": (None, [_pi, _pi, _pi, _pi, _vp, _pi, _vp, _vp]),
     "rsetDevice": (None, [_pi]),
     "rgetDevice": (None, [_pi]),
     "rtestT": (None, [_vp, _vp, _pi, _vp]),
@@ -61,6 +62,8 @@ SIGNATURES = {
     "gt_pmcc_device_noalloc": (_i, [_i, _vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
     "gt_kendall": (_i, [_vp, _i64, _vp, _i64, _i64, _vp]),
     "gt_kendall_device": (_i, [_vp, _i64, _vp, _i64, _i64, _vp, _vp]),
+    "gt_mutual_info": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gt_mutual_info_device": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
     "gt_ttest_device": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "gt_cor_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),
     "gt_dist_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),

@@ -229,6 +229,44 @@ def kendall_device(X, Y=None, stream=None):
     return out
 
 
+def gpuMi(x, y=None, bins: int = 2, splineOrder: int = 1):
+    """B-spline mutual information of every column pair (R/gpuMi.R): x
+    (nsamples x na), y (nsamples x nb, default x).  Returns the nb x na matrix
+    R builds with matrix(mi, nb, na), entry [j, i] = MI(x_i, y_j)."""
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(-1, 1)
+    same = y is None
+    y = x if same else np.asarray(y, dtype=np.float64)
+    if y.ndim == 1:
+        y = y.reshape(-1, 1)
+    if y.shape[0] != x.shape[0]:
+        raise ValueError("x and y need the same number of samples")
+    n, na = x.shape
+    nb = y.shape[1]
+    A = np.ascontiguousarray(x.T, dtype=np.float32)  # as.single(x): variables contiguous
+    B = A if same else np.ascontiguousarray(y.T, dtype=np.float32)
+    out = np.empty(na * nb, np.float32)
+    check(load().gt_mutual_info(int(bins), int(splineOrder), n, A.ctypes.data_as(ctypes.c_void_p),
+                                na, B.ctypes.data_as(ctypes.c_void_p), nb,
+                                out.ctypes.data_as(ctypes.c_void_p)))
+    return out.reshape(nb, na)
+
+
+def mutual_info_device(X, Y=None, bins: int = 2, order: int = 1, stream=None):
+    """gt_mutual_info_device on variable-major CUDA tensors (nx, n), (ny, n);
+    returns (ny, nx) float32 with [y, x] = MI(X_x, Y_y)."""
+    import torch
+    Y = X if Y is None else Y
+    nx, n = X.shape
+    ny = Y.shape[0]
+    out = torch.empty((ny, nx), dtype=torch.float32, device=X.device)
+    check(load().gt_mutual_info_device(int(bins), int(order), n, ctypes.c_void_p(X.data_ptr()), nx,
+                                       ctypes.c_void_p(Y.data_ptr()), ny,
+                                       ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)))
+    return out
+
+
 def set_gram_path(path: str) -> None:
     """"bf16x3" / "bf16x6" (tcgen05 split-bf16), "f16x3" (tcgen05, scaled
     split-fp16) or "fp32" (CUDA cores)."""

@@ -731,6 +731,62 @@ struct EuclidLineFinish {
   }
 };
 
+// B-spline mutual information (inst/cuda/mi.cu:115-152 get_mi): rows and
+// columns are (variable, bin) with 2^lg bins per variable (zero padded), the
+// Gram entry times gscale / nsamples is the joint probability p_ab of the
+// two variables' bins.  A 32 x 32 block holds whole bin blocks: each lane sums
+// p log2 p over a column variable's bins, the lanes of one row variable add
+// their sums, and MI = that sum + H(x) + H(y) goes to out[y * ldo + x] (the
+// reference layout; with symmetric, pairs x <= y and their mirror).
+struct MiFinish {
+  float *out;
+  const float *hx, *hy;  // entropies of the row and column variables
+  int64_t nx, ny, ldo;   // variables, row length of out
+  float pscale;          // gscale / nsamples
+  int lg;                // log2 of the bins per variable
+  int symmetric;
+
+  __device__ __forceinline__ static float plog2p(float p) { return p > 0.f ? p * __log2f(p) : 0.f; }
+
+  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &) const {
+    const int lane = threadIdx.x & 31;
+    const int nb = 1 << lg;
+    const int64_t x = r >> lg;
+    float t[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) t[j] = plog2p(g[j] * pscale);
+    // segmented sums: t[j] of the first column of each column variable ends
+    // up holding the sum over that variable's bins
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+      if (l < lg) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 2 << l) t[j] += t[j + (1 << l)];
+      }
+    }
+    // ... and over the row variable's bins (its nb consecutive lanes)
+    for (int o = nb >> 1; o > 0; o >>= 1) {
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        if ((j & (nb - 1)) == 0) t[j] += __shfl_xor_sync(0xffffffffu, t[j], o);
+    }
+    if ((lane & (nb - 1)) != 0 || x >= nx) return;
+    const float hxx = hx[x];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if ((j & (nb - 1)) != 0) continue;
+      const int64_t y = (c0 + j) >> lg;
+      if (y >= ny || (symmetric && y < x)) continue;
+      const float mi = t[j] + hxx + hy[y];
+      out[y * ldo + x] = mi;
+      if (symmetric && y != x) out[x * ldo + y] = mi;
+    }
+  }
+  __device__ void begin_tile(int64_t, EpiCtx &) const {}
+  __device__ void end_tile(EpiCtx &) const {}
+  __device__ void drain(EpiCtx &) const {}
+};
+
 // Plain FP32 store of the contraction, C[r*ld + c].
 struct StoreFinish {
   float *out;
@@ -1607,6 +1663,19 @@ int tc_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad,
 }
 
 int tc_error_word(int **p) { return err_word(p); }
+
+// Mutual information from f16x3 weight planes (rows = variable * 2^lg + bin,
+// each weight times 2^14): the chunked Gram with MiFinish.
+int mi_tc(const void *planesX, int64_t rowsX, const void *planesY, int64_t rowsY, int64_t kpad,
+          int lg, int64_t nx, int64_t ny, int64_t nsamples, const float *hx, const float *hy,
+          float *out, int symmetric, cudaStream_t s) {
+  if (rowsX == 0 || rowsY == 0) return GT_OK;
+  MiFinish fin{out, hx, hy, nx, ny, nx, float(1.0 / (268435456.0 * double(nsamples))), lg,
+               symmetric};
+  return launch_gram<tc::KIND_F16X3, 32, true>(planesX, rowsX, planesY, rowsY, kpad,
+                                               symmetric ? kUpper : kFull, tc_chunk_kblocks(32),
+                                               fin, "mi_gram", s);
+}
 
 // C[r][c] = sum_k A_r[k] B_c[k] over split-bf16 planes ([part][row][kpad]),
 // chunked FP32 accumulation, stored as a row-major float matrix.

@@ -91,6 +91,18 @@ void RgpuKendall(const float *X, const int *nx, const float *Y, const int *ny,
   gt::report(st, "RgpuKendall");
 }
 
+void rBSplineMutualInfo(const int *nBins, const int *splineOrder, const int *nsamples,
+                        const int *rowsA, const float *A, const int *rowsB, const float *B,
+                        float *mutualInfo) {
+  gt::clear_error();
+  int st;
+  if (!nBins || !splineOrder || !nsamples || !rowsA || !rowsB)
+    st = gt::fail(GT_EINVAL, "null argument");
+  else
+    st = gt_mutual_info(*nBins, *splineOrder, *nsamples, A, *rowsA, B, *rowsB, mutualInfo);
+  gt::report(st, "rBSplineMutualInfo");
+}
+
 // src/correlation.cpp:163-171 setDevice: ids outside [0, count) are an error.
 void rsetDevice(const int *device) {
   gt::clear_error();

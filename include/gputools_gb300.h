@@ -93,6 +93,16 @@ void rpmcc(const int *whichObs, const float *samplesA, const int *numSamplesA,
 void RgpuKendall(const float *X, const int *nx, const float *Y, const int *ny,
                  const int *sampleSize, double *answers);
 
+/* Replaces src/rinterface.cpp:415-422 (declared src/rinterface.h:73-76;
+ * R/gpuMi.R).  B-spline mutual information of every pair (x in A, y in B),
+ * nsamples values per variable (variables contiguous), at
+ * mutualInfo[y*rowsA + x]: nBins bins, B-splines of order splineOrder
+ * (1 <= splineOrder <= min(nBins, 8)).  A variable whose values are all equal
+ * is scaled to zeros (the reference divides 0 by 0 there). */
+void rBSplineMutualInfo(const int *nBins, const int *splineOrder, const int *nsamples,
+                        const int *rowsA, const float *A, const int *rowsB,
+                        const float *B, float *mutualInfo);
+
 /* Replace src/rinterface.cpp:79-85 (declared src/rinterface.h:23-24). */
 void rsetDevice(const int *device);
 void rgetDevice(int *device);
@@ -181,6 +191,18 @@ int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny,
 /* Device buffers; d_Y == d_X marks cor(x) (diagonal exactly 1). */
 int gt_kendall_device(const float *d_X, int64_t nx, const float *d_Y,
                       int64_t ny, int64_t n, double *d_out, void *stream);
+
+/* Host buffers, synchronous.  Same result as rBSplineMutualInfo:
+ * out[y*nx + x] = MI(X_x, Y_y); Y == X (and ny == nx) is the symmetric case. */
+int gt_mutual_info(int nbins, int order, int64_t n, const float *X, int64_t nx,
+                   const float *Y, int64_t ny, float *out);
+
+/* Device buffers; d_Y == d_X with ny == nx computes each unordered pair once
+ * and writes both entries.  Up to 32 bins on the tensor cores (f16x3 Gram of
+ * the B-spline weights), more on the CUDA cores. */
+int gt_mutual_info_device(int nbins, int order, int64_t n, const float *d_X,
+                          int64_t nx, const float *d_Y, int64_t ny, float *d_out,
+                          void *stream);
 
 /* ---- adjoints (no counterpart in the reference) ------------------------- */
 

@@ -75,6 +75,7 @@ def _load():
         lib.orc_cor_backward.argtypes = [fp, i64, i64, fp, fp]
         lib.orc_dist_backward.argtypes = [fp, i64, i64, fp, fp]
         lib.orc_mds_stress.argtypes = [fp, i64, i64, fp, fp, fp]
+        lib.orc_bspline_mi.argtypes = [ctypes.c_int, ctypes.c_int, i64, fp, i64, fp, i64, fp, fp, fp]
         lib.orc_set_threads.argtypes = [ctypes.c_int]
         lib.orc_get_threads.restype = ctypes.c_int
         del dp
@@ -269,3 +270,21 @@ def mds_stress(X: np.ndarray, delta: np.ndarray):
     out = np.empty((n, d), np.float64)
     _load().orc_mds_stress(_ptr(X), n, d, _ptr(delta), _ptr(loss), _ptr(out))
     return float(loss[0]), out
+
+
+def bspline_mi(X: np.ndarray, Y: Optional[np.ndarray] = None, bins: int = 2, order: int = 1):
+    """B-spline mutual information (R's gpuMi): X (nx, n) and Y (ny, n), one
+    variable per row.  Returns (mi, hx, hy) with mi[y, x] = MI(X_x, Y_y) (the
+    reference layout out[y*nx + x]) and the entropies."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = X if Y is None else np.ascontiguousarray(Y, dtype=np.float32)
+    nx, n = X.shape
+    ny = Y.shape[0]
+    out = np.empty((ny, nx), np.float64)
+    hx = np.empty(nx, np.float64)
+    hy = np.empty(ny, np.float64)
+    rc = _load().orc_bspline_mi(int(bins), int(order), n, _ptr(X), nx, _ptr(Y), ny, _ptr(out),
+                                _ptr(hx), _ptr(hy))
+    if rc != 0:
+        raise ValueError(f"orc_bspline_mi failed ({rc})")
+    return out, hx, hy

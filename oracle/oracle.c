@@ -354,3 +354,117 @@ int orc_mds_stress(const float *X, int64_t n, int64_t dim, const float *delta,
   if (loss) *loss = total;
   return 0;
 }
+
+/* ------------------------------------------------------ mutual information --- */
+/* B-spline mutual information (R/gpuMi.R, src/mi.cpp, inst/cuda/mi.cu).
+ *
+ * Knots (src/mi.cpp:14-30 initKnots): order zeros, then 1, 2, ... up to
+ * index nbins - 1, then the last value + 1 repeated; nknots = nbins + order.
+ * Each variable is scaled to [0, knot_max] from its own min and max, in float
+ * as inst/cuda/mi.cu:3-25 scale() does (a variable whose max equals its min
+ * has no scale there -- 0/0 -- and is taken as all zeros here).  Its samples'
+ * B-spline weights follow the Cox-de Boor recursion with the index bounds of
+ * inst/cuda/mi.cu:39-86 get_bin_scores, here in double.  Entropies
+ * (inst/cuda/mi.cu:88-113) and mutual information (inst/cuda/mi.cu:115-152)
+ * use probabilities p = (sum of weights) / nsamples and log2, with p <= 0
+ * contributing nothing:
+ *   H(x)    = -sum_a p_a log2 p_a
+ *   MI(x,y) = sum_ab p_ab log2 p_ab + H(x) + H(y),  p_ab = sum_k wx_ka wy_kb / n. */
+static double mi_frac(double numer, double denom) {
+  if (numer == denom && numer != 0.0) return 1.0;
+  if (denom != 0.0) return numer / denom;
+  return 0.0;
+}
+
+/* weights w[k * nbins + a] of variable x (n samples) */
+static void mi_weights(const float *x, int64_t n, int nbins, int order, const float *knots,
+                       int nknots, double *w) {
+  float mn = x[0], mx = x[0];
+  for (int64_t k = 1; k < n; k++) {
+    if (x[k] < mn) mn = x[k];
+    if (x[k] > mx) mx = x[k];
+  }
+  const float kmax = knots[nknots - 1];
+  const float delta = mx - mn;
+  memset(w, 0, sizeof(double) * (size_t)n * (size_t)nbins);
+  for (int64_t k = 0; k < n; k++) {
+    const float z = delta > 0.f ? (kmax * (x[k] - mn)) / delta : 0.f;
+    double *b = w + k * nbins;
+    int i0 = (int)floorf(z) + order - 1;
+    if (i0 >= nbins) i0 = nbins - 1;
+    b[i0] = 1.0;
+    for (int i = 2; i <= order; i++) {
+      for (int j = i0 - i + 1; j <= i0; j++) {
+        double t1, t2;
+        if (j < 0 || j >= nbins || j >= nknots || j + i - 1 < 0 || j > nknots)
+          t1 = 0.0;
+        else
+          t1 = mi_frac((double)z - knots[j], (double)knots[j + i - 1] - knots[j]) * b[j];
+        if (j + 1 < 0 || j + 1 >= nbins || j + 1 >= nknots || j + i < 0 || j + i >= nknots)
+          t2 = 0.0;
+        else
+          t2 = mi_frac((double)knots[j + i] - z, (double)knots[j + i] - knots[j + 1]) * b[j + 1];
+        b[j] = t1 + t2;
+      }
+    }
+  }
+}
+
+static double plog2p(double p) { return p > 0.0 ? p * log2(p) : 0.0; }
+
+int orc_bspline_mi(int nbins, int order, int64_t n, const float *X, int64_t nx,
+                   const float *Y, int64_t ny, double *out, double *hx, double *hy) {
+  if (nbins < 1 || order < 1 || order > nbins || n < 1 || nx < 0 || ny < 0) return -1;
+  const int nknots = nbins + order;
+  float *knots = (float *)malloc(sizeof(float) * (size_t)nknots);
+  const int degree = nbins - 1;
+  for (int i = 0; i < nknots; i++) {
+    if (i <= order - 1) knots[i] = 0.f;
+    else if (i <= degree) knots[i] = knots[i - 1] + 1.f;
+    else knots[i] = knots[degree] + 1.f;
+  }
+  double *wx = (double *)malloc(sizeof(double) * (size_t)(nx * n * nbins));
+  double *wy = (double *)malloc(sizeof(double) * (size_t)(ny * n * nbins));
+  double *ex = (double *)malloc(sizeof(double) * (size_t)(nx > 0 ? nx : 1));
+  double *ey = (double *)malloc(sizeof(double) * (size_t)(ny > 0 ? ny : 1));
+  if (!knots || !wx || !wy || !ex || !ey) {
+    free(knots); free(wx); free(wy); free(ex); free(ey);
+    return -3;
+  }
+  const float *src[2] = {X, Y};
+  double *w[2] = {wx, wy}, *e[2] = {ex, ey};
+  const int64_t cnt[2] = {nx, ny};
+  for (int s = 0; s < 2; s++) {
+#pragma omp parallel for schedule(dynamic, 4) num_threads(orc_get_threads())
+    for (int64_t v = 0; v < cnt[s]; v++) {
+      double *wv = w[s] + v * n * nbins;
+      mi_weights(src[s] + v * n, n, nbins, order, knots, nknots, wv);
+      double h = 0.0;
+      for (int a = 0; a < nbins; a++) {
+        ksum acc = {0.0, 0.0};
+        for (int64_t k = 0; k < n; k++) ks_add(&acc, wv[k * nbins + a]);
+        h -= plog2p(ks_val(&acc) / (double)n);
+      }
+      e[s][v] = h;
+    }
+  }
+#pragma omp parallel for collapse(2) schedule(dynamic, 16) num_threads(orc_get_threads())
+  for (int64_t y = 0; y < ny; y++) {
+    for (int64_t x = 0; x < nx; x++) {
+      const double *a = wx + x * n * nbins, *b = wy + y * n * nbins;
+      double mi = 0.0;
+      for (int i = 0; i < nbins; i++) {
+        for (int j = 0; j < nbins; j++) {
+          ksum acc = {0.0, 0.0};
+          for (int64_t k = 0; k < n; k++) ks_add(&acc, a[k * nbins + i] * b[k * nbins + j]);
+          mi += plog2p(ks_val(&acc) / (double)n);
+        }
+      }
+      out[y * nx + x] = mi + ex[x] + ey[y];
+    }
+  }
+  if (hx) memcpy(hx, ex, sizeof(double) * (size_t)nx);
+  if (hy) memcpy(hy, ey, sizeof(double) * (size_t)ny);
+  free(knots); free(wx); free(wy); free(ex); free(ey);
+  return 0;
+}

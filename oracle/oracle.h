@@ -22,6 +22,9 @@
  *             variant instead, and the counts exposed here let tests check
  *             both.
  *   ttest   : src/correlation.cpp:17-49 testSignif / inst/cuda/correlation.cu:294-313.
+ *   mi      : B-spline mutual information, src/mi.cpp:14-164 with
+ *             inst/cuda/mi.cu:1-152 (knots, min-max scaling in float, the
+ *             Cox-de Boor weights, entropies and MI in log2).
  *
  * Layouts follow the reference: points row-major N x D (src/distance.h:10-26),
  * distances d[y*N + x]; correlation inputs variable-contiguous (A[x*n + k]),
@@ -77,6 +80,12 @@ int orc_dist_backward(const float *X, int64_t n, int64_t dim, const double *G,
                       double *dX);
 int orc_mds_stress(const float *X, int64_t n, int64_t dim, const float *delta,
                    double *loss, double *dX);
+
+/* B-spline mutual information (src/mi.cpp, inst/cuda/mi.cu): out[y*nx + x]
+ * = MI(X_x, Y_y) over n samples (variables contiguous, X[x*n + k]); hx, hy
+ * (may be NULL) receive the entropies.  See oracle.c for the restatement. */
+int orc_bspline_mi(int nbins, int order, int64_t n, const float *X, int64_t nx,
+                   const float *Y, int64_t ny, double *out, double *hx, double *hy);
 
 #ifdef __cplusplus
 }
