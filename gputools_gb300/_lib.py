@@ -39,6 +39,8 @@ SIGNATURES = {
     "rpmcc": (None, [_pi, _vp, _pi, _vp, _pi, _pi, _vp, _vp, _vp]),
     "RgpuKendall": (None, [_vp, _pi, _vp, _pi, _pi, _vp]),
     "rBSplineMutualInfo": (None, [_pi, _pi, _pi, _pi, _vp, _pi, _vp, _vp]),
+    "Rhcluster": (None, [_vp, _pi, _vp, _vp, _vp, _pcp]),
+    "Rdistclust": (None, [_pcp, _pcp, _vp, _pi, _pi, _vp, _vp, _vp]),
     "rsetDevice": (None, [_pi]),
     "rgetDevice": (None, [_pi]),
     "rtestT": (None, [_vp, _vp, _pi, _vp]),
@@ -64,6 +66,10 @@ SIGNATURES = {
     "gt_kendall_device": (_i, [_vp, _i64, _vp, _i64, _i64, _vp, _vp]),
     "gt_mutual_info": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp]),
     "gt_mutual_info_device": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "gt_hclust": (_i, [_vp, _i64, _cp, _vp, _vp, _vp]),
+    "gt_hclust_device": (_i, [_vp, _i64, _cp, _vp, _vp, _vp, _vp]),
+    "gt_distclust": (_i, [_vp, _i64, _i64, _i, _cp, _vp, _vp, _vp]),
+    "gt_hclust_format": (_i, [_i, _vp, _vp, _vp, _vp]),
     "gt_ttest_device": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "gt_cor_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),
     "gt_dist_backward_device": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),

@@ -26,6 +26,10 @@ from ._lib import GT_LAYOUT_DIST, GT_LAYOUT_FULL, check, load
 
 DIST_METHODS = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
 COR_METHODS = ("pearson", "kendall")
+# R/gpuHclust.R gpuHclust's table; the chosen name goes to the library as is
+# ("flexible group" is then single linkage, as in the reference).
+HCLUST_METHODS = ("ward", "single", "complete", "average", "mcquitty", "median", "centroid",
+                  "flexible", "flexible group", "wpgma")
 COR_USES = ("everything", "pairwise.complete.obs")
 
 
@@ -265,6 +269,107 @@ def mutual_info_device(X, Y=None, bins: int = 2, order: int = 1, stream=None):
                                        ctypes.c_void_p(Y.data_ptr()), ny,
                                        ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)))
     return out
+
+
+class HClust:
+    """R's ``hclust`` object as gpuHclust / gpuDistClust build it: merge
+    ((n-1) x 2, negative = point, positive = earlier step), height, order
+    (1-based leaves), labels, method, dist_method."""
+
+    def __init__(self, merge, height, order, labels, method, dist_method):
+        self.merge = merge
+        self.height = height
+        self.order = order
+        self.labels = labels
+        self.method = method
+        self.dist_method = dist_method
+
+
+def _hclust_method(method: str) -> str:
+    idx = pmatch(method, HCLUST_METHODS)
+    if idx is None:
+        raise ValueError("invalid clustering method")
+    return HCLUST_METHODS[idx]
+
+
+def gpuHclust(distances, method: str = "complete") -> HClust:
+    """Hierarchical clustering of a ``Dist`` (R/gpuHclust.R:41-90)."""
+    method = _hclust_method(method)
+    n = getattr(distances, "size", None)
+    if n is None:
+        raise ValueError("invalid dissimilarities")
+    n = int(n)
+    if n < 2:
+        raise ValueError("must have n >= 2 objects to cluster")
+    want = n * (n - 1) // 2
+    if len(distances) != want:
+        if len(distances) < want:
+            raise ValueError("dissimilarities of improper length")
+        warnings.warn("dissimilarities of improper length")
+    full = np.ascontiguousarray(distances.to_matrix(), dtype=np.float32)
+    merge = np.empty(2 * (n - 1), np.int32)
+    order = np.empty(n, np.int32)
+    height = np.empty(n - 1, np.float32)
+    check(load().gt_hclust(_ptr(full), n, method.encode(), _ptr(merge), _ptr(order),
+                           _ptr(height)))
+    return HClust(merge.reshape(2, n - 1).T.copy(), height, order, distances.labels, method,
+                  distances.method)
+
+
+def gpuDistClust(points, distmethod: str = "euclidean", clustmethod: str = "complete",
+                 labels=None) -> HClust:
+    """Distances (p = 2) and clustering in one call, the distance matrix kept
+    on the device (R/gpuHclust.R:92-146).  As there, "euclidian" is not an
+    alias here (the reference's alias assignment names another variable)."""
+    idx = pmatch(distmethod, DIST_METHODS)
+    if idx is None:
+        raise ValueError("invalid distance method")
+    distmethod = DIST_METHODS[idx]
+    clustmethod = _hclust_method(clustmethod)
+    pts = np.asarray(points, dtype=np.float64)
+    if pts.ndim == 1:
+        pts = pts.reshape(-1, 1)
+    if not np.all(np.isfinite(pts)):
+        raise ValueError("NA/NaN/Inf in foreign function call (arg 3)")
+    n, d = pts.shape
+    if n < 2:
+        raise ValueError("must have n >= 2 objects to cluster")
+    rowmajor = np.ascontiguousarray(pts, dtype=np.float32)
+    merge = np.empty(2 * (n - 1), np.int32)
+    order = np.empty(n, np.int32)
+    height = np.empty(n - 1, np.float32)
+    check(load().gt_distclust(_ptr(rowmajor), n, d, idx, clustmethod.encode(), _ptr(merge),
+                              _ptr(order), _ptr(height)))
+    return HClust(merge.reshape(2, n - 1).T.copy(), height, order, labels, clustmethod,
+                  distmethod)
+
+
+def hclust_device(D, method: str = "complete", stream=None):
+    """gt_hclust_device on a contiguous float32 CUDA tensor (n, n), which is
+    overwritten.  Returns numpy (merge (n-1, 2), order (n,), height (n-1,)).
+    ``method`` goes to the library as is (no partial matching)."""
+    import torch
+    if D.dtype != torch.float32 or not D.is_cuda or not D.is_contiguous() or D.dim() != 2 \
+            or D.shape[0] != D.shape[1]:
+        raise ValueError("D must be a contiguous square float32 CUDA tensor")
+    n = D.shape[0]
+    merge = np.empty(2 * max(n - 1, 0), np.int32)
+    order = np.empty(n, np.int32)
+    height = np.empty(max(n - 1, 0), np.float32)
+    check(load().gt_hclust_device(ctypes.c_void_p(D.data_ptr()), n, method.encode(),
+                                  _ptr(merge), _ptr(order), _ptr(height), _stream_ptr(stream)))
+    return merge.reshape(2, n - 1).T.copy(), order, height
+
+
+def hclust_format(sub, sup):
+    """gt_hclust_format: 0-based step list -> (merge (len, 2), order (len+1,))."""
+    sub = np.ascontiguousarray(sub, dtype=np.int32)
+    sup = np.ascontiguousarray(sup, dtype=np.int32)
+    m = len(sub)
+    merge = np.empty(2 * m, np.int32)
+    order = np.empty(m + 1, np.int32)
+    check(load().gt_hclust_format(m, _ptr(sub), _ptr(sup), _ptr(merge), _ptr(order)))
+    return merge.reshape(2, m).T.copy(), order
 
 
 def set_gram_path(path: str) -> None:

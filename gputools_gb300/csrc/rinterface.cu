@@ -103,6 +103,29 @@ void rBSplineMutualInfo(const int *nBins, const int *splineOrder, const int *nsa
   gt::report(st, "rBSplineMutualInfo");
 }
 
+// src/rinterface.cpp:216-239: the full n x n matrix of R's as.matrix(dist).
+void Rhcluster(const float *distMat, const int *numPoints, int *merge, int *order, float *val,
+               const char **method) {
+  gt::clear_error();
+  int st;
+  if (!numPoints || !method) st = gt::fail(GT_EINVAL, "null argument");
+  else st = gt_hclust(distMat, *numPoints, *method, merge, order, val);
+  gt::report(st, "Rhcluster");
+}
+
+// src/rinterface.cpp:172-204: distances (p = 2) stay on the device.
+void Rdistclust(const char **distmethod, const char **clustmethod, const float *points,
+                const int *numPoints, const int *dim, int *merge, int *order, float *val) {
+  gt::clear_error();
+  int st;
+  if (!distmethod || !clustmethod || !numPoints || !dim)
+    st = gt::fail(GT_EINVAL, "null argument");
+  else
+    st = gt_distclust(points, *numPoints, *dim, gt::dist_enum(*distmethod), *clustmethod, merge,
+                      order, val);
+  gt::report(st, "Rdistclust");
+}
+
 // src/correlation.cpp:163-171 setDevice: ids outside [0, count) are an error.
 void rsetDevice(const int *device) {
   gt::clear_error();

@@ -103,6 +103,26 @@ void rBSplineMutualInfo(const int *nBins, const int *splineOrder, const int *nsa
                         const int *rowsA, const float *A, const int *rowsB,
                         const float *B, float *mutualInfo);
 
+/* Replaces src/rinterface.cpp:216-239 (declared src/rinterface.h:56-57;
+ * R/gpuHclust.R gpuHclust).  Agglomerative clustering of the numPoints x
+ * numPoints matrix distMat (R's as.matrix(dist); entry (i, j) at
+ * [i*numPoints + j], only the lower triangle and the rows of merged pairs
+ * are read).  merge: (numPoints-1) x 2 column-major, R's hclust convention
+ * (negative = point, positive = step); order: numPoints leaves, 1-based;
+ * val: merge heights.  method: "single", "complete", "average", "mcquitty",
+ * "wpgma", "median", "centroid", "flexible_group", "flexible", "ward"; any
+ * other string (R's "flexible group" included) means single linkage, as
+ * src/rinterface.cpp:158-170 getClusterEnum does.  Lance-Williams constants
+ * lambda = beta = 0.5. */
+void Rhcluster(const float *distMat, const int *numPoints, int *merge, int *order,
+               float *val, const char **method);
+
+/* Replaces src/rinterface.cpp:172-204 (declared src/rinterface.h:50-52;
+ * R/gpuHclust.R gpuDistClust).  Rdistances(points, distmethod, p = 2)
+ * followed by Rhcluster(clustmethod); the distances never leave the device. */
+void Rdistclust(const char **distmethod, const char **clustmethod, const float *points,
+                const int *numPoints, const int *dim, int *merge, int *order, float *val);
+
 /* Replace src/rinterface.cpp:79-85 (declared src/rinterface.h:23-24). */
 void rsetDevice(const int *device);
 void rgetDevice(int *device);
@@ -203,6 +223,25 @@ int gt_mutual_info(int nbins, int order, int64_t n, const float *X, int64_t nx,
 int gt_mutual_info_device(int nbins, int order, int64_t n, const float *d_X,
                           int64_t nx, const float *d_Y, int64_t ny, float *d_out,
                           void *stream);
+
+/* Host buffers, synchronous.  Same result as Rhcluster; method as there. */
+int gt_hclust(const float *dist, int64_t n, const char *method, int *merge, int *order,
+              float *height);
+
+/* Device matrix (n x n, overwritten: the merges are made in place), host
+ * results; returns after the merges are done (synchronises `stream`). */
+int gt_hclust_device(float *d_dist, int64_t n, const char *method, int *merge, int *order,
+                     float *height, void *stream);
+
+/* Host buffers, synchronous.  Same result as Rdistclust; dist_method is enum
+ * gt_dist_method. */
+int gt_distclust(const float *points, int64_t n, int64_t dim, int dist_method,
+                 const char *method, int *merge, int *order, float *height);
+
+/* src/rinterface.cpp:241-290 formatClustering on the host: the step list
+ * (sub[i], sup[i]: the two 0-based row indices merged at step i, len steps)
+ * to R's merge matrix and leaf order. */
+int gt_hclust_format(int len, const int *sub, const int *sup, int *merge, int *order);
 
 /* ---- adjoints (no counterpart in the reference) ------------------------- */
 

@@ -51,7 +51,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
         os.makedirs(BUILD, exist_ok=True)
         subprocess.check_call(
-            ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11", "-Wall",
+            ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11", "-Wall", "-ffp-contract=off",
              "-o", LIB, src, "-lm"])
     ref_script = os.path.join(HERE, "build_ref.sh")
     if (force or not os.path.exists(REF_LIB)) and os.path.isdir(
@@ -76,6 +76,9 @@ def _load():
         lib.orc_dist_backward.argtypes = [fp, i64, i64, fp, fp]
         lib.orc_mds_stress.argtypes = [fp, i64, i64, fp, fp, fp]
         lib.orc_bspline_mi.argtypes = [ctypes.c_int, ctypes.c_int, i64, fp, i64, fp, i64, fp, fp, fp]
+        lib.orc_hc_method.argtypes = [ctypes.c_char_p]
+        lib.orc_hclust.argtypes = [fp, i64, ctypes.c_int, ctypes.c_float, ctypes.c_float, fp, fp, fp]
+        lib.orc_format_clustering.argtypes = [ctypes.c_int, fp, fp, fp, fp]
         lib.orc_set_threads.argtypes = [ctypes.c_int]
         lib.orc_get_threads.restype = ctypes.c_int
         del dp
@@ -288,3 +291,31 @@ def bspline_mi(X: np.ndarray, Y: Optional[np.ndarray] = None, bins: int = 2, ord
     if rc != 0:
         raise ValueError(f"orc_bspline_mi failed ({rc})")
     return out, hx, hy
+
+
+def hclust(D: np.ndarray, method: str = "complete"):
+    """Hierarchical clustering of the full (n, n) float32 distance matrix as
+    the reference's kernels do it (gpuHclust).  Returns (sub, sup, height):
+    per step the merged column and row indices and the merge height."""
+    D = np.ascontiguousarray(D, dtype=np.float32)
+    n = D.shape[0]
+    sub = np.empty(n - 1, np.int32)
+    sup = np.empty(n - 1, np.int32)
+    val = np.empty(n - 1, np.float32)
+    m = _load().orc_hc_method(method.encode())
+    rc = _load().orc_hclust(_ptr(D), n, m, 0.5, 0.5, _ptr(sub), _ptr(sup), _ptr(val))
+    if rc != 0:
+        raise ValueError(f"orc_hclust failed ({rc})")
+    return sub, sup, val
+
+
+def format_clustering(sub: np.ndarray, sup: np.ndarray):
+    """R's merge matrix ((n-1) x 2) and order (1-based) from sub/sup, as the
+    reference's formatClustering does it."""
+    sub = np.ascontiguousarray(sub, np.int32)
+    sup = np.ascontiguousarray(sup, np.int32)
+    ln = sub.size
+    merge = np.empty(2 * ln, np.int32)
+    order = np.empty(ln + 1, np.int32)
+    _load().orc_format_clustering(ln, _ptr(sub), _ptr(sup), _ptr(merge), _ptr(order))
+    return merge.reshape(2, ln).T.copy(), order

@@ -468,3 +468,179 @@ int orc_bspline_mi(int nbins, int order, int64_t n, const float *X, int64_t nx,
   free(knots); free(wx); free(wy); free(ex); free(ey);
   return 0;
 }
+
+/* ------------------------------------------------- hierarchical clustering --- */
+/* gpuHclust / gpuDistClust (R/gpuHclust.R:41-146): the reference's loop of
+ * src/hcluster.cpp:40-201 over the kernels of inst/cuda/hcluster.cu, on the
+ * full n x n float matrix, with the diagonal set to +inf:
+ *   per active row (count > 0) the minimum over columns 0..row, ties broken
+ *   as its 32-thread strided scan and tree reduction break them (smallest
+ *   column mod 32, then smallest column: find_min1_kernel, :11-59); the
+ *   winning row likewise over the rows' minima (find_min2_kernel, :61-106);
+ *   sub = the winning column, sup = the winning row, val = the minimum,
+ *   count[sup] += count[sub], count[sub] = -count[sub]; then the row and
+ *   column of sup get the linkage update and those of sub +inf (:108-401).
+ * The update expressions are evaluated as written there (float, with the
+ * double promotions of the 2.0 / 4.0 / 1.0 - lambda constants), each
+ * operation rounded on its own (no fused multiply-add; the reference's
+ * run-time compilation leaves that choice to its compiler).  Methods follow
+ * getClusterEnum (src/rinterface.cpp): an unknown name -- among them R's
+ * "flexible group", which the reference matches against "flexible_group" --
+ * is single linkage. */
+enum { HC_SINGLE = 0, HC_COMPLETE, HC_WPGMA, HC_AVERAGE, HC_MEDIAN, HC_CENTROID,
+       HC_FLEXIBLE_GROUP, HC_FLEXIBLE, HC_WARD, HC_MCQUITTY };
+
+int orc_hc_method(const char *name) {
+  static const char *names[] = {"complete", "wpgma", "average", "median", "centroid",
+                                "flexible_group", "flexible", "ward", "mcquitty"};
+  static const int ids[] = {HC_COMPLETE, HC_WPGMA, HC_AVERAGE, HC_MEDIAN, HC_CENTROID,
+                            HC_FLEXIBLE_GROUP, HC_FLEXIBLE, HC_WARD, HC_MCQUITTY};
+  for (int i = 0; i < 9; i++)
+    if (name && strcmp(name, names[i]) == 0) return ids[i];
+  return HC_SINGLE;
+}
+
+/* (v1, c1) before (v2, c2): the value, then column mod 32, then column; a
+ * NaN is never before anything. */
+static int hc_before(float v1, int64_t c1, float v2, int64_t c2) {
+  if (v1 < v2) return 1;
+  if (!(v1 == v2)) return 0;
+  if ((c1 & 31) != (c2 & 31)) return (c1 & 31) < (c2 & 31);
+  return c1 < c2;
+}
+
+float orc_hc_update(int method, float top, float bot, float nr, float np, float nk, float val,
+                    float lambda, float beta) {
+  const float nq = nr - np;
+  switch (method) {
+    case HC_COMPLETE: return top > bot ? top : (bot == bot ? bot : top);
+    case HC_WPGMA:
+    case HC_MCQUITTY: return (float)((double)(bot + top) / 2.0);
+    case HC_AVERAGE: {
+      const float a = top * np, b = bot * nq;
+      return (a + b) / nr;
+    }
+    case HC_MEDIAN: return (float)((double)(bot + top) / 2.0 - (double)val / 4.0);
+    case HC_CENTROID: {
+      const float a = top * np, b = bot * nq;
+      const float t1 = (a + b) / nr;
+      const float pq = np * nq, num = pq * val, den = nr * nr;
+      return t1 - num / den;
+    }
+    case HC_FLEXIBLE_GROUP: {
+      const double l1 = 1.0 - (double)lambda;
+      const double a = ((double)bot * l1) * (double)np, b = ((double)top * l1) * (double)nq;
+      const float bv = beta * val;
+      return (float)((a + b) / (double)nr + (double)bv);
+    }
+    case HC_FLEXIBLE: {
+      const double l1 = 1.0 - (double)lambda;
+      const double a = (double)bot * l1, b = (double)top * l1;
+      const float bv = beta * val;
+      return (float)((a + b) / 2.0 + (double)bv);
+    }
+    case HC_WARD: {
+      const float a = bot * (np + nk), b = top * (nq + nk), c = val * nk;
+      float r = ((a + b) - c) / (nr + nk);
+      if (isinf(r)) r = INFINITY;
+      return r;
+    }
+    default: return bot < top ? bot : (top == top ? top : bot);  /* single: fminf */
+  }
+}
+
+int orc_hclust(const float *D, int64_t n, int method, float lambda, float beta, int *sub,
+               int *sup, float *val) {
+  if (n < 2) return -1;
+  float *d = (float *)malloc(sizeof(float) * (size_t)(n * n));
+  float *cnt = (float *)malloc(sizeof(float) * (size_t)n);
+  float *mv = (float *)malloc(sizeof(float) * (size_t)n);
+  int64_t *mc = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+  if (!d || !cnt || !mv || !mc) {
+    free(d); free(cnt); free(mv); free(mc);
+    return -3;
+  }
+  memcpy(d, D, sizeof(float) * (size_t)(n * n));
+  for (int64_t i = 0; i < n; i++) {
+    d[i * n + i] = INFINITY;
+    cnt[i] = 1.f;
+  }
+  for (int64_t it = 0; it + 1 < n; it++) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(orc_get_threads())
+    for (int64_t row = 0; row < n; row++) {
+      float bv = INFINITY;
+      int64_t bc = 0;
+      if (cnt[row] > 0.f) {
+        for (int64_t col = 0; col <= row; col++) {
+          const float t = d[row * n + col];
+          if (hc_before(t, col, bv, bc)) { bv = t; bc = col; }
+        }
+      }
+      mv[row] = bv;
+      mc[row] = bc;
+    }
+    float bv = INFINITY;
+    int64_t br = 0;
+    for (int64_t row = 0; row < n; row++)
+      if (cnt[row] > 0.f && hc_before(mv[row], row, bv, br)) { bv = mv[row]; br = row; }
+    const int64_t c = mc[br], r = br;
+    sub[it] = (int)c;
+    sup[it] = (int)r;
+    val[it] = bv;
+    cnt[r] += cnt[c];
+    cnt[c] = -cnt[c];
+    const float nr = cnt[r], np = -cnt[c];
+    for (int64_t col = 0; col < n; col++) {
+      const float top = d[c * n + col], bot = d[r * n + col];
+      float nv = orc_hc_update(method, top, bot, nr, np, cnt[col], bv, lambda, beta);
+      if (col == c || col == r || (method == HC_WARD && nr == -cnt[col])) nv = INFINITY;
+      d[r * n + col] = nv;
+      d[col * n + r] = nv;
+    }
+    for (int64_t col = 0; col < n; col++) {
+      d[c * n + col] = INFINITY;
+      d[col * n + c] = INFINITY;
+    }
+  }
+  free(d); free(cnt); free(mv); free(mc);
+  return 0;
+}
+
+/* formatClustering + getPrintOrder (src/rinterface.cpp): R's merge matrix
+ * (column-major len x 2; -(i+1) a point, j+1 the cluster of step j) and the
+ * dendrogram order, the depth-first walk kept on an explicit stack. */
+void orc_format_clustering(int len, const int *sub, const int *sup, int *merge, int *order) {
+  for (int i = 0; i < len; i++) {
+    merge[i] = -(sub[i] + 1);
+    merge[i + len] = -(sup[i] + 1);
+  }
+  for (int i = 0; i < len; i++) {
+    for (int j = i + 1; j < len; j++) {
+      if (merge[j] == merge[i] || merge[j] == merge[i + len]) merge[j] = i + 1;
+      if (merge[j + len] == merge[i] || merge[j + len] == merge[i + len]) merge[j + len] = i + 1;
+      if ((merge[j + len] < 0 && merge[j] > 0) ||
+          (merge[j] > 0 && merge[j + len] > 0 && merge[j] > merge[j + len])) {
+        const int h = merge[j];
+        merge[j] = merge[j + len];
+        merge[j + len] = h;
+      }
+    }
+  }
+  if (len < 1) return;
+  int *stack = (int *)malloc(sizeof(int) * (size_t)(2 * len + 2));
+  int top = 0, otop = len;
+  stack[top++] = len - 1;
+  while (top > 0) {
+    const int level = stack[--top];
+    /* the recursion visits the right child, then the left: push left first */
+    const int left = merge[level], right = merge[level + len];
+    if (left < 0) stack[top++] = -1 - (-left);  /* leaf marker: -(point + 2) */
+    else stack[top++] = left - 1;
+    if (right < 0) stack[top++] = -1 - (-right);
+    else stack[top++] = right - 1;
+    while (top > 0 && stack[top - 1] < 0) {
+      order[otop--] = -(stack[--top] + 1);
+    }
+  }
+  free(stack);
+}

@@ -87,6 +87,19 @@ int orc_mds_stress(const float *X, int64_t n, int64_t dim, const float *delta,
 int orc_bspline_mi(int nbins, int order, int64_t n, const float *X, int64_t nx,
                    const float *Y, int64_t ny, double *out, double *hx, double *hy);
 
+/* Hierarchical clustering as the reference's kernels do it (see oracle.c):
+ * D the full n x n float matrix (read only); sub/sup/val receive n - 1 steps.
+ * orc_hc_method maps a method name as getClusterEnum does; lambda and beta
+ * are 0.5 in every reference entry point. */
+int orc_hc_method(const char *name);
+float orc_hc_update(int method, float top, float bot, float nr, float np, float nk, float val,
+                    float lambda, float beta);
+int orc_hclust(const float *D, int64_t n, int method, float lambda, float beta, int *sub,
+               int *sup, float *val);
+/* formatClustering (src/rinterface.cpp): merge (len x 2, column-major) and
+ * the 1-based dendrogram order of len + 1 points. */
+void orc_format_clustering(int len, const int *sub, const int *sup, int *merge, int *order);
+
 #ifdef __cplusplus
 }
 #endif
