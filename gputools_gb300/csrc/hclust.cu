@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -34,7 +35,7 @@ namespace gt {
 
 namespace {
 
-constexpr int kHcThreads = 1024;
+constexpr int kHcThreads = 512;
 enum { HC_SINGLE = 0, HC_COMPLETE, HC_WPGMA, HC_AVERAGE, HC_MEDIAN, HC_CENTROID,
        HC_FLEXIBLE_GROUP, HC_FLEXIBLE, HC_WARD, HC_MCQUITTY };
 
@@ -50,6 +51,8 @@ int hc_method(const char *name) {
     if (name && std::strcmp(name, names[i]) == 0) return ids[i];
   return HC_SINGLE;
 }
+
+__device__ __forceinline__ int64_t cdiv_d(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // (v1, c1) before (v2, c2): value, then index mod 32, then index; NaN never.
 __device__ __forceinline__ bool hc_before(float v1, int c1, float v2, int c2) {
@@ -102,20 +105,17 @@ __device__ float hc_update(int method, float top, float bot, float nr, float np,
   }
 }
 
-// Diagonal to +inf (convert_kernel), unit counts, and every row's minimum
+// Diagonal to +inf (convert_kernel) and every row's minimum
 // over columns 0..row: one warp per row, lanes strided by 32 as the reference.
 __global__ void __launch_bounds__(256)
-hc_init_kernel(float *__restrict__ D, int64_t n, float *__restrict__ count,
-               float *__restrict__ minv, int *__restrict__ minc) {
+hc_init_kernel(float *__restrict__ D, int64_t n, float *__restrict__ minv,
+               int *__restrict__ minc) {
   const unsigned FULL = 0xffffffffu;
   const int64_t row = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
   if (row >= n) return;
   const int lane = threadIdx.x & 31;
   float *p = D + row * n;
-  if (lane == 0) {
-    p[row] = INFINITY;
-    count[row] = 1.f;
-  }
+  if (lane == 0) p[row] = INFINITY;
   __syncwarp();
   float v = INFINITY;
   int c = 0;
@@ -135,124 +135,372 @@ hc_init_kernel(float *__restrict__ D, int64_t n, float *__restrict__ count,
   }
 }
 
-// Block-wide smallest (v, c) by hc_before; every thread gets the result.
-__device__ __forceinline__ void hc_block_min(float &v, int &c, float *sv, int *sc) {
+// A candidate minimum: value, the index its ties are ordered by (column for
+// a row's minimum, row for the smallest row minimum) and the other index.
+struct alignas(16) HcCand {
+  float v;
+  int k;
+  int a;
+  int pad;
+};
+// What a CTA publishes after each merge: the smallest kept minimum of its
+// rows (r and c excluded) and its part of the kept row r's new minimum.
+struct alignas(32) HcSlot {
+  HcCand x, rm;
+};
+
+constexpr int kHcWarps = kHcThreads / 32;
+constexpr int kHcRescan = 2;  // rows scanned again within the step's reduction
+constexpr int kHcCands = 2 + kHcRescan;
+constexpr int kHcPre = 4;     // owned columns per thread loaded at once
+constexpr int kHcMaxCtas = 16;
+
+__device__ __forceinline__ HcCand hc_cand(float v, int k, int a) { return HcCand{v, k, a, 0}; }
+__device__ __forceinline__ HcCand hc_none() { return HcCand{INFINITY, 0, 0, 0}; }
+__device__ __forceinline__ void hc_take(HcCand &best, const HcCand &o) {
+  if (hc_before(o.v, o.k, best.v, best.k)) best = o;
+}
+// Order-preserving keys: hc_before(v1, c1, v2, c2) <=> (vkey(v1), ikey(c1)) <
+// (vkey(v2), ikey(c2)) lexicographically, for non-NaN values (-0 and +0 tie;
+// a NaN, never chosen, maps above +inf).
+__device__ __forceinline__ unsigned hc_vkey(float v) {
+  if (v != v) return 0xffffffffu;
+  const unsigned u = __float_as_uint(v == 0.f ? 0.f : v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ unsigned hc_ikey(int k) {
+  const unsigned u = unsigned(k);
+  return ((u & 31u) << 27) | (u >> 5);
+}
+// Warp-wide smallest candidate, for every lane: two redux.sync on the keys.
+__device__ __forceinline__ void hc_warp_min(HcCand &c) {
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float ov = __shfl_xor_sync(FULL, v, o);
-    const int oc = __shfl_xor_sync(FULL, c, o);
-    if (hc_before(ov, oc, v, c)) { v = ov; c = oc; }
-  }
-  if (lane == 0) { sv[w] = v; sc[w] = c; }
-  __syncthreads();
-  if (w == 0) {
-    v = sv[lane];
-    c = sc[lane];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(FULL, v, o);
-      const int oc = __shfl_xor_sync(FULL, c, o);
-      if (hc_before(ov, oc, v, c)) { v = ov; c = oc; }
-    }
-    if (lane == 0) { sv[32] = v; sc[32] = c; }
-  }
-  __syncthreads();
-  v = sv[32];
-  c = sc[32];
-  __syncthreads();  // sv / sc may be reused at once
+  const unsigned vk = hc_vkey(c.v), ik = hc_ikey(c.k);
+  const unsigned mv = __reduce_min_sync(FULL, vk);
+  const unsigned mi = __reduce_min_sync(FULL, vk == mv ? ik : 0xffffffffu);
+  const int src = __ffs(__ballot_sync(FULL, vk == mv && ik == mi)) - 1;
+  c.v = __shfl_sync(FULL, c.v, src);
+  c.k = __shfl_sync(FULL, c.k, src);
+  c.a = __shfl_sync(FULL, c.a, src);
 }
 
-// All n - 1 merges in one CTA.
+// Block-wide smallest of c[0..nc) (nc block-uniform); every thread gets the
+// results.  s: kHcCands * (kHcWarps + 1) candidates, alternated between
+// consecutive calls (two barriers apart, so no barrier is needed after).
+__device__ __forceinline__ void hc_block_min(HcCand (&c)[kHcCands], int nc, HcCand *s) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < kHcCands; j++)
+    if (j < nc) hc_warp_min(c[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < kHcCands; j++)
+      if (j < nc) s[j * kHcWarps + w] = c[j];
+  }
+  __syncthreads();
+  if (w < nc) {
+    HcCand t = lane < kHcWarps ? s[w * kHcWarps + lane] : hc_none();
+    hc_warp_min(t);
+    if (lane == 0) s[kHcCands * kHcWarps + w] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kHcCands; j++)
+    if (j < nc) c[j] = s[kHcCands * kHcWarps + j];
+}
+
+// Thread-block cluster primitives: this CTA's rank, the cluster barrier
+// (release / acquire), and loads from another CTA's shared memory.
+__device__ __forceinline__ int hc_cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return int(r);
+}
+__device__ __forceinline__ void hc_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned hc_dsmem(const void *p, int rank) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
+  unsigned out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(a), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ void hc_st_dsmem4(unsigned addr, float4 v) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ float hc_ld_dsmem(unsigned addr) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+// This thread's part of row `row`'s minimum over columns 0..row, columns c
+// and r left out (the caller accounts for them).  Read through L2.
+__device__ __forceinline__ void hc_scan_row(const float *__restrict__ D, int64_t n, int64_t row,
+                                            int c, int r, HcCand &best) {
+  const int tid = threadIdx.x;
+  const float *p = D + row * n;
+  const int64_t len = row + 1;
+  const int64_t mis = int64_t(reinterpret_cast<uintptr_t>(p) >> 2) & 3;
+  const int64_t h = len < ((4 - mis) & 3) ? len : ((4 - mis) & 3);
+  auto take = [&](float t, int64_t col) {
+    if (col != c && col != r) hc_take(best, hc_cand(t, int(col), 0));
+  };
+  if (tid < h) take(__ldcg(p + tid), tid);
+  const float4 *q = reinterpret_cast<const float4 *>(p + h);
+  const int64_t n4 = (len - h) >> 2;
+  for (int64_t base = 0; base < n4; base += 4 * kHcThreads) {
+    float4 f[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int64_t j = base + u * kHcThreads + tid;
+      f[u] = j < n4 ? __ldcg(q + j) : make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int64_t j = base + u * kHcThreads + tid;
+      if (j < n4) {
+        const int64_t c0 = h + 4 * j;
+        take(f[u].x, c0);
+        take(f[u].y, c0 + 1);
+        take(f[u].z, c0 + 2);
+        take(f[u].w, c0 + 3);
+      }
+    }
+  }
+  const int64_t t0 = h + 4 * n4 + tid;
+  if (t0 < len) take(__ldcg(p + t0), t0);
+}
+
+// Writes this CTA's slot into slot [buf][b] of every CTA of the cluster.
+__device__ __forceinline__ void hc_push(HcSlot (*slots)[kHcMaxCtas], int buf, int b, int G,
+                                        const HcCand &x, const HcCand &rm) {
+  const int tid = threadIdx.x;
+  if (tid < G) {
+    const unsigned a = hc_dsmem(&slots[buf][b], tid);
+    hc_st_dsmem4(a, make_float4(x.v, __int_as_float(x.k), __int_as_float(x.a), 0.f));
+    hc_st_dsmem4(a + 16, make_float4(rm.v, __int_as_float(rm.k), __int_as_float(rm.a), 0.f));
+  }
+}
+
+// All n - 1 merges in one thread-block cluster of G <= 16 CTAs (one launch,
+// its CTAs co-scheduled by the hardware).  CTA b owns the indices [lo, hi) =
+// [n b / G, n (b + 1) / G): their columns in each update and their rows'
+// kept minima, in its shared memory.  Counts: with REP every CTA keeps all n
+// (updated by each merge), otherwise each CTA its own, read by the others
+// from its shared memory.  Step t:
+//   A. every warp reduces the G slots that the CTAs wrote into this CTA's
+//      shared memory in the previous step to the merge (v, r, c) and to the
+//      previous kept row's new minimum;
+//   B. list the owned rows whose minimum sat in column c or r; load rows c
+//      and r at the owned columns and the listed rows (columns c and r left
+//      out) together; write the new row / column r, row / column c = +inf;
+//      compare the other owned rows' kept minima with the new (x, r); one
+//      block reduction gives the owned rows' smallest minimum, the owned part
+//      of row r's minimum and the listed rows' minima;
+//   C. write the slot into every CTA (double-buffered) and pass the cluster
+//      barrier (release / acquire), which also orders the D writes before
+//      any other CTA's reads of them (through L2).
+template <bool REP>
 __global__ void __launch_bounds__(kHcThreads, 1)
 hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float beta,
-               float *__restrict__ count, float *__restrict__ minv, int *__restrict__ minc,
-               float *__restrict__ scratch, int *__restrict__ list, int *__restrict__ sub,
-               int *__restrict__ sup, float *__restrict__ val) {
-  __shared__ float sv[33];
-  __shared__ int sc[33];
+               const float *__restrict__ minv0, const int *__restrict__ minc0,
+               int *__restrict__ sub, int *__restrict__ sup, float *__restrict__ val) {
+  extern __shared__ __align__(16) float hc_smem[];
+  __shared__ HcSlot s_slots[2][kHcMaxCtas];
+  __shared__ HcCand sred[2][kHcCands * (kHcWarps + 1)];
   __shared__ int nlist;
-  const int tid = threadIdx.x;
+  const int G = int(gridDim.x), b = hc_cluster_rank(), tid = threadIdx.x, lane = tid & 31;
+  const int64_t lo = n * b / G, hi = n * (b + 1) / G, smax = cdiv_d(n, G);
+  float *s_minv = hc_smem;
+  int *s_minc = reinterpret_cast<int *>(s_minv + smax);
+  int *s_list = s_minc + smax;
+  float *s_cnt = reinterpret_cast<float *>(s_list + smax);  // n (REP) or smax entries
+  auto cnt_own = [&](int64_t i) -> float & { return REP ? s_cnt[i] : s_cnt[i - lo]; };
+  int sb = 0;
+
+  HcCand cand[kHcCands];
+#pragma unroll
+  for (int j = 0; j < kHcCands; j++) cand[j] = hc_none();
+  if (REP) {
+    for (int64_t i = tid; i < n; i += kHcThreads) s_cnt[i] = 1.f;
+  }
+  for (int64_t i = lo + tid; i < hi; i += kHcThreads) {
+    const float mv = minv0[i];
+    const int mc = minc0[i];
+    s_minv[i - lo] = mv;
+    s_minc[i - lo] = mc;
+    if (!REP) s_cnt[i - lo] = 1.f;
+    hc_take(cand[0], hc_cand(mv, int(i), mc));
+  }
+  if (tid == 0) nlist = 0;
+  hc_block_min(cand, 2, sred[sb]);
+  sb ^= 1;
+  hc_cluster_sync();  // every CTA has started before shared memory is written remotely
+  hc_push(s_slots, 0, b, G, cand[0], cand[1]);
+  hc_cluster_sync();
+  int pr = -1, pc = -1;
+  float prf = 0.f, pcf = 0.f;  // the previous merge's rows and their counts after it
+
   for (int64_t it = 0; it + 1 < n; it++) {
-    // the smallest kept minimum over the active rows (find_min2_kernel)
-    float v = INFINITY;
-    int rw = 0;
-    for (int64_t x = tid; x < n; x += kHcThreads)
-      if (count[x] > 0.f && hc_before(minv[x], int(x), v, rw)) { v = minv[x]; rw = int(x); }
-    hc_block_min(v, rw, sv, sc);
-    const int r = rw, c = minc[r];
-    __syncthreads();  // every thread has read minc[r] before it changes
+    // A. the merge
+    const int par = int(it & 1);
+    HcCand x = hc_none(), y = hc_none();
+    if (lane < G) {
+      const HcSlot &sl = s_slots[par][lane];
+      x = sl.x;
+      y = sl.rm;
+    }
+    hc_warp_min(x);
+    hc_warp_min(y);
+    if (pr >= 0 && prf > 0.f) hc_take(x, hc_cand(y.v, pr, y.k));
+    const float v = x.v;
+    const int r = x.k, c = x.a;
+    auto cnt_any = [&](int64_t i) -> float {
+      if (REP) return s_cnt[i];
+      if (i == pc) return pcf;  // their owners store these now
+      if (i == pr) return prf;
+      const int o = int(((i + 1) * G - 1) / n);
+      return o == b ? s_cnt[i - lo] : hc_ld_dsmem(hc_dsmem(&s_cnt[i - n * o / G], o));
+    };
+    // counts as src/hcluster.cpp updates them (cnt[r] += cnt[c]; cnt[c] = -cnt[c])
+    const float cr0 = cnt_any(r), cc0 = cnt_any(c);
+    const float a = cr0 + cc0;
+    const float cfin = -(c == r ? a : cc0);
+    const float rfin = c == r ? cfin : a;
+    const float nr = rfin, np = -cfin;
     if (tid == 0) {
-      sub[it] = c;
-      sup[it] = r;
-      val[it] = v;
-      // hcluster.cpp's statement order, which also fixes the sizes when an
-      // all-infinite row makes c == r
-      count[r] += count[c];
-      count[c] = -count[c];
-      sv[0] = count[r];
-      sv[1] = -count[c];
-      minv[c] = INFINITY;
-      minc[c] = 0;
+      if (pr >= lo && pr < hi) {
+        s_minv[pr - lo] = y.v;
+        s_minc[pr - lo] = y.k;
+        if (!REP) s_cnt[pr - lo] = prf;
+      }
+      if (!REP && pc >= lo && pc < hi) s_cnt[pc - lo] = pcf;  // after pr: pc == pr keeps pcf
+      if (b == 0) {
+        sub[it] = c;
+        sup[it] = r;
+        val[it] = v;
+      }
+    }
+
+    // B. rows to scan again (pr's values from registers: stored just now)
+    for (int64_t i = lo + tid; i < hi; i += kHcThreads) {
+      if (i <= c || i == r) continue;
+      const float ci = (!REP && i == pc) ? pcf : (!REP && i == pr) ? prf : cnt_own(i);
+      if (!(ci > 0.f)) continue;
+      const int mc = i == pr ? y.k : s_minc[i - lo];
+      if (mc == c || (i > r && mc == r)) s_list[atomicAdd(&nlist, 1)] = int(i);
+    }
+    __syncthreads();
+    const int L = nlist, L1 = L < kHcRescan ? L : kHcRescan;
+#pragma unroll
+    for (int j = 0; j < kHcCands; j++) cand[j] = hc_none();
+    for (int64_t base = lo; base < hi; base += int64_t(kHcPre) * kHcThreads) {
+      float top[kHcPre], bot[kHcPre];
+#pragma unroll
+      for (int u = 0; u < kHcPre; u++) {
+        const int64_t i = base + u * kHcThreads + tid;
+        top[u] = i < hi ? __ldcg(D + int64_t(c) * n + i) : 0.f;
+        bot[u] = i < hi ? __ldcg(D + int64_t(r) * n + i) : 0.f;
+      }
+      if (base == lo) {
+#pragma unroll
+        for (int e = 0; e < kHcRescan; e++)
+          if (e < L1) hc_scan_row(D, n, s_list[e], c, r, cand[2 + e]);
+      }
+#pragma unroll
+      for (int u = 0; u < kHcPre; u++) {
+        const int64_t i = base + u * kHcThreads + tid;
+        if (i >= hi) continue;
+        const float nk = cnt_own(i);
+        float nv;
+        if (i == c || i == r || (method == HC_WARD && nr == -nk))
+          nv = INFINITY;
+        else
+          nv = hc_update(method, top[u], bot[u], nr, np, nk, v, lambda, beta);
+        if (i <= r) hc_take(cand[1], hc_cand(nv, int(i), 0));
+        D[int64_t(r) * n + i] = nv;
+        D[i * n + r] = nv;
+        D[int64_t(c) * n + i] = INFINITY;
+        D[i * n + c] = INFINITY;
+        if (i == r || i == c || !(nk > 0.f)) continue;
+        float mv = s_minv[i - lo];
+        int mc = s_minc[i - lo];
+        if (i > c && (mc == c || (i > r && mc == r))) {
+#pragma unroll
+          for (int e = 0; e < kHcRescan; e++)
+            if (e < L1 && s_list[e] == i && r <= i) hc_take(cand[2 + e], hc_cand(nv, r, 0));
+        } else {
+          if (i > r && hc_before(nv, r, mv, mc)) {
+            mv = nv;
+            mc = r;
+            s_minv[i - lo] = mv;
+            s_minc[i - lo] = mc;
+          }
+          hc_take(cand[0], hc_cand(mv, int(i), mc));
+        }
+      }
+    }
+    hc_block_min(cand, 2 + L1, sred[sb]);
+    sb ^= 1;
+    HcCand best = cand[0];
+    const HcCand rmin = cand[1];
+#pragma unroll
+    for (int e = 0; e < kHcRescan; e++) {
+      if (e < L1) {
+        const int row = s_list[e];
+        if (tid == 0) {
+          s_minv[row - lo] = cand[2 + e].v;
+          s_minc[row - lo] = cand[2 + e].k;
+        }
+        hc_take(best, hc_cand(cand[2 + e].v, row, cand[2 + e].k));
+      }
+    }
+    for (int e0 = kHcRescan; e0 < L; e0 += kHcRescan) {  // more rows: further rounds
+#pragma unroll
+      for (int j = 0; j < kHcCands; j++) cand[j] = hc_none();
+#pragma unroll
+      for (int e = 0; e < kHcRescan; e++) {
+        if (e0 + e < L) {
+          const int row = s_list[e0 + e];
+          hc_scan_row(D, n, row, c, r, cand[e]);
+          // (row, r) was written by this CTA in this step
+          if (tid == 0 && r <= row) hc_take(cand[e], hc_cand(__ldcg(D + int64_t(row) * n + r), r, 0));
+        }
+      }
+      const int m = L - e0 < kHcRescan ? L - e0 : kHcRescan;
+      hc_block_min(cand, m, sred[sb]);
+      sb ^= 1;
+#pragma unroll
+      for (int e = 0; e < kHcRescan; e++) {
+        if (e < m) {
+          const int row = s_list[e0 + e];
+          if (tid == 0) {
+            s_minv[row - lo] = cand[e].v;
+            s_minc[row - lo] = cand[e].k;
+          }
+          hc_take(best, hc_cand(cand[e].v, row, cand[e].k));
+        }
+      }
+    }
+
+    // C. publish
+    if (tid == 0) {
       nlist = 0;
-    }
-    __syncthreads();
-    const float nr = sv[0], np = sv[1];
-    __syncthreads();
-    // the kept row's new entries
-    for (int64_t col = tid; col < n; col += kHcThreads) {
-      float nv;
-      const float nk = count[col];
-      if (col == c || col == r || (method == HC_WARD && nr == -nk))
-        nv = INFINITY;
-      else
-        nv = hc_update(method, D[int64_t(c) * n + col], D[int64_t(r) * n + col], nr, np, nk, v,
-                       lambda, beta);
-      scratch[col] = nv;
-    }
-    __syncthreads();
-    for (int64_t col = tid; col < n; col += kHcThreads) {
-      const float nv = scratch[col];
-      D[int64_t(r) * n + col] = nv;
-      D[col * n + r] = nv;
-      D[int64_t(c) * n + col] = INFINITY;
-      D[col * n + c] = INFINITY;
-    }
-    __syncthreads();
-    // kept minima: rows below c that lost their minimum's column, rows below
-    // r that may gain the new (x, r)
-    for (int64_t x = int64_t(c) + 1 + tid; x < n; x += kHcThreads) {
-      if (x == r || !(count[x] > 0.f)) continue;
-      const int mc = minc[x];
-      if (mc == c || (x > r && mc == r)) {
-        list[atomicAdd(&nlist, 1)] = int(x);
-      } else if (x > r) {
-        const float t = scratch[x];
-        if (hc_before(t, r, minv[x], mc)) { minv[x] = t; minc[x] = r; }
+      if (REP) {
+        s_cnt[r] = rfin;
+        s_cnt[c] = cfin;  // after r: c == r keeps cfin
       }
     }
-    if (tid == 0) list[atomicAdd(&nlist, 1)] = r;
-    __syncthreads();
-    const int cnt = nlist;
-    for (int e = 0; e < cnt; e++) {
-      const int x = list[e];
-      const float *p = D + int64_t(x) * n;
-      float bv = INFINITY;
-      int bc = 0;
-      // lanes strided by 32 within each 1024-column stretch: the key order
-      // is total, so any partition gives the reference's result
-      for (int64_t col = tid; col <= x; col += kHcThreads) {
-        const float t = p[col];
-        if (hc_before(t, int(col), bv, bc)) { bv = t; bc = int(col); }
-      }
-      hc_block_min(bv, bc, sv, sc);
-      if (tid == 0) {
-        minv[x] = bv;
-        minc[x] = bc;
-      }
-    }
-    __syncthreads();
+    hc_push(s_slots, par ^ 1, b, G, best, rmin);
+    pr = r;
+    pc = c;
+    prf = rfin;
+    pcf = cfin;
+    hc_cluster_sync();
   }
 }
 
@@ -317,23 +565,55 @@ int hclust_device(float *dD, int64_t n, const char *method, int *sub, int *sup, 
                   cudaStream_t s) {
   if (n < 2) return fail(GT_EINVAL, "must have n >= 2 objects to cluster");
   if (n > 2147483647LL / 2) return fail(GT_EINVAL, "too many objects");
-  const int m = hc_method(method);
+  int m = hc_method(method);
+  // one cluster of up to 16 CTAs, at least ~64 indices each
+  int G = int(std::min<int64_t>(kHcMaxCtas, cdiv(n, 64)));
+  if (const char *e = std::getenv("GT_HCLUST_CTAS")) G = std::max(1, std::min(G, std::atoi(e)));
+  // shared memory: kept minima, rescan list, counts (all n when they fit)
+  const size_t cap = size_t(200) * 1024;
+  auto smem_of = [&](int g, bool rep) {
+    return size_t(cdiv(n, g)) * 12 + (rep ? size_t(n) : size_t(cdiv(n, g))) * 4;
+  };
+  const bool rep = smem_of(G, true) <= cap;
+  auto kern = rep ? hc_loop_kernel<true> : hc_loop_kernel<false>;
+  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  for (;; G /= 2) {  // the largest cluster that the device can place
+    const size_t smem = G >= 1 ? smem_of(G, rep) : 0;
+    if (G < 1 || smem > cap)
+      return fail(GT_EUNSUPPORTED, "no thread-block cluster large enough for %lld objects",
+                  static_cast<long long>(n));
+    GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(kHcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    GT_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
+    if (nclusters >= 1) break;
+  }
   void *pw = nullptr;
-  const size_t bytes = size_t(n) * (3 * sizeof(float) + 2 * sizeof(int)) +
-                       size_t(n - 1) * (2 * sizeof(int) + sizeof(float)) + 64;
+  const size_t bytes = size_t(n) * 8 + size_t(n - 1) * 12 + 256;
   GT_TRY(ws_get(WS_SCRATCH3, bytes, &pw));
-  float *count = static_cast<float *>(pw);
-  float *minv = count + n, *scratch = minv + n;
-  int *minc = reinterpret_cast<int *>(scratch + n), *list = minc + n;
-  int *dsub = list + n, *dsup = dsub + (n - 1);
+  float *minv = static_cast<float *>(pw);
+  int *minc = reinterpret_cast<int *>(minv + n);
+  int *dsub = minc + n, *dsup = dsub + (n - 1);
   float *dval = reinterpret_cast<float *>(dsup + (n - 1));
   {
     ProfScope prof("hclust", s);
-    hc_init_kernel<<<unsigned(cdiv(n, 8)), 256, 0, s>>>(dD, n, count, minv, minc);
-    hc_loop_kernel<<<1, kHcThreads, 0, s>>>(dD, n, m, 0.5f, 0.5f, count, minv, minc, scratch,
-                                            list, dsub, dsup, dval);
-    count_launch(2);
+    hc_init_kernel<<<unsigned(cdiv(n, 8)), 256, 0, s>>>(dD, n, minv, minc);
     GT_CUDA(cudaGetLastError());
+    GT_CUDA(cudaLaunchKernelEx(&cfg, kern, dD, n, m, 0.5f, 0.5f,
+                               static_cast<const float *>(minv), static_cast<const int *>(minc),
+                               dsub, dsup, dval));
+    count_launch(2);
   }
   GT_CUDA(cudaMemcpyAsync(sub, dsub, size_t(n - 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
   GT_CUDA(cudaMemcpyAsync(sup, dsup, size_t(n - 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
