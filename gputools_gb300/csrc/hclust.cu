@@ -150,7 +150,7 @@ struct alignas(32) HcSlot {
 };
 
 constexpr int kHcWarps = kHcThreads / 32;
-constexpr int kHcRescan = 2;  // rows scanned again within the step's reduction
+constexpr int kHcRescan = 2;  // rows scanned again within the step's reduction (hc_scan_rows: two)
 constexpr int kHcCands = 2 + kHcRescan;
 constexpr int kHcPre = 4;     // owned columns per thread loaded at once
 constexpr int kHcMaxCtas = 16;
@@ -237,42 +237,59 @@ __device__ __forceinline__ float hc_ld_dsmem(unsigned addr) {
   return v;
 }
 
-// This thread's part of row `row`'s minimum over columns 0..row, columns c
-// and r left out (the caller accounts for them).  Read through L2.
-__device__ __forceinline__ void hc_scan_row(const float *__restrict__ D, int64_t n, int64_t row,
-                                            int c, int r, HcCand &best) {
+// This thread's part of the minima of rows row0 and row1 (row1 < 0: none)
+// over columns 0..row, columns c and r left out (the caller accounts for
+// them).  The two rows' loads are issued together; read through L2.
+__device__ __forceinline__ void hc_scan_rows(const float *__restrict__ D, int64_t n, int64_t row0,
+                                             int64_t row1, int c, int r, HcCand &b0, HcCand &b1) {
   const int tid = threadIdx.x;
-  const float *p = D + row * n;
-  const int64_t len = row + 1;
-  const int64_t mis = int64_t(reinterpret_cast<uintptr_t>(p) >> 2) & 3;
-  const int64_t h = len < ((4 - mis) & 3) ? len : ((4 - mis) & 3);
-  auto take = [&](float t, int64_t col) {
+  const float4 inf4 = make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
+  const float *p0 = D + row0 * n, *p1 = D + (row1 < 0 ? 0 : row1) * n;
+  const int64_t len0 = row0 + 1, len1 = row1 + 1;  // len1 = 0 for no row
+  auto head = [&](const float *p, int64_t len) {
+    const int64_t mis = int64_t(reinterpret_cast<uintptr_t>(p) >> 2) & 3;
+    return len < ((4 - mis) & 3) ? len : ((4 - mis) & 3);
+  };
+  const int64_t h0 = head(p0, len0), h1 = head(p1, len1);
+  const int64_t m0 = (len0 - h0) >> 2, m1 = (len1 - h1) >> 2;
+  const float4 *q0 = reinterpret_cast<const float4 *>(p0 + h0);
+  const float4 *q1 = reinterpret_cast<const float4 *>(p1 + h1);
+  auto take = [&](HcCand &best, float t, int64_t col) {
     if (col != c && col != r) hc_take(best, hc_cand(t, int(col), 0));
   };
-  if (tid < h) take(__ldcg(p + tid), tid);
-  const float4 *q = reinterpret_cast<const float4 *>(p + h);
-  const int64_t n4 = (len - h) >> 2;
-  for (int64_t base = 0; base < n4; base += 4 * kHcThreads) {
-    float4 f[4];
+  if (tid < h0) take(b0, __ldcg(p0 + tid), tid);
+  if (tid < h1) take(b1, __ldcg(p1 + tid), tid);
+  const int64_t mm = m0 > m1 ? m0 : m1;
+  for (int64_t base = 0; base < mm; base += 4 * kHcThreads) {
+    float4 f0[4], f1[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const int64_t j = base + u * kHcThreads + tid;
-      f[u] = j < n4 ? __ldcg(q + j) : make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
+      f0[u] = j < m0 ? __ldcg(q0 + j) : inf4;
+      f1[u] = j < m1 ? __ldcg(q1 + j) : inf4;
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const int64_t j = base + u * kHcThreads + tid;
-      if (j < n4) {
-        const int64_t c0 = h + 4 * j;
-        take(f[u].x, c0);
-        take(f[u].y, c0 + 1);
-        take(f[u].z, c0 + 2);
-        take(f[u].w, c0 + 3);
+      if (j < m0) {
+        const int64_t c0 = h0 + 4 * j;
+        take(b0, f0[u].x, c0);
+        take(b0, f0[u].y, c0 + 1);
+        take(b0, f0[u].z, c0 + 2);
+        take(b0, f0[u].w, c0 + 3);
+      }
+      if (j < m1) {
+        const int64_t c1 = h1 + 4 * j;
+        take(b1, f1[u].x, c1);
+        take(b1, f1[u].y, c1 + 1);
+        take(b1, f1[u].z, c1 + 2);
+        take(b1, f1[u].w, c1 + 3);
       }
     }
   }
-  const int64_t t0 = h + 4 * n4 + tid;
-  if (t0 < len) take(__ldcg(p + t0), t0);
+  const int64_t t0 = h0 + 4 * m0 + tid, t1 = h1 + 4 * m1 + tid;
+  if (t0 < len0) take(b0, __ldcg(p0 + t0), t0);
+  if (t1 < len1) take(b1, __ldcg(p1 + t1), t1);
 }
 
 // Writes this CTA's slot into slot [buf][b] of every CTA of the cluster.
@@ -406,11 +423,8 @@ hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float
         top[u] = i < hi ? __ldcg(D + int64_t(c) * n + i) : 0.f;
         bot[u] = i < hi ? __ldcg(D + int64_t(r) * n + i) : 0.f;
       }
-      if (base == lo) {
-#pragma unroll
-        for (int e = 0; e < kHcRescan; e++)
-          if (e < L1) hc_scan_row(D, n, s_list[e], c, r, cand[2 + e]);
-      }
+      if (base == lo && L1 > 0)
+        hc_scan_rows(D, n, s_list[0], L1 > 1 ? s_list[1] : -1, c, r, cand[2], cand[3]);
 #pragma unroll
       for (int u = 0; u < kHcPre; u++) {
         const int64_t i = base + u * kHcThreads + tid;
@@ -462,11 +476,11 @@ hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float
     for (int e0 = kHcRescan; e0 < L; e0 += kHcRescan) {  // more rows: further rounds
 #pragma unroll
       for (int j = 0; j < kHcCands; j++) cand[j] = hc_none();
+      hc_scan_rows(D, n, s_list[e0], e0 + 1 < L ? s_list[e0 + 1] : -1, c, r, cand[0], cand[1]);
 #pragma unroll
       for (int e = 0; e < kHcRescan; e++) {
         if (e0 + e < L) {
           const int row = s_list[e0 + e];
-          hc_scan_row(D, n, row, c, r, cand[e]);
           // (row, r) was written by this CTA in this step
           if (tid == 0 && r <= row) hc_take(cand[e], hc_cand(__ldcg(D + int64_t(row) * n + r), r, 0));
         }
