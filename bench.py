@@ -542,8 +542,9 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     on 4000 x 100, gpuCor kendall (500 obs x 1000 integer variables, bit-exact
     spot check) and pearson (500 x 1000), gpuDist euclidean 2000 x 64 through
     the host C ABI, the adjoints (gpuCorBackward 1024 x 4096 with a
-    symmetric 4096 x 4096 upstream; MDS stress on 8192 x 32) and gpuMi
-    (2000 variables x 1000 samples, 10 bins, order 3)."""
+    symmetric 4096 x 4096 upstream; MDS stress on 8192 x 32), gpuMi
+    (2000 variables x 1000 samples, 10 bins, order 3) and gpuHclust (10000
+    points, average linkage)."""
     import torch
     import oracle
     sptr = ctypes.c_void_p(stream.cuda_stream)
@@ -652,8 +653,54 @@ def run_configs(lib, g, _lib, stream, dev, steps):
                                   "cuda_core_ms": ms_cc, "max_abs_err_sample": err}
     del dXi, mi
     torch.cuda.empty_cache()
+    out["hclust"] = run_hclust(g, dev)
     out["batch"] = run_batches(g, stream, dev, k)
     return out
+
+
+def run_hclust(g, dev):
+    """gpuHclust, average linkage, on the euclidean distances of 10000 points
+    in 16 dimensions drawn around 8 centres: the merge loop alone (a fresh
+    copy of the device matrix per call; the call returns merges, order and
+    heights on the host), and gpuDistClust end to end from host points.  The
+    oracle runs on the first 1000 points (its loop rescans every row each
+    step, O(n^3)) for the CPU rate and an exact comparison of the merges."""
+    import torch
+    import oracle
+    rng = np.random.default_rng(31)
+    n, d = 10000, 16
+    centres = rng.standard_normal((8, d)) * 4
+    pts = (centres[rng.integers(0, 8, n)] + rng.standard_normal((n, d))).astype(np.float32)
+    dp = torch.from_numpy(pts).to(dev)
+    full = g.distances_device(dp, "euclidean").view(n, n)
+    work = torch.empty_like(full)
+    times = []
+    for rep in range(3):
+        work.copy_(full)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.hclust_device(work, "average")
+        times.append(time.perf_counter() - t0)
+    ms = min(times[1:]) * 1e3
+    del work, full, dp
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    g.gpuDistClust(pts, "euclidean", "average")
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    m = 1000
+    sub = g.gpuDist(pts[:m])
+    dm = sub.to_matrix().astype(np.float32)
+    t0 = time.perf_counter()
+    s_, p_, h_ = oracle.hclust(dm, "average")
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    om, oo = oracle.format_clustering(s_, p_)
+    res = g.gpuHclust(sub, "average")
+    exact = bool(np.array_equal(res.merge, om) and np.array_equal(res.order, oo)
+                 and np.array_equal(res.height.view(np.int32), h_.view(np.int32)))
+    return {"average_10000x16": {"ms": ms, "us_per_merge": ms * 1e3 / (n - 1),
+                                 "gpuDistClust_e2e_ms": e2e_ms},
+            "oracle_cpu_1000_ms": cpu_ms, "oracle_cpu_threads": oracle.threads(),
+            "exact_vs_oracle_1000": exact}
 
 
 def run_batches(g, stream, dev, k):
