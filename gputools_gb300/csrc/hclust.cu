@@ -588,7 +588,9 @@ int hclust_device(float *dD, int64_t n, const char *method, int *sub, int *sup, 
   auto smem_of = [&](int g, bool rep) {
     return size_t(cdiv(n, g)) * 12 + (rep ? size_t(n) : size_t(cdiv(n, g))) * 4;
   };
-  const bool rep = smem_of(G, true) <= cap;
+  bool rep = smem_of(G, true) <= cap;
+  if (const char *e = std::getenv("GT_HCLUST_COUNTS"))  // "owned": the large-n layout at any n
+    if (std::strcmp(e, "owned") == 0) rep = false;
   auto kern = rep ? hc_loop_kernel<true> : hc_loop_kernel<false>;
   GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};

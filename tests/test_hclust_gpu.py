@@ -67,8 +67,8 @@ def test_hclust_matches_oracle(gpu, oracle_mod, method, kind):
 
 
 @pytest.mark.parametrize("method", ["single", "average", "ward", "centroid"])
-def test_hclust_more_rows_than_threads(gpu, oracle_mod, method):
-    # n above the loop's 1024 threads and not a multiple of 32
+def test_hclust_ragged_size(gpu, oracle_mod, method):
+    # 1500 points: not a multiple of 32 nor of the 16 CTAs' slices
     rng = np.random.default_rng(7)
     D = sym(rng, 1500, "points")
     same(run_host(gpu, D, method), want(oracle_mod, D, method))
@@ -174,3 +174,24 @@ def test_gpuDistClust_well_separated_clusters(gpu):
     assert np.all(np.diff(res.height) >= -1e-6)
     assert res.height[-5] < 10 < res.height[-4]
     assert sorted(res.order.tolist()) == list(range(1, 201))
+
+
+@pytest.mark.parametrize("ctas", ["1", "3", "7", "16"])
+@pytest.mark.parametrize("counts", ["auto", "owned"])
+def test_hclust_cluster_sizes_and_count_layouts(gpu, oracle_mod, monkeypatch, ctas, counts):
+    # the merges do not depend on how the indices are split over the CTAs, nor
+    # on where the counts live (all of them in every CTA, or each CTA its own
+    # and the others read through distributed shared memory -- the layout
+    # used above ~40000 points)
+    monkeypatch.setenv("GT_HCLUST_CTAS", ctas)
+    if counts == "owned":
+        monkeypatch.setenv("GT_HCLUST_COUNTS", "owned")
+    rng = np.random.default_rng(16)
+    for n, kind in ((1100, "points"), (257, "ties")):
+        D = sym(rng, n, kind)
+        for method in ("average", "ward", "single"):
+            same(run_host(gpu, D, method), want(oracle_mod, D, method))
+    D = sym(rng, 90)
+    D[:45, 45:] = np.inf
+    D[45:, :45] = np.inf
+    same(run_host(gpu, D, "centroid"), want(oracle_mod, D, "centroid"))
