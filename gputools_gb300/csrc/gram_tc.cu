@@ -745,6 +745,7 @@ struct MiFinish {
   float pscale;          // gscale / nsamples
   int lg;                // log2 of the bins per variable
   int symmetric;
+  unsigned colmask;      // bit j: column j of a 32-column block is a real bin (not padding)
 
   __device__ __forceinline__ static float plog2p(float p) { return p > 0.f ? p * __log2f(p) : 0.f; }
 
@@ -753,8 +754,9 @@ struct MiFinish {
     const int nb = 1 << lg;
     const int64_t x = r >> lg;
     float t[32];
+    // padding bins are zero columns: skipped (the same positions in every lane)
 #pragma unroll
-    for (int j = 0; j < 32; j++) t[j] = plog2p(g[j] * pscale);
+    for (int j = 0; j < 32; j++) t[j] = (colmask >> j) & 1u ? plog2p(g[j] * pscale) : 0.f;
     // segmented sums: t[j] of the first column of each column variable ends
     // up holding the sum over that variable's bins
 #pragma unroll
@@ -1667,14 +1669,19 @@ int tc_error_word(int **p) { return err_word(p); }
 // Mutual information from f16x3 weight planes (rows = variable * 2^lg + bin,
 // each weight times 2^14): the chunked Gram with MiFinish.
 int mi_tc(const void *planesX, int64_t rowsX, const void *planesY, int64_t rowsY, int64_t kpad,
-          int lg, int64_t nx, int64_t ny, int64_t nsamples, const float *hx, const float *hy,
-          float *out, int symmetric, cudaStream_t s) {
+          int lg, int nbins, int64_t nx, int64_t ny, int64_t nsamples, const float *hx,
+          const float *hy, float *out, int symmetric, cudaStream_t s) {
   if (rowsX == 0 || rowsY == 0) return GT_OK;
+  unsigned colmask = 0u;
+  for (int j = 0; j < 32; j++)
+    if ((j & ((1 << lg) - 1)) < nbins) colmask |= 1u << j;
   MiFinish fin{out, hx, hy, nx, ny, nx, float(1.0 / (268435456.0 * double(nsamples))), lg,
-               symmetric};
+               symmetric, colmask};
+  // FP32 chunks of 512 samples: 15 % faster than 256 at 10 bins x 1000 samples, with a
+  // largest MI error of 7.5e-6 bits against the FP64 oracle (4.1e-6 with 256)
   return launch_gram<tc::KIND_F16X3, 32, true>(planesX, rowsX, planesY, rowsY, kpad,
-                                               symmetric ? kUpper : kFull, tc_chunk_kblocks(32),
-                                               fin, "mi_gram", s);
+                                               symmetric ? kUpper : kFull, 512 / 32, fin,
+                                               "mi_gram", s);
 }
 
 // C[r][c] = sum_k A_r[k] B_c[k] over split-bf16 planes ([part][row][kpad]),

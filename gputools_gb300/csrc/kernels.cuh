@@ -68,8 +68,8 @@ int pearson_pairwise_tc(const float *dA, int64_t nA, const float *dB, int64_t nB
 // [variable * 2^lg + bin][kpad], weights times 2^14, zero padded), entropies
 // hx, hy; out[y * nx + x] (symmetric: X == Y, both triangles written).
 int mi_tc(const void *planesX, int64_t rowsX, const void *planesY, int64_t rowsY, int64_t kpad,
-          int lg, int64_t nx, int64_t ny, int64_t nsamples, const float *hx, const float *hy,
-          float *out, int symmetric, cudaStream_t s);
+          int lg, int nbins, int64_t nx, int64_t ny, int64_t nsamples, const float *hx,
+          const float *hy, float *out, int symmetric, cudaStream_t s);
 
 // C[r][c] = sum_k A_r[k] B_c[k] on tcgen05 from `nsplit` (2 or 3) split-bf16
 // planes ([part][row][kpad], kpad a multiple of 64), stored as row-major float.

@@ -256,7 +256,8 @@ int mi_impl(int nbins, int order, int64_t n, const float *dX, int64_t nx, const 
       GT_TRY(prep(order, dX, nx, n, nbins, lg, kpad, px, nullptr, hx, s));
       if (!sym) GT_TRY(prep(order, dY, ny, n, nbins, lg, kpad, py, nullptr, hy, s));
     }
-    return mi_tc(px, nx * nbp, py, ny * nbp, kpad, lg, nx, ny, n, hx, hy, dOut, sym ? 1 : 0, s);
+    return mi_tc(px, nx * nbp, py, ny * nbp, kpad, lg, nbins, nx, ny, n, hx, hy, dOut, sym ? 1 : 0,
+                 s);
   }
   const size_t wx = size_t(nx) * size_t(nbins) * size_t(n) * 4;
   const size_t wy = sym ? 0 : size_t(ny) * size_t(nbins) * size_t(n) * 4;
