@@ -307,6 +307,9 @@ def gpuHclust(distances, method: str = "complete") -> HClust:
             raise ValueError("dissimilarities of improper length")
         warnings.warn("dissimilarities of improper length")
     full = np.ascontiguousarray(distances.to_matrix(), dtype=np.float32)
+    if not np.all(np.isfinite(full)):
+        # .C's default NAOK = FALSE rejects NA/NaN/Inf before the call
+        raise ValueError("NA/NaN/Inf in foreign function call (arg 1)")
     merge = np.empty(2 * (n - 1), np.int32)
     order = np.empty(n, np.int32)
     height = np.empty(n - 1, np.float32)

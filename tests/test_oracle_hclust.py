@@ -238,3 +238,23 @@ def test_host_format_rejects_non_trees(gt):
         gt.hclust_format([0, 0], [1, 1])  # the same pair twice
     with pytest.raises(Exception):
         gt.hclust_format([0], [5])  # index outside 0..len
+
+
+def test_gpuHclust_argument_checks(gt):
+    # R/gpuHclust.R's checks, raised before the library is called
+    from gputools_gb300.api import Dist
+    d = Dist(np.array([1.0, 2.0, 3.0]), 3, "euclidean")
+    with pytest.raises(ValueError, match="invalid clustering method"):
+        gt.gpuHclust(d, "nonsense")
+    with pytest.raises(ValueError, match="invalid clustering method"):
+        gt.gpuHclust(d, "flex")  # ambiguous between flexible and flexible group
+    with pytest.raises(ValueError, match="n >= 2"):
+        gt.gpuHclust(Dist(np.array([]), 1, "euclidean"))
+    with pytest.raises(ValueError, match="improper length"):
+        gt.gpuHclust(Dist(np.array([1.0, 2.0]), 3, "euclidean"))
+    with pytest.raises(ValueError, match="NA/NaN/Inf"):
+        gt.gpuHclust(Dist(np.array([1.0, np.inf, 3.0]), 3, "euclidean"))
+    with pytest.raises(ValueError, match="invalid distance method"):
+        gt.gpuDistClust(np.zeros((3, 2)), "euclidian")  # the alias does not reach distmethod
+    with pytest.raises(ValueError, match="NA/NaN/Inf"):
+        gt.gpuDistClust(np.array([[0.0, np.nan], [1.0, 2.0]]))
