@@ -17,11 +17,14 @@
 // other rows below r compare their kept minimum with the new (x, r).  Ties
 // are broken as the reference's 32-lane strided scan and tree reduction break
 // them (value, then column mod 32, then column; rows likewise), so the merges
-// are the reference's.  One CTA runs all merges (no inter-CTA waits: the
-// per-merge work is O(n) and latency-bound), after a multi-CTA kernel that
-// initialises the kept minima.  The linkage expressions are evaluated as the
-// reference writes them (float, with its double promotions), each operation
-// rounded on its own.
+// are the reference's.  All merges run in one launch of a thread-block
+// cluster (up to 16 CTAs exchanging their candidates through distributed
+// shared memory, one hardware cluster barrier per merge), after a multi-CTA
+// kernel that initialises the kept minima.  The linkage expressions are
+// evaluated as the reference writes them (float, with its double
+// promotions), each operation rounded on its own; the reference compiles
+// them with NVRTC --use_fast_math, so its own rounding is the compiler's
+// choice of contractions.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -210,7 +213,7 @@ __device__ __forceinline__ void hc_block_min(HcCand (&c)[kHcCands], int nc, HcCa
 }
 
 // Thread-block cluster primitives: this CTA's rank, the cluster barrier
-// (release / acquire), and loads from another CTA's shared memory.
+// (release / acquire), and accesses to another CTA's shared memory.
 __device__ __forceinline__ int hc_cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
