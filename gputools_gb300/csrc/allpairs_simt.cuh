@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -76,6 +77,25 @@ __device__ __forceinline__ void simt_store(float *sm, const float4 (&reg)[ROWS *
 // Out concept:
 //   __device__ void operator()(int64_t r, int64_t c, const float (&acc)[NACC],
 //                              bool mirror) const;
+// optionally, for one value per entry whose mirror is written through shared
+// memory (coalesced) instead of one scattered store per entry:
+//   static constexpr bool kStagedMirror = true;
+//   __device__ bool staged(bool mirror) const;       this tile goes that way
+//   __device__ float value(int64_t r, int64_t c, const float (&acc)[NACC]) const;
+//   __device__ void store(int64_t r, int64_t c, float v) const;
+//   static constexpr bool kSkipPad = true;     optional: the last k-slab stops
+//                                              at K instead of computing its padding
+//                                              (for costly steps or small K; the
+//                                              check slows the cheap steps down)
+template <class T, class = void>
+struct SkipPad : std::false_type {};
+template <class T>
+struct SkipPad<T, std::void_t<decltype(T::kSkipPad)>> : std::bool_constant<T::kSkipPad> {};
+template <class T, class = void>
+struct HasStagedMirror : std::false_type {};
+template <class T>
+struct HasStagedMirror<T, std::void_t<decltype(T::kStagedMirror)>>
+    : std::bool_constant<T::kStagedMirror> {};
 template <class Op, class Out, int TM, int TN>
 __global__ void __launch_bounds__(kSimtThreads)
 allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
@@ -114,6 +134,9 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
     const float *pb = sB[buf];
 #pragma unroll
     for (int kk = 0; kk < kSimtBK / 4; kk++) {
+      if constexpr (SkipPad<Op>::value) {
+        if (kb * kSimtBK + kk * 4 >= a.K) break;  // the last slab's padding (uniform)
+      }
       float4 av[TM];
 #pragma unroll
       for (int i = 0; i < TM; i++)
@@ -138,6 +161,45 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   }
 
   const bool mirror = a.symmetric && ti != tj;
+  if constexpr (HasStagedMirror<Out>::value) {
+    if (out.staged(mirror)) {
+      // the tile's entries, then its mirror in 32-row chunks through the
+      // (now idle) operand buffers: each warp writes 32 consecutive floats of
+      // a mirrored row per store
+      constexpr int kLdT = BN + 1;
+      static_assert(32 * kLdT <= 2 * BM * kSimtLd, "a 32-row chunk fits the operand buffers");
+      float *T = &sA[0][0];
+#pragma unroll
+      for (int i = 0; i < TM; i++) {
+        const int64_t r = row0 + ty + 16 * i;
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+          const int64_t c = col0 + tx + 16 * j;
+          const float v = out.value(r, c, acc[i][j]);
+          acc[i][j][0] = v;
+          if (r < a.nr && c < a.nc) out.store(r, c, v);
+        }
+      }
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+      for (int q = 0; q < BM / 32; q++) {
+        __syncthreads();  // the previous chunk (or the main loop) is done with T
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int i = 2 * q + h;  // rows ty + 16 i of this chunk
+#pragma unroll
+          for (int j = 0; j < TN; j++) T[(ty + 16 * h) * kLdT + tx + 16 * j] = acc[i][j][0];
+        }
+        __syncthreads();
+        const int64_t r = row0 + 32 * q + lane;
+        for (int cc = warp; cc < BN; cc += kSimtThreads / 32) {
+          const int64_t c = col0 + cc;
+          if (r < a.nr && c < a.nc) out.store(c, r, T[lane * kLdT + cc]);
+        }
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int i = 0; i < TM; i++) {
     const int64_t r = row0 + ty + 16 * i;

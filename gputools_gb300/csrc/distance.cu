@@ -55,6 +55,7 @@ struct OpMaximum {
 
 struct OpCanberra {
   static constexpr int NACC = 2;  // sum of terms, number of terms used
+  static constexpr bool kSkipPad = true;
   __device__ static float pad() { return 0.f; }
   __device__ void init(float (&c)[2]) const { c[0] = 0.f; c[1] = 0.f; }
   __device__ void step(float (&c)[2], float a, float b) const {
@@ -70,19 +71,41 @@ struct OpCanberra {
   }
 };
 
-struct OpBinary {
+// Binary on bit-packed points (bit k of word w: coordinate 32 w + k is
+// nonzero); the engine carries the words as float bit patterns and the two
+// counts (bits on in exactly one point, bits on in either) as integers in
+// the accumulator slots.  The reference counts per coordinate in float
+// (inst/cuda/distance.cu:366-415); the counts, and so the results, are the same.
+struct OpBinaryBits {
   static constexpr int NACC = 2;  // bits on in exactly one, bits on in either
+  static constexpr bool kSkipPad = true;
   __device__ static float pad() { return 0.f; }
-  __device__ void init(float (&c)[2]) const { c[0] = 0.f; c[1] = 0.f; }
+  __device__ void init(float (&c)[2]) const { c[0] = __int_as_float(0); c[1] = __int_as_float(0); }
   __device__ void step(float (&c)[2], float a, float b) const {
-    const bool x = a != 0.f, y = b != 0.f;
-    c[0] += (x != y) ? 1.f : 0.f;
-    c[1] += (x || y) ? 1.f : 0.f;
+    const unsigned x = __float_as_uint(a), y = __float_as_uint(b);
+    c[0] = __int_as_float(__float_as_int(c[0]) + __popc(x ^ y));
+    c[1] = __int_as_float(__float_as_int(c[1]) + __popc(x | y));
   }
   __device__ float finish(const float (&c)[2], int64_t) const {
-    return c[1] != 0.f ? c[0] / c[1] : 0.f;
+    const float d = float(__float_as_int(c[1]));
+    return d != 0.f ? float(__float_as_int(c[0])) / d : 0.f;
   }
 };
+
+// One warp per point: word w of point i holds the nonzero pattern of
+// coordinates 32 w .. 32 w + 31 (NaN counts as nonzero, as in OpBinary).
+__global__ void __launch_bounds__(256)
+pack_nonzero_kernel(const float *__restrict__ P, int64_t n, int64_t dim, int64_t words,
+                    unsigned *__restrict__ bits) {
+  const int64_t i = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
+  if (i >= n) return;  // whole warps
+  const int lane = threadIdx.x & 31;
+  for (int64_t w = 0; w < words; w++) {
+    const int64_t k = 32 * w + lane;
+    const unsigned b = __ballot_sync(0xffffffffu, k < dim && P[i * dim + k] != 0.f);
+    if (lane == 0) bits[i * words + w] = b;
+  }
+}
 
 struct OpMink3 {
   static constexpr int NACC = 1;
@@ -92,7 +115,9 @@ struct OpMink3 {
     const float d = fabsf(a - b);
     c[0] = fmaf(d * d, d, c[0]);
   }
-  __device__ float finish(const float (&c)[1], int64_t) const { return float(cbrt(double(c[0]))); }
+  // FP32 root: one FP64 root per entry would cost GB300 more than the entry's
+  // whole sum (its FP64 rate is ~1/64 of FP32); cbrtf is within 1 ulp
+  __device__ float finish(const float (&c)[1], int64_t) const { return cbrtf(c[0]); }
 };
 
 struct OpMinkP {
@@ -101,8 +126,9 @@ struct OpMinkP {
   __device__ static float pad() { return 0.f; }
   __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
   __device__ void step(float (&c)[1], float a, float b) const { c[0] += powf(fabsf(a - b), p); }
+  // s^(1/p) in FP32 as 2^(log2(s) / p): relative error about |log2 s| ulp
   __device__ float finish(const float (&c)[1], int64_t) const {
-    return float(pow(double(c[0]), 1.0 / double(p)));
+    return c[0] > 0.f ? exp2f(__fdiv_rn(log2f(c[0]), p)) : c[0];
   }
 };
 
@@ -114,6 +140,13 @@ struct OutDist {
   float *out;
   int64_t n, K;
   int layout;
+  // the full layout's mirror goes through shared memory (coalesced stores)
+  static constexpr bool kStagedMirror = true;
+  __device__ bool staged(bool mirror) const { return mirror && layout == GT_LAYOUT_FULL; }
+  __device__ float value(int64_t r, int64_t c, const float (&acc)[Op::NACC]) const {
+    return (r == c) ? 0.f : op.finish(acc, K);
+  }
+  __device__ void store(int64_t r, int64_t c, float v) const { out[r * n + c] = v; }
   __device__ void operator()(int64_t r, int64_t c, const float (&acc)[Op::NACC], bool mirror) const {
     if (layout == GT_LAYOUT_FULL) {
       const float v = (r == c) ? 0.f : op.finish(acc, K);
@@ -168,7 +201,18 @@ int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
   case GT_MAXIMUM: e = run_metric(OpMaximum{}, d_pts, n, dim, d_out, layout, st); break;
   case GT_MANHATTAN: e = run_metric(OpManhattan{}, d_pts, n, dim, d_out, layout, st); break;
   case GT_CANBERRA: e = run_metric(OpCanberra{}, d_pts, n, dim, d_out, layout, st); break;
-  case GT_BINARY: e = run_metric(OpBinary{}, d_pts, n, dim, d_out, layout, st); break;
+  case GT_BINARY: {
+    const int64_t words = cdiv(dim, 32);
+    void *pb = nullptr;
+    GT_TRY(ws_get(WS_SCRATCH0, size_t(n) * size_t(words) * 4, &pb));
+    pack_nonzero_kernel<<<unsigned(cdiv(n, 8)), 256, 0, st>>>(d_pts, n, dim, words,
+                                                             static_cast<unsigned *>(pb));
+    count_launch();
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = run_metric(OpBinaryBits{}, static_cast<const float *>(pb), n, words, d_out, layout, st);
+    break;
+  }
   case GT_MINKOWSKI:
     if (p == 1.f) e = run_metric(OpManhattan{}, d_pts, n, dim, d_out, layout, st);
     else if (p == 2.f) e = run_metric(OpEuclid{}, d_pts, n, dim, d_out, layout, st);

@@ -139,3 +139,21 @@ def test_gpuDist_api_matches_oracle(gpu, oracle_mod, rng):
     assert d.p == 4
     d = g.gpuDist(pts, "euclidian")
     assert d.method == "euclidean"
+
+
+@pytest.mark.parametrize("n,d", [(200, 1000), (97, 31), (64, 32), (40, 33)])
+def test_binary_exact(gpu, rng, n, d):
+    # counts are exact, so the result is the float32 quotient of the two
+    # integer counts, bit for bit; all-zero rows give 0, NaN counts as nonzero
+    pts = (rng.random((n, d)) < 0.2).astype(np.float32)
+    pts[3] = 0.0
+    pts[5] = 0.0
+    pts[7, ::5] = np.nan
+    nz = pts != 0
+    x = (nz[:, None, :] != nz[None, :, :]).sum(-1).astype(np.float32)
+    o = (nz[:, None, :] | nz[None, :, :]).sum(-1).astype(np.float32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        want = np.where(o != 0, x / np.where(o != 0, o, 1), 0).astype(np.float32)
+    np.fill_diagonal(want, 0.0)
+    got = rdistances(gpu, pts, "binary")
+    np.testing.assert_array_equal(got.view(np.int32), want.view(np.int32))
