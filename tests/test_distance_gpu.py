@@ -157,3 +157,22 @@ def test_binary_exact(gpu, rng, n, d):
     np.fill_diagonal(want, 0.0)
     got = rdistances(gpu, pts, "binary")
     np.testing.assert_array_equal(got.view(np.int32), want.view(np.int32))
+
+
+def test_canberra_extreme_operands(gpu, oracle_mod, rng):
+    # |a - b| / |a + b| at a = -b (an infinite term), with subnormal and tiny
+    # magnitudes and zero coordinates: float results agree with the FP64
+    # oracle to float tolerance, infinities included (sums that overflow
+    # float are left out: the FP64 oracle keeps them finite)
+    n, d = 48, 24
+    pts = rng.standard_normal((n, d)).astype(np.float32)
+    pts[1] = -pts[0]                                   # every term infinite
+    pts[2, :4] = -pts[3, :4]                           # some terms infinite
+    pts[4] *= np.float32(1e-39)                        # subnormal magnitudes
+    pts[5] *= np.float32(3e-38)
+    pts[8, ::3] = 0.0
+    pts[9] = np.float32(1e-30) * pts[10]               # ratio near 1, tiny
+    got = rdistances(gpu, pts, "canberra")
+    want = oracle_mod.dist(pts, "canberra")
+    np.fill_diagonal(want, 0.0)
+    check_close(got, want)
