@@ -32,36 +32,46 @@ constexpr int kKT = 256;        // threads per count CTA
 constexpr int kKBK = 16;        // words per shared slab
 constexpr int kKLd = 18;        // padded shared row, in words (uint2)
 
-// One warp per (variable, pair-row d, word w): lane b handles i = 32 w + b.
+// One warp per chunk of 32 consecutive words of one variable's rows d0+1 ..
+// d0+drows (Wn words each): for word (d, w), lane b handles i = 32 w + b and
+// the ballots form the word; lane e keeps word e of the chunk, so the chunk
+// is stored with one coalesced 256-byte store, and the untied count goes to
+// T[v] with one atomic per chunk.
 __global__ void kendall_masks_kernel(const float *__restrict__ X, int64_t nvar, int64_t n,
                                      int64_t d0, int64_t drows, int64_t Wn,
                                      uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
-  const int64_t per_var = drows * Wn;
-  const int64_t total = nvar * per_var;
-  for (int64_t t = warp; t < total; t += nwarps) {
-    const int64_t v = t / per_var;
-    const int64_t rem = t - v * per_var;
-    const int64_t dr = rem / Wn, w = rem - dr * Wn;
-    const int64_t d = d0 + dr + 1;
-    const int64_t i = 32 * w + lane;
-    bool valid = i < n && (2 * d < n || i < n / 2);
-    bool untied = false, greater = false;
-    if (valid) {
-      int64_t j = i + d;
-      if (j >= n) j -= n;
-      const float xi = X[v * n + i], xj = X[v * n + j];
-      untied = xj != xi;
-      greater = xj > xi;
+  const int64_t per_var = drows * Wn, chunks = (per_var + 31) / 32;
+  for (int64_t t = warp; t < nvar * chunks; t += nwarps) {
+    const int64_t v = t / chunks, base = (t - v * chunks) * 32;
+    const int cnt = per_var - base < 32 ? int(per_var - base) : 32;
+    const float *x = X + v * n;
+    int64_t dr = base / Wn, w = base - dr * Wn;
+    uint2 mine = make_uint2(0u, 0u);
+    unsigned long long untied_bits = 0;
+    for (int e = 0; e < cnt; e++) {  // warp-uniform
+      const int64_t d = d0 + dr + 1, i = 32 * w + lane;
+      bool untied = false, greater = false;
+      if (i < n && (2 * d < n || i < n / 2)) {
+        int64_t j = i + d;
+        if (j >= n) j -= n;
+        const float xi = x[i], xj = x[j];
+        untied = xj != xi;
+        greater = xj > xi;
+      }
+      const unsigned u = __ballot_sync(0xffffffffu, untied);
+      const unsigned g = __ballot_sync(0xffffffffu, greater);
+      if (lane == e) mine = make_uint2(u, g);
+      untied_bits += __popc(u);
+      if (++w == Wn) {
+        w = 0;
+        dr++;
+      }
     }
-    const unsigned u = __ballot_sync(0xffffffffu, untied);
-    const unsigned g = __ballot_sync(0xffffffffu, greater);
-    if (lane == 0) {
-      M[v * per_var + rem] = make_uint2(u, g);
-      if (u) atomicAdd(&T[v], (unsigned long long)__popc(u));
-    }
+    if (lane < cnt) M[v * per_var + base + lane] = mine;
+    if (lane == 0 && untied_bits) atomicAdd(&T[v], untied_bits);
   }
 }
 
@@ -215,12 +225,12 @@ int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64
       const int64_t dr = (Dr - d0 < rows_chunk) ? Dr - d0 : rows_chunk;
       const int64_t K = dr * Wn;
       uint2 *MXs = M, *MYs = same ? M : M + nx * K;
-      kendall_masks_kernel<<<grid_cap(nx * K * 32, 256), 256, 0, s>>>(dX, nx, n, d0, dr, Wn, MXs,
-                                                                     TX);
+      kendall_masks_kernel<<<grid_cap(nx * cdiv(K, 32) * 32, 256), 256, 0, s>>>(dX, nx, n, d0, dr,
+                                                                                Wn, MXs, TX);
       count_launch();
       if (!same)
-        kendall_masks_kernel<<<grid_cap(ny * K * 32, 256), 256, 0, s>>>(dY, ny, n, d0, dr, Wn,
-                                                                       MYs, TY);
+        kendall_masks_kernel<<<grid_cap(ny * cdiv(K, 32) * 32, 256), 256, 0, s>>>(dY, ny, n, d0,
+                                                                                  dr, Wn, MYs, TY);
       if (!same) count_launch();
       const int64_t gy = cdiv(ny, 64), gx = cdiv(nx, 64);
       if (gy > 65535 || gx > 2147483647LL) return fail(GT_EINVAL, "too many variables");
