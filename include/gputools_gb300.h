@@ -1,6 +1,7 @@
 /*
  * gputools_gb300.h -- C ABI of libgputools_gb300.so, the GB300 (sm_103a)
- * implementation of gputools' all-pairs hot path (gpuDist, gpuCor).
+ * implementation of gputools' all-pairs hot path (gpuDist, gpuCor, gpuTtest)
+ * and the statistics built on it (gpuMi, gpuHclust / gpuDistClust).
  *
  * Two layers:
  *
