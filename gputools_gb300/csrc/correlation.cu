@@ -25,8 +25,11 @@
 #include "kernels.cuh"
 #include "stats.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 namespace gt {
 
@@ -327,6 +330,31 @@ extern "C" int gt_pmcc_device(int use, const float *d_A, int64_t nA, const float
                           static_cast<cudaStream_t>(stream));
 }
 
+namespace gt {
+namespace {
+
+// Writes v into out[0 .. count) with up to 16 host threads (one per 64 MB).
+void host_fill(float *out, int64_t count, float v) {
+  const int64_t per = int64_t(16) << 20;  // floats per thread, at least
+  int64_t nt = (count + per - 1) / per;
+  const int64_t hw = std::max<int64_t>(1, std::thread::hardware_concurrency());
+  nt = std::min<int64_t>(std::min<int64_t>(nt, 16), hw);
+  if (nt <= 1) {
+    std::fill_n(out, count, v);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(size_t(nt));
+  for (int64_t t = 0; t < nt; t++) {
+    const int64_t b = count * t / nt, e = count * (t + 1) / nt;
+    th.emplace_back([=] { std::fill_n(out + b, e - b, v); });
+  }
+  for (auto &x : th) x.join();
+}
+
+}  // namespace
+}  // namespace gt
+
 extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int64_t nB, int64_t n,
                        float *pairs, float *corr, float *ts) {
   gt::clear_error();
@@ -347,19 +375,25 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
       GT_TRY(gt::same_contents(static_cast<float *>(dA), static_cast<float *>(dB), nA * n, &sym, s));
   }
   if (sym) dB = dA;
+  // "everything": every pair count is n (src/correlation.cpp:66-161 counts
+  // all observations), so the host fills `pairs` while the device works and
+  // the host link carries two matrices instead of three
+  const bool host_pairs = pairs && use == GT_EVERYTHING;
   // outputs the kernels can write in place (no staging copy), else workspace
   void *h0 = corr ? gt::host_direct_ptr(corr) : nullptr;
   void *h1 = ts ? gt::host_direct_ptr(ts) : nullptr;
-  void *h2 = pairs ? gt::host_direct_ptr(pairs) : nullptr;
+  void *h2 = pairs && !host_pairs ? gt::host_direct_ptr(pairs) : nullptr;
   if (corr && !(o0 = h0)) GT_TRY(gt::ws_get(gt::WS_OUT0, outb, &o0));
   if (ts && !(o1 = h1)) GT_TRY(gt::ws_get(gt::WS_OUT1, outb, &o1));
-  if (pairs && !(o2 = h2)) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));
+  if (pairs && !host_pairs && !(o2 = h2)) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));
   GT_TRY(gt::pearson_impl(use, static_cast<float *>(dA), nA, static_cast<float *>(dB), nB, n,
                           static_cast<float *>(o2), static_cast<float *>(o0),
                           static_cast<float *>(o1), sym ? 1 : 0, s));
   if (corr && !h0) GT_CUDA(cudaMemcpyAsync(corr, o0, outb, cudaMemcpyDeviceToHost, s));
   if (ts && !h1) GT_CUDA(cudaMemcpyAsync(ts, o1, outb, cudaMemcpyDeviceToHost, s));
-  if (pairs && !h2) GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
+  if (pairs && !host_pairs && !h2)
+    GT_CUDA(cudaMemcpyAsync(pairs, o2, outb, cudaMemcpyDeviceToHost, s));
+  if (host_pairs) gt::host_fill(pairs, nA * nB, float(n));
   GT_CUDA(cudaStreamSynchronize(s));
   bool failed = false;
   GT_TRY(gt::tc_check_error(s, &failed));
