@@ -333,9 +333,15 @@ extern "C" int gt_pmcc_device(int use, const float *d_A, int64_t nA, const float
 namespace gt {
 namespace {
 
-// Writes v into out[0 .. count) with up to 16 host threads (one per 64 MB).
+// Matrices from this size on (floats; 256 MB) have their constant pair counts
+// filled on the host: with 16 threads the fill hides behind the link time of
+// the other two matrices; below it, the device writing one more matrix over
+// the link is the cheaper way.
+constexpr int64_t kHostFillMin = int64_t(64) << 20;
+
+// Writes v into out[0 .. count) with up to 16 host threads.
 void host_fill(float *out, int64_t count, float v) {
-  const int64_t per = int64_t(16) << 20;  // floats per thread, at least
+  const int64_t per = int64_t(4) << 20;  // floats per thread, at least
   int64_t nt = (count + per - 1) / per;
   const int64_t hw = std::max<int64_t>(1, std::thread::hardware_concurrency());
   nt = std::min<int64_t>(std::min<int64_t>(nt, 16), hw);
@@ -376,9 +382,9 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
   }
   if (sym) dB = dA;
   // "everything": every pair count is n (src/correlation.cpp:66-161 counts
-  // all observations), so the host fills `pairs` while the device works and
-  // the host link carries two matrices instead of three
-  const bool host_pairs = pairs && use == GT_EVERYTHING;
+  // all observations), so for large outputs the host fills `pairs` while the
+  // device works and the host link carries two matrices instead of three
+  const bool host_pairs = pairs && use == GT_EVERYTHING && nA * nB >= gt::kHostFillMin;
   // outputs the kernels can write in place (no staging copy), else workspace
   void *h0 = corr ? gt::host_direct_ptr(corr) : nullptr;
   void *h1 = ts ? gt::host_direct_ptr(ts) : nullptr;

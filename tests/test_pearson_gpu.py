@@ -222,3 +222,21 @@ def test_gpuTtest(gpu, rng):
     got = g.gpuTtest(gp, co)
     r = co.astype(np.float32); n = gp.astype(np.float32)
     np.testing.assert_allclose(got, r * np.sqrt((n - 2) / (1 - r * r)), rtol=2e-6)
+
+
+def test_everything_large_output_pairs_from_host(gpu):
+    # 8192^2 entries reach the size from which the constant pair counts of
+    # "everything" are filled on the host while the device writes r and t
+    nv, n = 8192, 8
+    rng = np.random.default_rng(31)
+    X = rng.standard_normal((nv, n)).astype(np.float32)
+    pairs = np.full((nv, nv), -1.0, np.float32)
+    corr = np.empty((nv, nv), np.float32)
+    ts = np.empty((nv, nv), np.float32)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert gpu.gt_pmcc(0, vp(X), nv, vp(X), nv, n, vp(pairs), vp(corr), vp(ts)) == 0
+    assert np.all(pairs == np.float32(n))
+    rows = np.array([0, 1, 4095, 8191])
+    want = np.corrcoef(X.astype(np.float64))[rows]
+    assert np.max(np.abs(corr[rows] - want)) < 5e-6
+    assert np.all(np.isfinite(ts[rows]))
