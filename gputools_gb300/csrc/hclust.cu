@@ -138,6 +138,35 @@ hc_init_kernel(float *__restrict__ D, int64_t n, float *__restrict__ minv,
   }
 }
 
+// *asym = 1 unless D[i][j] == D[j][i] for every i, j (NaN counts as a
+// difference): 32 x 32 tiles of the lower triangle against their transposes,
+// both read coalesced through shared memory.
+__global__ void __launch_bounds__(256)
+hc_symmetry_kernel(const float *__restrict__ D, int64_t n, int *__restrict__ asym) {
+  __shared__ float t[32][33];
+  const int64_t nt = (n + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int64_t b = blockIdx.x; b < nt * (nt + 1) / 2; b += gridDim.x) {
+    // tile (bi, bj), bj <= bi, from the triangular index b
+    int64_t bi = int64_t((sqrt(8.0 * double(b) + 1.0) - 1.0) / 2.0);
+    while (bi * (bi + 1) / 2 > b) bi--;
+    while ((bi + 1) * (bi + 2) / 2 <= b) bi++;
+    const int64_t bj = b - bi * (bi + 1) / 2;
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {  // the transposed tile (bj, bi), row by row
+      const int64_t row = bj * 32 + k, col = bi * 32 + tx;
+      t[k][tx] = (row < n && col < n) ? D[row * n + col] : 0.f;
+    }
+    __syncthreads();
+    bool diff = false;
+    for (int k = ty; k < 32; k += 8) {
+      const int64_t row = bi * 32 + k, col = bj * 32 + tx;
+      if (row < n && col < n) diff |= !(D[row * n + col] == t[tx][k]);
+    }
+    if (__syncthreads_or(diff) && threadIdx.x == 0) atomicExch(asym, 1);
+  }
+}
+
 // A candidate minimum: value, the index its ties are ordered by (column for
 // a row's minimum, row for the smallest row minimum) and the other index.
 struct alignas(16) HcCand {
@@ -328,7 +357,8 @@ template <bool REP>
 __global__ void __launch_bounds__(kHcThreads, 1)
 hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float beta,
                const float *__restrict__ minv0, const int *__restrict__ minc0,
-               int *__restrict__ sub, int *__restrict__ sup, float *__restrict__ val) {
+               const int *__restrict__ asym, int *__restrict__ sub, int *__restrict__ sup,
+               float *__restrict__ val) {
   extern __shared__ __align__(16) float hc_smem[];
   __shared__ HcSlot s_slots[2][kHcMaxCtas];
   __shared__ HcCand sred[2][kHcCands * (kHcWarps + 1)];
@@ -364,6 +394,8 @@ hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float
   hc_cluster_sync();
   int pr = -1, pc = -1;
   float prf = 0.f, pcf = 0.f;  // the previous merge's rows and their counts after it
+  // a symmetric matrix stays symmetric (every update writes both halves)
+  const bool symmetric = *asym == 0;
 
   for (int64_t it = 0; it + 1 < n; it++) {
     // A. the merge
@@ -406,13 +438,24 @@ hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float
       }
     }
 
-    // B. rows to scan again (pr's values from registers: stored just now)
+    // B. rows to scan again (pr's values from registers: stored just now).
+    // Single linkage on a symmetric matrix: the new (i, r) is min(old (i, r),
+    // old (i, c)), never above the old minimum's entry; when the row's
+    // minimum sat in column r it stays there, and when it sat in column c
+    // with r ordered before c (r <= i), (i, r) is the new minimum: no scan.
+    const bool single_short = method == HC_SINGLE && symmetric && c != r;
+    const bool r_before_c = hc_before(0.f, r, 0.f, c);
+    auto rescan = [&](int64_t i, int mc) {
+      if (!(mc == c || (i > r && mc == r))) return false;
+      if (single_short && (mc == r || (r <= i && r_before_c))) return false;
+      return true;
+    };
     for (int64_t i = lo + tid; i < hi; i += kHcThreads) {
       if (i <= c || i == r) continue;
       const float ci = (!REP && i == pc) ? pcf : (!REP && i == pr) ? prf : cnt_own(i);
       if (!(ci > 0.f)) continue;
       const int mc = i == pr ? y.k : s_minc[i - lo];
-      if (mc == c || (i > r && mc == r)) s_list[atomicAdd(&nlist, 1)] = int(i);
+      if (rescan(i, mc)) s_list[atomicAdd(&nlist, 1)] = int(i);
     }
     __syncthreads();
     const int L = nlist, L1 = L < kHcRescan ? L : kHcRescan;
@@ -446,12 +489,17 @@ hc_loop_kernel(float *__restrict__ D, int64_t n, int method, float lambda, float
         if (i == r || i == c || !(nk > 0.f)) continue;
         float mv = s_minv[i - lo];
         int mc = s_minc[i - lo];
-        if (i > c && (mc == c || (i > r && mc == r))) {
+        if (i > c && rescan(i, mc)) {
 #pragma unroll
           for (int e = 0; e < kHcRescan; e++)
             if (e < L1 && s_list[e] == i && r <= i) hc_take(cand[2 + e], hc_cand(nv, r, 0));
         } else {
-          if (i > r && hc_before(nv, r, mv, mc)) {
+          if (i > c && mc == c) {  // single linkage, see above: (i, r) is the minimum
+            mv = nv;
+            mc = r;
+            s_minv[i - lo] = mv;
+            s_minc[i - lo] = mc;
+          } else if (i > r && hc_before(nv, r, mv, mc)) {
             mv = nv;
             mc = r;
             s_minv[i - lo] = mv;
@@ -619,19 +667,31 @@ int hclust_device(float *dD, int64_t n, const char *method, int *sub, int *sup, 
     if (nclusters >= 1) break;
   }
   void *pw = nullptr;
-  const size_t bytes = size_t(n) * 8 + size_t(n - 1) * 12 + 256;
+  const size_t bytes = 256 + size_t(n) * 8 + size_t(n - 1) * 12 + 256;
   GT_TRY(ws_get(WS_SCRATCH3, bytes, &pw));
-  float *minv = static_cast<float *>(pw);
+  int *asym = static_cast<int *>(pw);
+  float *minv = reinterpret_cast<float *>(static_cast<char *>(pw) + 256);
   int *minc = reinterpret_cast<int *>(minv + n);
   int *dsub = minc + n, *dsup = dsub + (n - 1);
   float *dval = reinterpret_cast<float *>(dsup + (n - 1));
   {
     ProfScope prof("hclust", s);
+    // single linkage's shortcut needs a symmetric matrix (R's as.matrix(dist)
+    // is); other methods never look at the flag
+    GT_CUDA(cudaMemsetAsync(asym, 0, sizeof(int), s));
+    if (m == HC_SINGLE) {
+      const int64_t tiles = cdiv(n, 32) * (cdiv(n, 32) + 1) / 2;
+      hc_symmetry_kernel<<<unsigned(std::min<int64_t>(tiles, int64_t(sm_count()) * 8)), 256, 0,
+                           s>>>(dD, n, asym);
+      count_launch();
+    } else {
+      GT_CUDA(cudaMemsetAsync(asym, 0xff, sizeof(int), s));
+    }
     hc_init_kernel<<<unsigned(cdiv(n, 8)), 256, 0, s>>>(dD, n, minv, minc);
     GT_CUDA(cudaGetLastError());
     GT_CUDA(cudaLaunchKernelEx(&cfg, kern, dD, n, m, 0.5f, 0.5f,
                                static_cast<const float *>(minv), static_cast<const int *>(minc),
-                               dsub, dsup, dval));
+                               static_cast<const int *>(asym), dsub, dsup, dval));
     count_launch(2);
   }
   GT_CUDA(cudaMemcpyAsync(sub, dsub, size_t(n - 1) * sizeof(int), cudaMemcpyDeviceToHost, s));

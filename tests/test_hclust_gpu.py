@@ -195,3 +195,18 @@ def test_hclust_cluster_sizes_and_count_layouts(gpu, oracle_mod, monkeypatch, ct
     D[:45, 45:] = np.inf
     D[45:, :45] = np.inf
     same(run_host(gpu, D, "centroid"), want(oracle_mod, D, "centroid"))
+
+
+@pytest.mark.parametrize("method", ["single", "complete"])
+def test_hclust_asymmetric_matrix(gpu, oracle_mod, method):
+    # the C ABI takes any n x n matrix: an asymmetric one is clustered as the
+    # reference would (row c and the lower triangle are read), and single
+    # linkage's shortcut for symmetric matrices stays off
+    rng = np.random.default_rng(17)
+    for n in (40, 700):
+        D = rng.random((n, n)).astype(np.float32)
+        np.fill_diagonal(D, 0)
+        same(run_host(gpu, D, method), want(oracle_mod, D, method))
+    D = sym(rng, 300, "ties")
+    D[5, 7] += 0.5  # one entry off
+    same(run_host(gpu, D, "single"), want(oracle_mod, D, "single"))
