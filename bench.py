@@ -513,6 +513,38 @@ def run_case(args):
         out = torch.empty((p, p), dtype=torch.float64, device=dev)
         fn = lambda: _lib.check(lib.gt_kendall_device(vp(dX), p, vp(dX), p, n, vp(out), sptr))
         names = ("kendall_count",)
+    elif args.case == "dist":
+        # p points x n dims; binary on Bernoulli(0.3) 0/1 data, the others N(0,1)
+        methods = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
+        mi_ = methods.index(args.metric)
+        pts = ((rng.random((p, n)) < 0.3).astype(np.float32) if args.metric == "binary"
+               else rng.standard_normal((p, n), dtype=np.float32))
+        dP = torch.from_numpy(pts).to(dev)
+        lay = 0 if args.layout == "full" else 1
+        out = torch.empty(p * p if lay == 0 else p * (p - 1) // 2, dtype=torch.float32, device=dev)
+        fn = lambda: _lib.check(lib.gt_distances_device(vp(dP), p, n, vp(out), lay, mi_,
+                                                        ctypes.c_float(3.0), sptr))
+        names = ("dist", "euclid_gram")
+    elif args.case == "mi":
+        # p variables x n samples sharing a common component (cor(x)-style)
+        X = (rng.standard_normal((1, n)) + 0.7 * rng.standard_normal((p, n))).astype(np.float32)
+        dX = torch.from_numpy(X).to(dev)
+        out = torch.empty((p, p), dtype=torch.float32, device=dev)
+        fn = lambda: _lib.check(lib.gt_mutual_info_device(args.bins, args.order, n, vp(dX), p,
+                                                          vp(dX), p, vp(out), sptr))
+        names = ("mi_prologue", "mi_gram")
+    elif args.case == "hclust":
+        # p points x n dims around 8 centres; each step clusters a fresh copy
+        # of their euclidean distance matrix (the copy is inside the step)
+        centres = rng.standard_normal((8, n)) * 4
+        pts = (centres[rng.integers(0, 8, p)] + rng.standard_normal((p, n))).astype(np.float32)
+        full = g.distances_device(torch.from_numpy(pts).to(dev), "euclidean").view(p, p)
+        work = torch.empty_like(full)
+
+        def fn():
+            work.copy_(full)
+            g.hclust_device(work, args.method, stream)
+        names = ("hclust",)
     else:
         raise SystemExit(f"unknown case {args.case}")
     for _ in range(args.warmup):
@@ -765,12 +797,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--skip-euclid", action="store_true")
-    ap.add_argument("--case", choices=("pearson", "euclid", "kendall"),
+    ap.add_argument("--case", choices=("pearson", "euclid", "kendall", "dist", "mi", "hclust"),
                     help="run one workload at the given size instead of the benchmark")
     ap.add_argument("--p", type=int, default=4096, help="--case: variables / points")
     ap.add_argument("--n", type=int, default=4096, help="--case: observations")
     ap.add_argument("--path", default="bf16x3", help="--case: gram path")
     ap.add_argument("--layout", default="dist", help="--case euclid: full or dist")
+    ap.add_argument("--metric", default="manhattan", help="--case dist: distance method")
+    ap.add_argument("--bins", type=int, default=10, help="--case mi: bins")
+    ap.add_argument("--order", type=int, default=3, help="--case mi: spline order")
+    ap.add_argument("--method", default="average", help="--case hclust: linkage")
     ap.add_argument("--use", type=int, default=0,
                     help="--case pearson: 0 everything, 1 pairwise.complete.obs")
     ap.add_argument("--nan-frac", type=float, default=0.0,
