@@ -349,12 +349,19 @@ void host_fill(float *out, int64_t count, float v) {
     std::fill_n(out, count, v);
     return;
   }
+  // slices that get no thread (thread creation failed) are filled here
   std::vector<std::thread> th;
-  th.reserve(size_t(nt));
-  for (int64_t t = 0; t < nt; t++) {
-    const int64_t b = count * t / nt, e = count * (t + 1) / nt;
-    th.emplace_back([=] { std::fill_n(out + b, e - b, v); });
+  int64_t done = 0;
+  try {
+    th.reserve(size_t(nt));
+    for (int64_t t = 0; t < nt; t++) {
+      const int64_t b = count * t / nt, e = count * (t + 1) / nt;
+      th.emplace_back([=] { std::fill_n(out + b, e - b, v); });
+      done = e;
+    }
+  } catch (...) {
   }
+  std::fill_n(out + done, count - done, v);
   for (auto &x : th) x.join();
 }
 
