@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <vector>
 
 namespace gt {
@@ -702,8 +703,12 @@ int hclust_device(float *dD, int64_t n, const char *method, int *sub, int *sup, 
 }
 
 int hclust_format(int len, const int *sub, const int *sup, int *merge, int *order) {
-  if (!format_clustering(len, sub, sup, merge, order))
-    return fail(GT_EINVAL, "the merge steps do not form a tree over %d points", len + 1);
+  try {
+    if (!format_clustering(len, sub, sup, merge, order))
+      return fail(GT_EINVAL, "the merge steps do not form a tree over %d points", len + 1);
+  } catch (const std::bad_alloc &) {
+    return fail(GT_ENOMEM, "host memory for the merge formatting");
+  }
   return GT_OK;
 }
 
@@ -721,7 +726,13 @@ extern "C" int gt_hclust_device(float *d_dist, int64_t n, const char *method, in
                                 int *order, float *height, void *stream) {
   gt::clear_error();
   if (!d_dist || !merge || !order || !height) return gt::fail(GT_EINVAL, "null pointer");
-  std::vector<int> sub(size_t(n > 1 ? n - 1 : 1)), sup(sub.size());
+  std::vector<int> sub, sup;
+  try {
+    sub.resize(size_t(n > 1 ? n - 1 : 1));
+    sup.resize(sub.size());
+  } catch (const std::bad_alloc &) {
+    return gt::fail(GT_ENOMEM, "host memory for %lld merge steps", static_cast<long long>(n));
+  }
   GT_TRY(gt::hclust_device(d_dist, n, method, sub.data(), sup.data(), height,
                            static_cast<cudaStream_t>(stream)));
   return gt::hclust_format(int(n - 1), sub.data(), sup.data(), merge, order);
