@@ -27,6 +27,7 @@ GT_GRAM_TC_BF16X3 = 0
 GT_GRAM_TC_BF16X6 = 1
 GT_GRAM_FP32 = 2
 GT_GRAM_TC_F16X3 = 3
+GT_GRAM_TC_F16X6 = 4
 
 # (name, restype, argtypes) of every symbol include/gputools_gb300.h declares.
 _i, _i64, _f, _vp, _cp = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p, ctypes.c_char_p
@@ -50,6 +51,8 @@ SIGNATURES = {
     "gt_last_error": (_cp, []),
     "gt_version": (_i, []),
     "gt_release_workspace": (None, []),
+    "gt_device_status": (_i, [_vp]),
+    "gt_set_wait_limit_ns": (_i, [ctypes.c_uint64]),
     "gt_kernel_launches": (ctypes.c_uint64, []),
     "gt_profile_enable": (None, [_i]),
     "gt_profile_reset": (None, []),

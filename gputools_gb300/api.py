@@ -375,16 +375,21 @@ def hclust_format(sub, sup):
     return merge.reshape(2, m).T.copy(), order
 
 
+GRAM_PATHS = {"bf16x3": _lib.GT_GRAM_TC_BF16X3, "bf16x6": _lib.GT_GRAM_TC_BF16X6,
+              "fp32": _lib.GT_GRAM_FP32, "f16x3": _lib.GT_GRAM_TC_F16X3,
+              "f16x6": _lib.GT_GRAM_TC_F16X6}
+
+
 def set_gram_path(path: str) -> None:
     """"bf16x3" / "bf16x6" (tcgen05 split-bf16), "f16x3" (tcgen05, scaled
-    split-fp16) or "fp32" (CUDA cores)."""
-    code = {"bf16x3": _lib.GT_GRAM_TC_BF16X3, "bf16x6": _lib.GT_GRAM_TC_BF16X6,
-            "fp32": _lib.GT_GRAM_FP32, "f16x3": _lib.GT_GRAM_TC_F16X3}[path]
-    check(load().gt_set_gram_path(code))
+    split-fp16), "f16x6" (tcgen05, fixed-point fp16 digits whose products
+    sum exactly: Pearson at FP64-level error) or "fp32" (CUDA cores)."""
+    check(load().gt_set_gram_path(GRAM_PATHS[path]))
 
 
 def get_gram_path() -> str:
-    return {0: "bf16x3", 1: "bf16x6", 2: "fp32", 3: "f16x3"}[load().gt_get_gram_path()]
+    code = load().gt_get_gram_path()
+    return next(k for k, v in GRAM_PATHS.items() if v == code)
 
 
 # ---------------------------------------------------------------------------

@@ -31,7 +31,7 @@ struct gt_batch_plan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t tiles = 0, ctas = 0;
-  int *err = nullptr;  // device error word of the tensor-core kernel, if any
+  int *err = nullptr;  // the device error word, when the plan runs tensor-core kernels
   double config_ms = 0.0;
   char config[160] = {0};
 };
@@ -101,9 +101,10 @@ int plan_finalize(gt_batch_plan *p, int flags) {
     if (e != cudaSuccess) st = fail(GT_ECUDA, "batch plan first run: %s", cudaGetErrorString(e));
   }
   if (st == GT_OK && p->err) {
-    int h = 0;
-    GT_CUDA(cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) st = fail(GT_ETIMEOUT, "batch plan first run: a tensor-core kernel wait timed out");
+    bool failed = false;
+    st = device_error_check(s, &failed);
+    if (st == GT_OK && failed)
+      st = fail(GT_ETIMEOUT, "batch plan first run: a tensor-core kernel wait timed out");
   }
   if (st == GT_OK && !(flags & GT_BATCH_NO_GRAPH)) {
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);

@@ -71,6 +71,20 @@ class ProfScope {
 // by one.  GT_DIRECT_HOST=0 disables it.
 void *host_direct_ptr(void *host);
 
+// Per-device error word of the kernels with bounded waits (allocated and
+// zeroed on first use, kept until gt_release_workspace).  Kernels only set it;
+// device_error_check() reads and clears it.
+int device_error_word(int **p);
+// Synchronises `s`, reads the current device's error word and clears it;
+// *failed is set when a bounded wait inside a kernel gave up since the last
+// check on this device.
+int device_error_check(cudaStream_t s, bool *failed);
+
+// Limit of each bounded device-side wait, in nanoseconds (2 s unless changed
+// by gt_set_wait_limit_ns), and the sleep hint that goes with it.
+uint64_t wait_limit_ns();
+uint32_t wait_sleep_hint_ns();
+
 // Host-side reads of the device the library runs on.
 int current_device(int *dev);
 int sm_count();

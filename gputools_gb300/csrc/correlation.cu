@@ -409,7 +409,7 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
   if (host_pairs) gt::host_fill(pairs, nA * nB, float(n));
   GT_CUDA(cudaStreamSynchronize(s));
   bool failed = false;
-  GT_TRY(gt::tc_check_error(s, &failed));
+  GT_TRY(gt::device_error_check(s, &failed));
   if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return GT_OK;
 }

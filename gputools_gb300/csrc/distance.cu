@@ -259,7 +259,7 @@ extern "C" int gt_distances(const float *points, int64_t n, int64_t dim, float *
     GT_CUDA(cudaMemcpyAsync(out, dout, size_t(n) * size_t(n) * 4, cudaMemcpyDeviceToHost, st));
   GT_CUDA(cudaStreamSynchronize(st));
   bool failed = false;
-  GT_TRY(gt::tc_check_error(st, &failed));
+  GT_TRY(gt::device_error_check(st, &failed));
   if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return GT_OK;
 }

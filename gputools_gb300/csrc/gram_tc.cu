@@ -46,6 +46,7 @@
 // drains its in-flight copies and MMAs, releases its TMEM and exits.
 #include "common.cuh"
 #include "dist_lines.cuh"
+#include "gram_core.cuh"
 #include "kernels.cuh"
 #include "tc_ptx.cuh"
 #include "stats.cuh"
@@ -66,272 +67,6 @@
 namespace gt {
 
 namespace {
-
-constexpr int kBM = 128, kBN = 256;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per barrier wait
-constexpr uint64_t kDrainLimitNs = 200000000ull;  // 0.2 s for in-flight work at exit
-constexpr int kKPad = 64;                         // K padding of the operand planes
-constexpr int kMaxSmem = 232448;                  // dynamic shared memory per CTA (227 KB)
-constexpr int kEpiTileFloats = 32 * 33;           // one warp's padded 32 x 32 staging tile
-
-// ----------------------------------------------------------------- tiling
-// Tile sets.  kFull: every (row block, column block).  kUpper (symmetric
-// problems whose entries r < c are wanted): column block tj holds row blocks
-// 0 .. min(2 tj + 1, tr - 1), the 128-row blocks that reach the upper
-// triangle of a 256-column block.  kLower (entries c < r): row block ti holds
-// column blocks 0 .. min(ti / 2, tc - 1), enumerated row by row.
-enum TileMode { kFull = 0, kUpper = 1, kLower = 2 };
-
-struct TileSpace {
-  int64_t tr, tc;    // row blocks (128), column blocks (256)
-  int64_t j0;        // upper: column blocks whose tile count is 2*tj + 2
-  int64_t ntiles;    // below 2^31
-  int64_t group;     // upper / full: column blocks per band of the tile order (power of two)
-  int group_log2;
-  int symmetric;     // TileMode
-};
-
-// Tile order.  Column blocks are grouped into bands of `group` (a power of
-// two); a band's tiles are consecutive, row block by row block, so the CTAs
-// working at one time share a few operand panels in L2: the band's B panels
-// stay resident while its A panels stream past once per band instead of once
-// per column block.  Every role of every CTA evaluates this per tile, so it
-// runs in 32-bit arithmetic (the host keeps tile counts below 2^31): 64-bit
-// integer division is a long software sequence on the GPU.
-__host__ __device__ inline void tile_coords(const TileSpace &ts, int64_t t64, int64_t &ti,
-                                            int64_t &tj) {
-  const uint32_t t = uint32_t(t64), tr = uint32_t(ts.tr), tc = uint32_t(ts.tc);
-  const uint32_t G = uint32_t(ts.group), lg = uint32_t(ts.group_log2);
-  if (ts.symmetric == kLower) {
-    // row pairs (2m, 2m + 1) hold m + 1 tiles each while m + 1 <= tc; rows
-    // from 2 tc on hold tc tiles
-    const uint32_t head = tc * (tc + 1);
-    if (t < head) {
-      int32_t m = int32_t((sqrtf(float(t) * 4.f + 1.f) - 1.f) * 0.5f);
-      if (m < 0) m = 0;
-      while (uint32_t(m + 1) * uint32_t(m + 2) <= t) m++;
-      while (uint32_t(m) * uint32_t(m + 1) > t) m--;
-      const uint32_t u = t - uint32_t(m) * uint32_t(m + 1), w = uint32_t(m) + 1;
-      const uint32_t e = u >= w ? 1u : 0u;
-      ti = 2 * uint32_t(m) + e;
-      tj = u - e * w;
-    } else {
-      const uint32_t u = t - head;
-      const uint32_t i = u / tc;
-      ti = 2 * tc + i;
-      tj = u - i * tc;
-    }
-    return;
-  }
-  if (ts.symmetric == kFull) {
-    const uint32_t c0 = (t / (tr << lg)) << lg;
-    const uint32_t g = (tc - c0) < G ? (tc - c0) : G;
-    const uint32_t u = t - c0 * tr;
-    const uint32_t i = u / g;
-    ti = i;
-    tj = c0 + (u - i * g);
-    return;
-  }
-  // column block of t in column-major order, hence its band
-  const uint32_t j0 = uint32_t(ts.j0);
-  const uint32_t head = j0 * (j0 + 1);
-  uint32_t col;
-  if (t < head) {
-    // float estimate, corrected in integers
-    int32_t j = int32_t((sqrtf(float(t) * 4.f + 1.f) - 1.f) * 0.5f);
-    if (j < 0) j = 0;
-    while (uint32_t(j + 1) * uint32_t(j + 2) <= t) j++;
-    while (uint32_t(j) * uint32_t(j + 1) > t) j--;
-    col = uint32_t(j);
-  } else {
-    col = j0 + (t - head) / tr;
-  }
-  const uint32_t c0 = (col >> lg) << lg;
-  const uint32_t c1 = (c0 + G) < tc ? (c0 + G) : tc;
-  const uint32_t g = c1 - c0;
-  const uint32_t pre = c0 <= j0 ? c0 * (c0 + 1) : head + (c0 - j0) * tr;
-  uint32_t u = t - pre;
-  // rows 0 .. 2 c0 + 1 meet every column block of the band
-  const uint32_t F = (2 * c0 + 2) < tr ? (2 * c0 + 2) : tr;
-  if (u < F * g) {
-    const uint32_t i = u / g;
-    ti = i;
-    tj = c0 + (u - i * g);
-    return;
-  }
-  // row F + w meets the last g - 1 - floor(w / 2) column blocks
-  u -= F * g;
-  for (uint32_t w = 0;; w++) {
-    const uint32_t cnt = g - 1 - w / 2;
-    if (u < cnt) {
-      ti = F + w;
-      tj = c1 - cnt + u;
-      return;
-    }
-    u -= cnt;
-  }
-}
-
-TileSpace make_tiles(int64_t nr, int64_t nc, int mode, int64_t group) {
-  TileSpace ts;
-  ts.tr = cdiv(nr, kBM);
-  ts.tc = cdiv(nc, kBN);
-  ts.symmetric = mode;
-  ts.group_log2 = 0;
-  while ((int64_t(2) << ts.group_log2) <= group) ts.group_log2++;
-  ts.group = int64_t(1) << ts.group_log2;
-  if (mode == kLower) {
-    ts.j0 = 0;
-    ts.group = 1;
-    ts.group_log2 = 0;
-    if (ts.tr <= 2 * ts.tc) {
-      const int64_t m = ts.tr / 2, e = ts.tr % 2;
-      ts.ntiles = m * (m + 1) + e * (m + 1);
-    } else {
-      ts.ntiles = ts.tc * (ts.tc + 1) + (ts.tr - 2 * ts.tc) * ts.tc;
-    }
-  } else if (mode == kUpper) {
-    ts.j0 = ts.tr / 2;
-    if (ts.j0 > ts.tc) ts.j0 = ts.tc;
-    ts.ntiles = ts.j0 * (ts.j0 + 1) + (ts.tc - ts.j0) * ts.tr;
-  } else {
-    ts.j0 = 0;
-    ts.ntiles = ts.tr * ts.tc;
-  }
-  return ts;
-}
-
-// Band width for operand planes of `panel_bytes` per 256-row B panel: as
-// many B panels as fit in about 40 MB of L2, at most 16.
-int64_t band_group(int64_t panel_bytes) {
-  const int64_t g = (int64_t(40) << 20) / (panel_bytes > 0 ? panel_bytes : 1);
-  return g < 1 ? 1 : (g > 16 ? 16 : g);
-}
-
-// ----------------------------------------------------------------- finishes
-// Each finish handles a warp's 32 x 32 block: lane = row r (consecutive rows
-// across lanes), g[j] = entry (r, c0 + j).  The epilogue context carries the
-// warp's staging tile and the rows / columns of its part of the tile; after
-// the last block of a tile the epilogue calls flush().
-
-constexpr int kEuclidList = 64;  // pending near-zero pairs per epilogue warp
-
-constexpr int kEuclidCols = 64;  // columns per epilogue warp of the Euclidean kernels
-
-// Per-warp state of the epilogue.  Only what changes per tile lives here;
-// the list and the column norms sit at fixed offsets after the staging tile.
-struct EpiCtx {
-  float *wsm;       // 32 x 33 staging tile, then (Euclidean) the list and column norms
-  float2 me;        // this lane's row's {norm, scale} (Euclidean)
-  int nlist;        // warp-uniform: entries in the shared-memory list
-  int gcount;       // warp-uniform: entries in the warp's region of a global list
-  int64_t rbase;    // first row of the warp's 32 rows
-  int64_t col0;     // first column of the warp's columns
-  // kEuclidList entries: (row - rbase) << 8 | (col - col0), or finish-defined
-  __device__ __forceinline__ uint32_t *list() const {
-    return reinterpret_cast<uint32_t *>(wsm + kEpiTileFloats);
-  }
-  // the warp's kEuclidCols columns' {norm, scale} (Euclidean)
-  __device__ __forceinline__ float2 *cnrm() const {
-    return reinterpret_cast<float2 *>(wsm + kEpiTileFloats + kEuclidList);
-  }
-};
-
-__device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
-
-// hostSignif's rule (src/correlation.cpp:51-64), t = r sqrt(n-2) / sqrt(1-r^2)
-// with sqrt(n-2) precomputed and a hardware reciprocal square root.
-__device__ __forceinline__ float signif_fast(float r, float sq_nm2) {
-  if (r >= 0.999f) return 10000.0f;
-  return r * sq_nm2 * tc::rsqrt_approx(1.f - r * r);
-}
-
-struct PearsonFinish {
-  float *corr, *ts, *pairs;
-  int64_t ld, nr, nc;
-  float npairs, sq_nm2;
-  float gscale;  // removes the operand scales (2^-28 for f16x3, else 1)
-  int symmetric;
-  const int *gate = nullptr;  // when set, the kernel does nothing unless *gate == 0
-
-  __device__ __forceinline__ bool skip() const { return gate && *gate != 0; }
-
-  __device__ __forceinline__ void put(float *pc, float *pt, float *pp, float v) const {
-    if (corr) *pc = v;
-    if (ts) *pt = signif_fast(v, sq_nm2);
-    if (pairs) *pp = npairs;
-  }
-
-  __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
-    const int lane = threadIdx.x & 31;
-    float *wsm = ctx.wsm;
-    const int64_t rbase = r - lane;
-    // interior block: every entry exists and (symmetric) lies above the diagonal
-    const bool interior = (c0 + 31 < nc) && (symmetric ? (rbase + 31 < c0) : (rbase + 31 < nr));
-    if (interior) {
-      // branch-free stores with pointer increments
-      if (symmetric) {
-        const int64_t o = c0 * ld + r;
-        float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-          put(pc, pt, pp, clamp_r(g[j] * gscale));
-          pc += ld;
-          pt += ld;
-          pp += ld;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-      __syncwarp();
-      const int64_t o = rbase * ld + c0 + lane;
-      float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
-#pragma unroll 8
-      for (int i = 0; i < 32; i++) {
-        put(pc, pt, pp, clamp_r(wsm[i * 33 + lane] * gscale));
-        pc += ld;
-        pt += ld;
-        pp += ld;
-      }
-      __syncwarp();
-      return;
-    }
-    // mirror orientation (lanes hold consecutive rows): coalesced from registers
-    if (symmetric && r < nr) {
-#pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const int64_t c = c0 + j;
-        if (c < nc && r < c) {
-          const float v = clamp_r(g[j] * gscale);
-          const int64_t o = c * ld + r;
-          if (corr) corr[o] = v;
-          if (ts) ts[o] = signif_fast(v, sq_nm2);
-          if (pairs) pairs[o] = npairs;
-        }
-      }
-    }
-    // row orientation through the staging tile
-#pragma unroll
-    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-    __syncwarp();
-    const int64_t c = c0 + lane;
-    int64_t o = rbase * ld + c;
-    for (int i = 0; i < 32; i++, o += ld) {
-      const int64_t ri = rbase + i;
-      if (ri >= nr) break;
-      if (c >= nc || (symmetric && c < ri)) continue;
-      float v = clamp_r(wsm[i * 33 + lane] * gscale);
-      if (symmetric && c == ri && v == v) v = 1.f;
-      if (corr) corr[o] = v;
-      if (ts) ts[o] = signif_fast(v, sq_nm2);
-      if (pairs) pairs[o] = npairs;
-    }
-    __syncwarp();
-  }
-  __device__ void begin_tile(int64_t, EpiCtx &) const {}
-  __device__ void end_tile(EpiCtx &) const {}
-  __device__ void drain(EpiCtx &) const {}
-};
 
 // Operands are the points centred by their column means (distances do not
 // change).  The kernel runs the lower tile set: TMEM lane = point a, column =
@@ -857,97 +592,6 @@ __device__ __forceinline__ void product_parts(int p, int &pa, int &pb) {
   }
 }
 
-// ----------------------------------------------------------------- work sources
-// A work source tells every role of the kernel, for the cursor-th tile of
-// this CTA, which tensor maps to load from, the tile's row / column blocks,
-// its number of k-blocks, and the finish to apply.
-struct TileRef {
-  const CUtensorMap *ma, *mb;
-  int64_t row0, col0;  // first operand row of the A and B boxes (A may start below 0)
-  int64_t nk, prob;
-};
-
-// One problem: maps and finish as kernel parameters, tiles dealt round-robin.
-template <class Fin>
-struct SingleWork {
-  CUtensorMap ma, mb;
-  TileSpace ts;
-  int64_t nk;
-  Fin fin;
-  __device__ bool tile(int64_t cursor, TileRef &ref) const {
-    const int64_t t = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
-    if (t >= ts.ntiles) return false;
-    int64_t ti, tj;
-    tile_coords(ts, t, ti, tj);
-    ref.row0 = ti * kBM;
-    ref.col0 = tj * kBN;
-    ref.ma = &ma;
-    ref.mb = &mb;
-    ref.nk = nk;
-    ref.prob = 0;
-    return true;
-  }
-  static constexpr bool kPrefetch = false;
-  __device__ bool skip() const {
-    if constexpr (std::is_same<Fin, PearsonFinish>::value) return fin.skip();
-    return false;
-  }
-  __device__ const Fin &finish(const TileRef &) const { return fin; }
-  __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
-  __device__ void prefetch() const {
-    tc::prefetch_tensormap(&ma);
-    tc::prefetch_tensormap(&mb);
-  }
-};
-
-__device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ prefix, int64_t n,
-                                                int64_t x) {
-  int64_t lo = 0, hi = n;  // prefix has n + 1 entries; largest i with prefix[i] <= x
-  while (hi - lo > 1) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (prefix[mid] <= x) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// A batch of cor(x) problems: per-problem maps and finishes in device
-// memory; each CTA walks its own host-balanced list of global tile ids.
-struct PearsonBatchProblem {  // aligned as CUtensorMap
-  CUtensorMap map_a, map_b;  // 128-row and 256-row boxes over the same planes
-  TileSpace ts;
-  int64_t nk;
-  PearsonFinish fin;
-};
-
-struct PearsonBatchWork {
-  const PearsonBatchProblem *probs;
-  const int64_t *tile_prefix;
-  int64_t nprob;
-  const int64_t *cta_tiles, *cta_off;
-  __device__ bool tile(int64_t cursor, TileRef &ref) const {
-    const int64_t idx = cta_off[blockIdx.x] + cursor;
-    if (idx >= cta_off[blockIdx.x + 1]) return false;
-    const int64_t t = cta_tiles[idx];
-    const int64_t pi = find_segment(tile_prefix, nprob, t);
-    const PearsonBatchProblem &pr = probs[pi];
-    int64_t ti, tj;
-    tile_coords(pr.ts, t - tile_prefix[pi], ti, tj);
-    ref.row0 = ti * kBM;
-    ref.col0 = tj * kBN;
-    ref.ma = &pr.map_a;
-    ref.mb = &pr.map_b;
-    ref.nk = pr.nk;
-    ref.prob = pi;
-    return true;
-  }
-  static constexpr bool kPrefetch = false;
-  __device__ bool skip() const { return false; }
-  __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
-  __device__ void drain(EpiCtx &) const {}
-  __device__ void prefetch() const {}
-};
-
 // The dist layout in aligned lines (DistLines, LineTiles): the tiles' origins
 // come from a table, so that a lookup is one load the cursor issues a tile
 // ahead.
@@ -979,44 +623,9 @@ struct EuclidLineWork {
   }
 };
 
-// Walks this CTA's tiles first, first + step, ... of a work source.  With
-// Work::kPrefetch it looks up the next tile while the current one is
-// processed (the lookup is a global load); else it looks each tile up when it
-// is reached, holding no second TileRef.
-template <class Work, bool PREFETCH = Work::kPrefetch>
-struct TileCursor {
-  const Work &work;
-  TileRef nref;
-  int64_t cur;
-  int step;
-  bool have;
-  __device__ TileCursor(const Work &w, int first, int stp) : work(w), cur(first), step(stp) {
-    have = work.tile(cur, nref);
-  }
-  __device__ bool next(TileRef &ref) {
-    if (!have) return false;
-    ref = nref;
-    cur += step;
-    have = work.tile(cur, nref);
-    return true;
-  }
-};
-template <class Work>
-struct TileCursor<Work, false> {
-  const Work &work;
-  int64_t cur;
-  int step;
-  __device__ TileCursor(const Work &w, int first, int stp) : work(w), cur(first), step(stp) {}
-  __device__ bool next(TileRef &ref) {
-    const bool got = work.tile(cur, ref);
-    cur += step;
-    return got;
-  }
-};
-
 template <int KIND, int BK, bool CHUNKED, class Work>
 __global__ void __launch_bounds__(TcCfg<KIND, BK, !CHUNKED>::THREADS, 1)
-gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
+gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg wc) {
   using C = TcCfg<KIND, BK, !CHUNKED>;
   if (work.skip()) return;  // a gated launch whose gate is closed: before any setup
   constexpr int NSPLIT = C::NSPLIT;
@@ -1065,7 +674,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
         for (int64_t kb = 0; kb < ref.nk; kb++, it++) {
           const int s = int(it % C::STAGES);
           const uint32_t use = uint32_t(it / C::STAGES);
-          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
+          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, wc)) {
             *abort_flag = 1;
             break;
           }
@@ -1104,7 +713,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
         for (int64_t ch = 0; ch < nch && ok; ch++, cc++) {
           const int buf = int(cc & 1);
           const uint32_t ause = uint32_t(cc >> 1);
-          if (!tc::mbar_wait(&acce[buf], (ause & 1u) ^ 1u, abort_flag, kWaitLimitNs)) {
+          if (!tc::mbar_wait(&acce[buf], (ause & 1u) ^ 1u, abort_flag, wc)) {
             ok = false;
             break;
           }
@@ -1114,7 +723,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
           for (int64_t kb = kb0; kb < kb1; kb++, it++) {
             const int s = int(it % C::STAGES);
             const uint32_t use = uint32_t(it / C::STAGES);
-            if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, kWaitLimitNs)) {
+            if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, wc)) {
               ok = false;
               break;
             }
@@ -1171,7 +780,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
         for (int64_t ch = 0; ch < nch; ch++, cc++) {
           const int buf = int(cc & 1);
           const uint32_t ause = uint32_t(cc >> 1);
-          const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
+          const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, wc);
           if (!__all_sync(0xffffffffu, got)) {
             ok = false;
             break;
@@ -1202,7 +811,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
       } else {
         const int buf = int(cc & 1);
         const uint32_t ause = uint32_t(cc >> 1);
-        const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, kWaitLimitNs);
+        const bool got = tc::mbar_wait(&accf[buf], ause & 1u, abort_flag, wc);
         if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
@@ -1227,7 +836,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, int *err) {
     if (!ok) *abort_flag = 1;
   }
   __syncthreads();
-  if (*abort_flag && threadIdx.x == 0) atomicExch(err, 1);
+  if (*abort_flag && threadIdx.x == 0) atomicOr(wc.err, 1);
   if (warp == 1) {
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem_base, 2 * kBN);
@@ -1564,29 +1173,19 @@ int make_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpa
   return GT_OK;
 }
 
-// Device error word of the tensor-core kernels (bytes 64..67 of the small
-// scratch slot; bytes 0..3 hold the content-comparison flag).
-int err_word(int **p) {
-  void *v = nullptr;
-  GT_TRY(ws_get(WS_SCRATCH4, 256, &v));
-  *p = static_cast<int *>(v) + 16;
-  return GT_OK;
-}
-
 // Launches the persistent kernel over `ntiles` tiles of work source w.
 template <int KIND, int BK, bool CHUNKED, class W>
 int launch_work(const W &w, int64_t ntiles, int64_t ckb, const char *prof_name,
                 cudaStream_t s) {
   using C = TcCfg<KIND, BK, !CHUNKED>;
   if (ntiles == 0) return GT_OK;
-  int *err = nullptr;
-  GT_TRY(err_word(&err));
-  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  tc::WaitCfg wc;
+  GT_TRY(make_wait_cfg(&wc));
   auto kern = gram_tc_kernel<KIND, BK, CHUNKED, W>;
   GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
   const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
   ProfScope prof(prof_name, s);
-  kern<<<unsigned(grid), C::THREADS, C::SMEM, s>>>(w, ckb, err);
+  kern<<<unsigned(grid), C::THREADS, C::SMEM, s>>>(w, ckb, wc);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
@@ -1661,8 +1260,6 @@ int tc_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad,
   return make_plane_map(map, base, rows, kpad, nplanes, box_rows, bk, f16);
 }
 
-int tc_error_word(int **p) { return err_word(p); }
-
 // Mutual information from f16x3 weight planes (rows = variable * 2^lg + bin,
 // each weight times 2^14): the chunked Gram with MiFinish.
 int mi_tc(const void *planesX, int64_t rowsX, const void *planesY, int64_t rowsY, int64_t kpad,
@@ -1706,19 +1303,9 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
                                                 tc_chunk_kblocks(64), fin, "gemm_store", s);
 }
 
-int tc_check_error(cudaStream_t s, bool *failed) {
-  int *err = nullptr;
-  GT_TRY(err_word(&err));
-  int h = 0;
-  GT_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GT_CUDA(cudaStreamSynchronize(s));
-  *failed = h != 0;
-  if (h) GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  return GT_OK;
-}
-
 int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int kind, int slot_z,
                         int slot_st, void **Z, int64_t *kpad, cudaStream_t s) {
+  if (kind == tc::KIND_F16X6) return pearson_exact_prologue(dX, nvar, n, slot_z, Z, kpad, s);
   GT_TRY(check_kind(kind));
   *kpad = cdiv(n, kKPad) * kKPad;
   void *pz = nullptr, *pst = nullptr;
@@ -1743,6 +1330,7 @@ int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int kind, int 
 
 int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int kind,
                const PearsonOut &out, cudaStream_t s) {
+  if (kind == tc::KIND_F16X6) return pearson_exact(zA, nA, zB, nB, kpad, out, s);
   GT_TRY(check_kind(kind));
   if (nA == 0 || nB == 0) return GT_OK;
   if (!out.corr && !out.ts && !out.pairs) return GT_OK;
@@ -1861,7 +1449,10 @@ int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
   // paths use bf16x6.  Entries with d^2 below tau (|a|^2 + |b|^2) are
   // recomputed exactly: tau = 1/8 for bf16x6 (float32-level products), 1/4
   // for f16x3 (~2^-21 products).
-  if (gt_get_gram_path() == GT_GRAM_TC_F16X3)
+  // (the exact Pearson setting, f16x6, runs distances as f16x3: with the
+  // near-zero recomputation they already meet its precision)
+  const int path = gt_get_gram_path();
+  if (path == GT_GRAM_TC_F16X3 || path == GT_GRAM_TC_F16X6)
     return euclid_tc_kind<tc::KIND_F16X3>(d_pts, n, dim, d_out, layout, 0.25f, st);
   return euclid_tc_kind<tc::KIND_BF16X6>(d_pts, n, dim, d_out, layout, 0.125f, st);
 }
@@ -1960,14 +1551,16 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     if (bytes) GT_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
     return GT_OK;
   };
-  void *d_desc = nullptr, *d_tp = nullptr, *d_ct = nullptr, *d_co = nullptr, *d_err = nullptr;
+  void *d_desc = nullptr, *d_tp = nullptr, *d_ct = nullptr, *d_co = nullptr;
   GT_TRY(upload(inputs.data(), inputs.size() * sizeof(PearsonBatchInput), &d_in));
   GT_TRY(upload(var_prefix.data(), var_prefix.size() * 8, &d_vp));
   GT_TRY(upload(descs.data(), descs.size() * sizeof(PearsonBatchProblem), &d_desc));
   GT_TRY(upload(tile_prefix.data(), tile_prefix.size() * 8, &d_tp));
   GT_TRY(upload(cta_tiles.data(), cta_tiles.size() * 8, &d_ct));
   GT_TRY(upload(cta_off.data(), cta_off.size() * 8, &d_co));
-  GT_TRY(alloc(256, &d_err));
+  // the device's error word; the wait limit is the one in force when the plan is built
+  tc::WaitCfg wc;
+  GT_TRY(make_wait_cfg(&wc));
   PearsonBatchWork w;
   w.probs = static_cast<const PearsonBatchProblem *>(d_desc);
   w.tile_prefix = static_cast<const int64_t *>(d_tp);
@@ -1976,14 +1569,12 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
   w.cta_off = static_cast<const int64_t *>(d_co);
   auto *in = static_cast<const PearsonBatchInput *>(d_in);
   auto *vp = static_cast<const int64_t *>(d_vp);
-  auto *err = static_cast<int *>(d_err);
-  *err_out = err;
+  *err_out = wc.err;
   const int64_t total_vars = vars;
   const int BKc = bk;
   *ntiles_out = ntiles;
   *nctas_out = ncta;
   *run = [=](cudaStream_t s) -> int {
-    GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     if (total_vars == 0) return GT_OK;
     const int64_t blocks = cdiv(total_vars, 8);
     if (blocks > 2147483647LL) return fail(GT_EINVAL, "too many variables in the batch");
@@ -2000,7 +1591,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     if (ncta == 0) return GT_OK;
     auto launch = [&](auto kern, int smem) -> int {
       GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      kern<<<unsigned(ncta), TcCfg<tc::KIND_BF16X3, 32, false>::THREADS, smem, s>>>(w, ckb, err);
+      kern<<<unsigned(ncta), TcCfg<tc::KIND_BF16X3, 32, false>::THREADS, smem, s>>>(w, ckb, wc);
       return GT_OK;
     };
     if (kind == tc::KIND_BF16X6) {

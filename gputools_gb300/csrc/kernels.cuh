@@ -23,11 +23,9 @@ int euclid_tc(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
               cudaStream_t st);
 
 // gram_tc.cu: a 3-D TMA map over planes [nplanes][rows][kpad] of 16-bit
-// values (box {bk, box_rows, 1}; bk 32 -> 64-byte swizzle, 64 -> 128-byte),
-// and the tensor-core kernels' device error word.
+// values (box {bk, box_rows, 1}; bk 32 -> 64-byte swizzle, 64 -> 128-byte).
 int tc_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpad, int nplanes,
                  int box_rows, int bk, bool f16);
-int tc_error_word(int **p);
 
 // Per-variable statistics of the Pearson prologue.
 struct ColStats {
@@ -35,10 +33,6 @@ struct ColStats {
   double inv_norm;  // 1 / sqrt(sum (x - mean)^2), or 0 for a constant variable
   int flags;        // bit 0: contains NaN; bit 1: zero variance
 };
-
-// Reads and clears the tensor-core kernels' device error word (synchronises
-// `s`); *failed is set when a bounded wait inside a kernel gave up.
-int tc_check_error(cudaStream_t s, bool *failed);
 
 int launch_colstats(const float *dX, int64_t nvar, int64_t n, int use, ColStats *st,
                     cudaStream_t s);
@@ -58,6 +52,15 @@ struct PearsonOut {
 // (multiple of 64), zero padded.
 int pearson_tc(const void *d_zA, int64_t nA, const void *d_zB, int64_t nB, int64_t kpad,
                int kind, const PearsonOut &out, cudaStream_t st);
+
+// gram_exact.cu: the error-free Pearson Gram (GT_GRAM_TC_F16X6): the
+// prologue writes three fixed-point fp16 digit planes per variable
+// ([plane][variable][kpad], kpad a multiple of 64), the Gram sums their
+// products exactly in three TMEM accumulators, fused Pearson epilogue.
+int pearson_exact_prologue(const float *dX, int64_t nvar, int64_t n, int slot_z, void **Z,
+                           int64_t *kpad, cudaStream_t s);
+int pearson_exact(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
+                  const PearsonOut &out, cudaStream_t s);
 
 // pairwise_tc.cu: pairwise-complete Pearson on the tensor cores (masked
 // Gram of the six sums); every launch gated on the device flag run_if.

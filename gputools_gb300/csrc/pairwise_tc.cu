@@ -56,7 +56,6 @@ constexpr int kPEpi = 16;                          // epilogue warps
 constexpr int kPThreads = 64 + 32 * kPEpi;         // + producer and MMA warps
 constexpr int kPSmem = kPStages * kPStage + 1024 + 256;
 constexpr int kR1 = 0, kR2 = 160, kR3 = 224, kR4 = 256;  // TMEM columns of the regions
-constexpr uint64_t kPWaitNs = 2000000000ull;
 constexpr uint64_t kPDrainNs = 200000000ull;
 constexpr float kPScale = 16384.f;                 // 2^14
 
@@ -133,7 +132,7 @@ __device__ __forceinline__ float signif_pw(float r, float pairs) {
 }
 
 __global__ void __launch_bounds__(kPThreads, 1)
-pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
+pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc) {
   if (a.run_if && *a.run_if == 0) return;  // a gated launch whose gate is closed
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -178,7 +177,7 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
         for (int64_t kb = 0; kb < a.nk; kb++, it++) {
           const int s = int(it % kPStages);
           const uint32_t use = uint32_t(it / kPStages);
-          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, kPWaitNs)) {
+          if (!tc::mbar_wait(&empty[s], (use & 1u) ^ 1u, abort_flag, wc)) {
             *abort_flag = 1;
             break;
           }
@@ -212,7 +211,7 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
       for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
         for (int64_t ch = 0; ch < nch && ok; ch++, cc++) {
           // one accumulator: wait until the epilogue has read the last chunk
-          if (!tc::mbar_wait(acce, uint32_t(cc & 1) ^ 1u, abort_flag, kPWaitNs)) {
+          if (!tc::mbar_wait(acce, uint32_t(cc & 1) ^ 1u, abort_flag, wc)) {
             ok = false;
             break;
           }
@@ -222,7 +221,7 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
           for (int64_t kb = kb0; kb < kb1; kb++, it++) {
             const int s = int(it % kPStages);
             const uint32_t use = uint32_t(it / kPStages);
-            if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, kPWaitNs)) {
+            if (!tc::mbar_wait(&full[s], use & 1u, abort_flag, wc)) {
               ok = false;
               break;
             }
@@ -269,7 +268,7 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
 #pragma unroll
       for (int j = 0; j < 8; j++) sN[j] = sA[j] = sB[j] = sAA[j] = sBB[j] = sAB[j] = 0.f;
       for (int64_t ch = 0; ch < nch; ch++, cc++) {
-        const bool got = tc::mbar_wait(accf, uint32_t(cc & 1), abort_flag, kPWaitNs);
+        const bool got = tc::mbar_wait(accf, uint32_t(cc & 1), abort_flag, wc);
         if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
@@ -341,7 +340,7 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, int *err) {
     if (!ok) *abort_flag = 1;
   }
   __syncthreads();
-  if (*abort_flag && threadIdx.x == 0) atomicExch(err, 1);
+  if (*abort_flag && threadIdx.x == 0) atomicOr(wc.err, 1);
   if (warp == 1) {
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem_base, 512);
@@ -401,14 +400,15 @@ int pearson_pairwise_tc(const float *dA, int64_t nA, const float *dB, int64_t nB
   a.nc = nB;
   a.symmetric = sym ? 1 : 0;
   a.run_if = run_if;
-  int *err = nullptr;
-  GT_TRY(tc_error_word(&err));
-  GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  tc::WaitCfg wc;
+  GT_TRY(device_error_word(&wc.err));
+  wc.limit_ns = wait_limit_ns();
+  wc.hint_ns = wait_sleep_hint_ns();
   GT_CUDA(cudaFuncSetAttribute(pairwise_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                kPSmem));
   const int64_t grid = a.ntiles < sm_count() ? a.ntiles : sm_count();
   ProfScope prof("pearson_pairwise", s);
-  pairwise_tc_kernel<<<unsigned(grid), kPThreads, kPSmem, s>>>(a, err);
+  pairwise_tc_kernel<<<unsigned(grid), kPThreads, kPSmem, s>>>(a, wc);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;

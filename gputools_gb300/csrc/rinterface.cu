@@ -48,7 +48,7 @@ extern "C" {
 int gt_set_gram_path(int path) {
   gt::clear_error();
   if (path != GT_GRAM_TC_BF16X3 && path != GT_GRAM_TC_BF16X6 && path != GT_GRAM_FP32 &&
-      path != GT_GRAM_TC_F16X3)
+      path != GT_GRAM_TC_F16X3 && path != GT_GRAM_TC_F16X6)
     return gt::fail(GT_EINVAL, "unknown gram path %d", path);
   gt::g_gram_path.store(path);
   return GT_OK;

@@ -26,8 +26,12 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   void *slot[WS_NSLOTS] = {};
   size_t bytes[WS_NSLOTS] = {};
+  int *err = nullptr;  // error word of the kernels with bounded waits
   int sms = 0;
 };
+
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;  // 2 s per barrier wait
+std::atomic<uint64_t> g_wait_ns{kDefaultWaitNs};
 
 std::mutex g_mu;
 DeviceState g_dev[kMaxDevices];
@@ -171,13 +175,58 @@ int ws_get(int slot, size_t bytes, void **ptr) {
   return GT_OK;
 }
 
+int device_error_word(int **p) {
+  int dev = 0;
+  GT_TRY(current_device(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState &d = g_dev[dev];
+  if (!d.err) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, 256);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GT_ENOMEM, "device error word unavailable: %s", cudaGetErrorString(e));
+    }
+    e = cudaMemset(q, 0, 256);
+    if (e != cudaSuccess) {
+      cudaFree(q);
+      return fail(GT_ECUDA, "clearing the device error word: %s", cudaGetErrorString(e));
+    }
+    d.err = static_cast<int *>(q);
+  }
+  *p = d.err;
+  return GT_OK;
+}
+
+int device_error_check(cudaStream_t s, bool *failed) {
+  *failed = false;
+  int *err = nullptr;
+  GT_TRY(device_error_word(&err));
+  int h = 0;
+  GT_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GT_CUDA(cudaStreamSynchronize(s));
+  if (h) {
+    *failed = true;
+    GT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    GT_CUDA(cudaStreamSynchronize(s));
+  }
+  return GT_OK;
+}
+
+uint64_t wait_limit_ns() { return g_wait_ns.load(); }
+
+uint32_t wait_sleep_hint_ns() {
+  const uint64_t w = g_wait_ns.load();
+  return w < 100000ull ? uint32_t(w) : 100000u;
+}
+
 void ws_release_all() {
   std::lock_guard<std::mutex> lk(g_mu);
   int cur = -1;
   cudaGetDevice(&cur);
   for (int dev = 0; dev < kMaxDevices; dev++) {
     DeviceState &d = g_dev[dev];
-    bool any = false;
+    bool any = d.err != nullptr;
     for (int s = 0; s < WS_NSLOTS; s++) any |= d.slot[s] != nullptr;
     if (!any) continue;
     cudaSetDevice(dev);
@@ -187,6 +236,8 @@ void ws_release_all() {
       d.slot[s] = nullptr;
       d.bytes[s] = 0;
     }
+    if (d.err) cudaFree(d.err);
+    d.err = nullptr;
   }
   if (cur >= 0) cudaSetDevice(cur);
 }
@@ -202,6 +253,20 @@ int gt_version(void) { return 10000; }
 uint64_t gt_kernel_launches(void) { return gt::g_launches.load(); }
 
 void gt_release_workspace(void) { gt::ws_release_all(); }
+
+int gt_device_status(void *stream) {
+  gt::clear_error();
+  bool failed = false;
+  GT_TRY(gt::device_error_check(static_cast<cudaStream_t>(stream), &failed));
+  if (failed) return gt::fail(GT_ETIMEOUT, "a bounded wait inside a device kernel timed out");
+  return GT_OK;
+}
+
+int gt_set_wait_limit_ns(uint64_t ns) {
+  gt::clear_error();
+  gt::g_wait_ns.store(ns == 0 ? gt::kDefaultWaitNs : ns);
+  return GT_OK;
+}
 
 void gt_profile_enable(int on) { gt::g_prof_on.store(on ? 1 : 0); }
 

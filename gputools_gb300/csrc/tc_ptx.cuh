@@ -71,18 +71,32 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
 
 constexpr uint32_t kSleepHintNs = 100000;  // 0.1 ms: well inside every wait limit
 
+// Bounded-wait settings of a launch: the device error word a CTA sets when
+// one of its waits gives up, the limit of each wait, and the sleep hint
+// (at most the limit, so that a short limit is honoured).
+struct WaitCfg {
+  int *err;
+  uint64_t limit_ns;
+  uint32_t hint_ns;
+};
+
 // Waits for the phase of `bar` with the given parity.  Gives up (returns
 // false) after `limit_ns` or as soon as *abort becomes non-zero, so a kernel
 // never spins forever on a barrier that will not complete.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                          uint64_t limit_ns) {
+                                          uint64_t limit_ns, uint32_t hint_ns = kSleepHintNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   while (true) {
-    if (mbar_try_wait_sleep(bar, parity, kSleepHintNs)) return true;
+    if (mbar_try_wait_sleep(bar, parity, hint_ns)) return true;
     if (*abort) return false;
     if (globaltimer_ns() - t0 > limit_ns) return false;
   }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                          const WaitCfg &wc) {
+  return mbar_wait(bar, parity, abort, wc.limit_ns, wc.hint_ns);
 }
 
 // Bounded wait that ignores the abort flag (used to drain in-flight work).
@@ -250,6 +264,8 @@ __host__ __device__ constexpr uint32_t idesc_f32acc(int M, int N, uint32_t ab_fm
 //           lo the next 11, so the three products keep ~2^-22 per element
 //           at the cost of bf16x3.
 constexpr int KIND_BF16X3 = 0, KIND_BF16X6 = 1, KIND_F16X3 = 3;
+// The error-free fixed-point split (gram_exact.cu) has its own kernel.
+constexpr int KIND_F16X6 = 4;
 
 template <int KIND>
 struct Kind {

@@ -62,7 +62,10 @@ enum gt_gram_path {
   GT_GRAM_TC_BF16X3 = 0, /* tcgen05, each operand split hi+lo bf16, 3 products */
   GT_GRAM_TC_BF16X6 = 1, /* tcgen05, 3-way bf16 split, 6 products             */
   GT_GRAM_FP32 = 2,      /* plain FP32 CUDA-core path                         */
-  GT_GRAM_TC_F16X3 = 3   /* tcgen05, power-of-two scaled hi+lo fp16, 3 products */
+  GT_GRAM_TC_F16X3 = 3,  /* tcgen05, power-of-two scaled hi+lo fp16, 3 products */
+  GT_GRAM_TC_F16X6 = 4   /* tcgen05, three fixed-point fp16 digits per value whose
+                            products sum exactly in FP32 (error-free split),
+                            6 products; Pearson only (gpuDist runs f16x3) */
 };
 
 /* ======================================================================== *
@@ -150,6 +153,22 @@ const char *gt_last_error(void);
 int gt_version(void);
 /* Frees the device workspace of every device this thread touched. */
 void gt_release_workspace(void);
+
+/* Bounded device-side waits.  The tensor-core kernels never wait without a
+ * limit: a wait that gives up makes its CTA stop, drain its copies and
+ * multiplies, free its tensor memory and set the device's error word, and
+ * the call's results are then incomplete.  The host-buffer entries (gt_pmcc,
+ * gt_distances, gt_mutual_info, the .C entries) read the word before they
+ * return and report GT_ETIMEOUT.  Device-buffer entries and batch-plan
+ * launches are asynchronous and report it only through gt_device_status:
+ * it synchronises `stream`, returns GT_ETIMEOUT if any such kernel on the
+ * current device timed out since the last check on that device (and clears
+ * the word), else GT_OK. */
+int gt_device_status(void *stream);
+/* Limit of each bounded wait in nanoseconds for launches made afterwards by
+ * this process (0 restores the default of 2 s).  A diagnostic: a very short
+ * limit makes waits give up while their work is still in flight. */
+int gt_set_wait_limit_ns(uint64_t ns);
 /* Number of CUDA kernels this library has launched in this process (a
  * monotone counter, for measuring how many launches a call makes). */
 uint64_t gt_kernel_launches(void);

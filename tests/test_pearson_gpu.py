@@ -7,6 +7,10 @@ Tolerances, per Gram evaluation:
   bf16x6  same as fp32                  (3-way bf16 split: float32-exact products)
   bf16x3  2e-5                          (2-way split drops the lo*lo product, ~2^-16)
   f16x3   same as fp32                  (scaled 2-way fp16 split, ~2^-21 per product)
+  f16x6   1.5e-7                        (fixed-point fp16 digits summed exactly: only
+                                         the float rounding of r remains)
+The metric's bar -- max relative error <= 1e-6 against FP64 for |r| >= 0.01 --
+is asserted for f16x6 at 4096 observations (test_relative_error_bar).
 pairs must match exactly; t-scores are checked against hostSignif's rule
 applied to the returned r, and against the oracle away from |r| -> 1.
 """
@@ -17,12 +21,14 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-PATHS = ("fp32", "bf16x3", "bf16x6", "f16x3")
+PATHS = ("fp32", "bf16x3", "bf16x6", "f16x3", "f16x6")
 
 
 def tol(path, n):
     if path == "bf16x3":
         return 2e-5
+    if path == "f16x6":
+        return 1.5e-7
     return 2e-6 * np.sqrt(max(n, 1) / 100.0) + 1e-6
 
 
@@ -173,13 +179,15 @@ def test_pairwise_missing_long_columns(gpu, oracle_mod, rng, path, frac):
     corr, pairs, ts = rpmcc(gpu, 1, A, A.copy())
     wc, wp, wt = oracle_mod.pearson(A, use=1)
     assert np.array_equal(pairs, wp.astype(np.float32))
-    check_r(corr, wc, 2e-5 if path == "bf16x3" else tol(path, n))
+    # the masked Gram of the six sums carries the f16x3 split whatever the path
+    ptol = 2e-5 if path == "bf16x3" else tol("f16x3" if path == "f16x6" else path, n)
+    check_r(corr, wc, ptol)
     B = (rng.standard_normal((70, n)) - 3).astype(np.float32)
     B[rng.random(B.shape) < frac] = np.nan
     corr, pairs, _ = rpmcc(gpu, 1, A, B)
     wc, wp, _ = oracle_mod.pearson(A, B, use=1)
     assert np.array_equal(pairs, wp.astype(np.float32))
-    check_r(corr, wc, 2e-5 if path == "bf16x3" else tol(path, n))
+    check_r(corr, wc, ptol)
 
 
 def test_pairwise_degenerate(gpu, oracle_mod):
@@ -240,3 +248,65 @@ def test_everything_large_output_pairs_from_host(gpu):
     want = np.corrcoef(X.astype(np.float64))[rows]
     assert np.max(np.abs(corr[rows] - want)) < 5e-6
     assert np.all(np.isfinite(ts[rows]))
+
+
+def _rel_err(got, want, floor):
+    ok = ~np.isnan(want) & (np.abs(want) >= floor)
+    return float((np.abs(got[ok].astype(np.float64) - want[ok]) / np.abs(want[ok])).max())
+
+
+@pytest.mark.parametrize("sym", [True, False])
+def test_relative_error_bar(gpu, oracle_mod, sym):
+    """Max relative error of r <= 1e-6 against the FP64 oracle for every entry
+    with |r| >= 0.01, on the error-free f16x6 path, at the precision
+    configuration's length and distribution (4096 observations,
+    lognormal(5, 1) plus per-column offsets in [0, 1e3]), with correlated
+    blocks so that |r| spans 0.01 .. 1 (near-collinear pairs included)."""
+    import gputools_gb300 as g
+    rng = np.random.default_rng(2024)
+    n, p = 4096, 384
+    base = rng.lognormal(5.0, 1.0, (p, n))
+    # every 8th variable gets partners at several mixing weights
+    for j in range(0, p - 7, 8):
+        for t, w in enumerate((1e-4, 1e-2, 0.1, 0.5, 0.9, 3.0, 30.0)):
+            base[j + 1 + t] = base[j] + w * base[j + 1 + t]
+    X = (base + rng.uniform(0, 1e3, (p, 1))).astype(np.float32)
+    old = g.get_gram_path()
+    g.set_gram_path("f16x6")
+    try:
+        if sym:
+            corr, _, _ = rpmcc(gpu, 0, X, X.copy())
+            wc, _, _ = oracle_mod.pearson(X, use=0)
+            np.fill_diagonal(wc, 1.0)
+        else:
+            A, B = X[: p // 2], X[p // 2 - 40:]
+            corr, _, _ = rpmcc(gpu, 0, A, B)
+            wc, _, _ = oracle_mod.pearson(A, B, use=0)
+    finally:
+        g.set_gram_path(old)
+    assert np.abs(wc).max() > 0.999  # near-collinear pairs are present
+    assert (np.abs(wc) < 0.02).sum() > 100  # and small correlations
+    assert _rel_err(corr, wc, 0.01) <= 1e-6
+    assert _rel_err(corr, wc, 0.1) <= 1e-6
+    assert np.abs(corr.astype(np.float64) - wc).max() <= 1.5e-7
+
+
+def test_exact_path_long_columns_and_ragged_sizes(gpu, oracle_mod, rng):
+    """f16x6 over 20000 observations (exactness of the first sum does not
+    depend on the length) and sizes that are not multiples of the tiles."""
+    import gputools_gb300 as g
+    n = 20000
+    A = (rng.standard_normal((131, n)) * 1e-3 + 1e3).astype(np.float32)
+    B = rng.standard_normal((257, n)).astype(np.float32)
+    B[3] = A[5] * 2 - B[3] * 1e-6
+    old = g.get_gram_path()
+    g.set_gram_path("f16x6")
+    try:
+        corr, pairs, ts = rpmcc(gpu, 0, A, B)
+    finally:
+        g.set_gram_path(old)
+    wc, wp, wt = oracle_mod.pearson(A, B, use=0)
+    assert np.array_equal(pairs, wp.astype(np.float32))
+    assert np.abs(corr.astype(np.float64) - wc).max() <= 1.5e-7
+    assert _rel_err(corr, wc, 0.01) <= 1e-6
+    check_ts(ts, corr, pairs, wt, wc)
