@@ -4,16 +4,19 @@
 Headline workload (the configuration the metric is quoted on): gpuCor
 pearson, cor(x) of x = 4096 observations x 20000 variables float32, values
 lognormal(mu=5, sigma=1) plus per-column offsets uniform in [0, 1e3].  One
-step = one full gt_pmcc_device call (FP64 column statistics, split-bf16
-tcgen05 Gram contraction, fused epilogue writing coefficients, t-scores and
-pair counts for all 20000^2 entries).  value = entries of the returned matrix
-per second.  The same line also carries the plain FP32 CUDA-core path and the
-3-way split on the same workload, the Euclidean precision workload (100000
-points x 128 from 1000 clusters, sd 1e-3, 5% exact duplicates, R `dist`
-layout), the max error against the FP64 oracle on sampled rows, the
-end-to-end number through the host C ABI (pinned host buffers, copies inside
-the timed region), the roofline of the Gram kernel, clocks and a CPU
-baseline.
+step = one full gt_pmcc_device call (FP64 column statistics, tcgen05 Gram
+contraction, fused epilogue writing coefficients, t-scores and pair counts
+for all 20000^2 entries).  value = entries of the returned matrix per
+second, on the Gram path that meets the metric's bar (max relative error
+<= 1e-6 against FP64 for |r| >= 0.01): the error-free f16x6 split.  The same
+line carries every other Gram path on the same workload (f16x3, bf16x6,
+bf16x3, the plain FP32 CUDA-core path) with their errors against the FP64
+oracle on sampled rows, the Euclidean precision workload (100000 points x
+128 from 1000 clusters, sd 1e-3, 5% exact duplicates, R `dist` layout), the
+end-to-end number through the host C ABI with the ordinary (pageable) host
+buffers R's .C passes (pinned buffers beside it), the roofline of the Gram
+kernel, clocks, the CPU baseline, and -- where the reference's own code is
+built on the host -- its GPU path and host loops timed on the same machine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -250,10 +253,10 @@ def run_ours(args, ranks: Ranks):
         ms = e0.elapsed_time(e1) / steps
         return ranks.max(ms), lib.gt_kernel_launches() - l0
 
-    # headline path: three-product scaled split-fp16 on tensor cores (max abs
-    # err of r <= 1e-6 against FP64 at the cost of split-bf16x3), unless the
+    # headline path: the error-free fixed-point split (f16x6: relative error of
+    # r <= 1e-6 against FP64 for |r| >= 0.01, the metric's bar), unless the
     # tensor-core path is unavailable
-    headline = "f16x3"
+    headline = "f16x6"
     try:
         g.set_gram_path(headline)
         pearson_step()
@@ -280,56 +283,81 @@ def run_ours(args, ranks: Ranks):
     rng = np.random.default_rng(7)
     rows = np.sort(rng.choice(P, SAMPLE_ROWS, replace=False))
 
-    def max_err(c):
-        got = c[torch.from_numpy(rows).to(dev)].cpu().numpy().astype(np.float64)
-        want, _, _ = oracle.pearson(X[rows], X)
-        for k, r in enumerate(rows):
-            want[k, r] = 1.0
-        d = np.abs(got - want)
-        big = np.abs(want) >= 1e-2
-        return float(d.max()), float((d[big] / np.abs(want[big])).max())
-
     t_cpu0 = time.perf_counter()
-    err_abs, err_rel = max_err(corr)
-    cpu_dt = time.perf_counter() - t_cpu0  # includes the oracle on SAMPLE_ROWS rows
+    want_rows, _, _ = oracle.pearson(X[rows], X)
+    cpu_dt = time.perf_counter() - t_cpu0  # the oracle on SAMPLE_ROWS rows
+    for k, r in enumerate(rows):
+        want_rows[k, r] = 1.0
+
+    def max_err(c):
+        """max |dr|, and max |dr| / |r| over the entries with |r| >= 0.1 and >= 0.01"""
+        got = c[torch.from_numpy(rows).to(dev)].cpu().numpy().astype(np.float64)
+        d = np.abs(got - want_rows)
+        res = {"max_abs_err": float(d.max())}
+        for floor in (0.1, 0.01):
+            big = np.abs(want_rows) >= floor
+            res[f"max_rel_err_r_ge_{floor}"] = float((d[big] / np.abs(want_rows[big])).max())
+        return res
+
+    head_err = max_err(corr)
 
     # the other Gram paths on the same workload (rank 0 only; extras)
     paths = {}
     if ranks.rank == 0:
-        for pth in ("fp32", "bf16x6", "bf16x3", "f16x3"):
+        for pth in ("f16x6", "f16x3", "bf16x6", "bf16x3", "fp32"):
             if pth == headline:
                 paths[pth] = {"entries_per_s": value / ranks.world, "ms_per_step": ms,
-                              "max_abs_err": err_abs, "max_rel_err_r_ge_0.01": err_rel}
+                              "gram_ms": gram_ms.value / max(1, gram_n.value), **head_err}
                 continue
             try:
                 g.set_gram_path(pth)
                 k = max(3, args.steps // 4)
+                lib.gt_profile_reset()
+                lib.gt_profile_enable(1)
                 pms, _ = timed(pearson_step, k, 1)
-                a, r = max_err(corr)
+                lib.gt_profile_enable(0)
+                gms = ctypes.c_double(0); gn = ctypes.c_uint64(0)
+                lib.gt_profile_kernel_ms(b"pearson_gram", ctypes.byref(gms), ctypes.byref(gn))
                 paths[pth] = {"entries_per_s": entries / (pms * 1e-3), "ms_per_step": pms,
-                              "max_abs_err": a, "max_rel_err_r_ge_0.01": r}
+                              "gram_ms": gms.value / max(1, gn.value), **max_err(corr)}
             except _lib.GpuToolsError as e:
                 paths[pth] = {"unavailable": str(e)}
+        for pth, rec in paths.items():
+            if "max_rel_err_r_ge_0.01" in rec:
+                rec["meets_1e-6_rel_bar"] = rec["max_rel_err_r_ge_0.01"] <= 1e-6
+        if "fp32" in paths and "entries_per_s" in paths["fp32"]:
+            for rec in paths.values():
+                if "entries_per_s" in rec:
+                    rec["x_fp32_path"] = rec["entries_per_s"] / paths["fp32"]["entries_per_s"]
         g.set_gram_path(headline)
 
-    # end to end through the host C ABI: pinned buffers, copies timed
-    hX = torch.from_numpy(X).pin_memory()
-    hc = torch.empty((P, P), dtype=torch.float32).pin_memory()
-    ht = torch.empty((P, P), dtype=torch.float32).pin_memory()
-    hp = torch.empty((P, P), dtype=torch.float32).pin_memory()
+    # end to end through the host C ABI, copies inside the timed region: with
+    # ordinary pageable numpy buffers (what R's .C hands the library: gt_pmcc
+    # page-locks them for the call), and with page-locked buffers
     del corr, ts, pairs
     torch.cuda.empty_cache()
-
-    def e2e_step():
-        _lib.check(lib.gt_pmcc(0, vp(hX), P, vp(hX), P, N_OBS, vp(hp), vp(hc), vp(ht)))
-
     e2e_steps = max(3, args.steps // 4)
-    e2e_step()
-    ranks.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = ranks.max((time.perf_counter() - t0) / e2e_steps)
+    fp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+
+    def e2e_time(hX, hp, hc, ht):
+        step = lambda: _lib.check(lib.gt_pmcc(0, hX, P, hX, P, N_OBS, hp, hc, ht))
+        step()
+        ranks.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            step()
+        return ranks.max((time.perf_counter() - t0) / e2e_steps)
+
+    # pageable: numpy arrays, every page touched before the call (as R's
+    # vectors are: .C passes filled copies)
+    nX = np.ascontiguousarray(X)
+    nbufs = [np.zeros((P, P), np.float32) for _ in range(3)]
+    e2e_s = e2e_time(fp(nX), *(fp(b) for b in nbufs))
+    del nbufs
+    hX = torch.from_numpy(X).pin_memory()
+    pbufs = [torch.empty((P, P), dtype=torch.float32).pin_memory() for _ in range(3)]
+    e2e_pinned_s = e2e_time(vp(hX), *(vp(b) for b in pbufs))
+    del pbufs, hX
     clk = clocks.stop()
 
     # Euclidean precision workload (rank 0; R dist layout, 5e9 entries)
@@ -337,6 +365,7 @@ def run_ours(args, ranks: Ranks):
     if ranks.rank == 0 and not args.skip_euclid:
         euclid = run_euclid(args, lib, g, _lib, stream, dev, headline)
     others = run_configs(lib, g, _lib, stream, dev, args.steps) if ranks.rank == 0 else {}
+    refcode = run_reference_code(lib, _lib, max(3, args.steps // 4)) if ranks.rank == 0 else {}
 
     if ranks.rank != 0:
         return
@@ -345,14 +374,15 @@ def run_ours(args, ranks: Ranks):
     tc = headline != "fp32"
     if tc:
         # the tensor-core fraction counts the issued MMA flops: every useful
-        # flop of the split encodings is 3 (bf16x3, f16x3) or 6 (bf16x6)
-        # tensor-core flops
-        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        # flop of the split encodings is 3 (bf16x3, f16x3) or 6 (bf16x6,
+        # f16x6) tensor-core flops.  The timed region is a burst (steps x a
+        # few ms), so the peak is the measured burst rate
+        peak = peaks.get("bf16_tflops", peaks.get("bf16_tflops_sustained"))
         useful = flops / (gram_avg_ms * 1e-3) / 1e12
-        products = {"bf16x3": 3, "bf16x6": 6, "f16x3": 3}[headline]
+        products = {"bf16x3": 3, "bf16x6": 6, "f16x3": 3, "f16x6": 6}[headline]
         achieved = useful * products
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 sustained",
+                "frac": achieved / peak, "peak_kind": f"{peaks_kind} bf16 burst",
                 "flops": f"issued MMA flops: {products} split products x 2*n per unique entry",
                 "useful_tflops": useful, "useful_frac": useful / peak,
                 "kernel": "pearson_gram (tcgen05)", "kernel_ms": gram_avg_ms,
@@ -378,19 +408,25 @@ def run_ours(args, ranks: Ranks):
                    "gram_path": headline, "parallelism": "replicas" if ranks.world > 1 else "single"},
         "e2e": {"value": ranks.world * entries / e2e_s, "unit": "entries/s",
                 "h2d_bytes_per_step": int(P * N_OBS * 4), "d2h_bytes_per_step": int(2 * P * P * 4),
-                "api": "gt_pmcc (host buffers, pinned; the kernels write r and t in place over the "
-                       "host link, the constant pair counts n are filled by host threads meanwhile)",
-                "ms_per_step": e2e_s * 1e3},
+                "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the library "
+                       "page-locks the outputs for the call and the kernels write r and t in place "
+                       "over the host link; the constant pair counts n are filled by host threads "
+                       "meanwhile)",
+                "ms_per_step": e2e_s * 1e3,
+                "pinned": {"value": ranks.world * entries / e2e_pinned_s,
+                           "ms_per_step": e2e_pinned_s * 1e3}},
         "gpu_launches": int(launches),
         "roofline": roof,
-        "precision": {"max_abs_err_r": err_abs, "max_rel_err_r_ge_0.01": err_rel,
+        "precision": {**head_err, "path": headline,
                       "sample": f"{SAMPLE_ROWS} rows x {N_VARS} vs FP64 oracle"},
         "paths": paths,
         "euclid": euclid,
         "configs": others,
         "cpu_baseline": {"value": SAMPLE_ROWS * P / cpu_dt, "unit": "entries/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"FP64 oracle, {SAMPLE_ROWS} rows x {N_VARS} vars x {N_OBS} obs"},
+                         "sample": f"FP64 oracle, {SAMPLE_ROWS} rows x {N_VARS} vars x {N_OBS} obs",
+                         "reference_host_loops": refcode.get("host_loops")},
+        "reference_gpu_path": refcode.get("gpu_path"),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -692,6 +728,70 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     return out
 
 
+def run_reference_code(lib, _lib, k):
+    """The reference's own code, where it is built on this host from the
+    staged reference sources (oracle/build_ref.sh, oracle/build_ref_gpu.sh):
+    its host loops single-threaded (distance_host, src/distance.cpp:174-207;
+    permHostKendall, src/correlation.cpp:506-516) and its GPU path
+    (pmcc, src/correlation.cpp:66-161, and distance(), src/distance.cpp:259-316,
+    with the kernels of inst/cuda, through the same host-buffer calls) beside
+    this library's host entry on the same inputs: gpuCor's 500 x 1000 and
+    gpuDist's 2000 x 64 configurations."""
+    import oracle
+    out = {}
+    rng = np.random.default_rng(31)
+    fp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    pts = rng.standard_normal((2000, 64)).astype(np.float32)
+    Xp = rng.standard_normal((1000, 500)).astype(np.float32)
+    if oracle.ref_available():
+        t0 = time.perf_counter()
+        oracle.ref_distance_host(pts, "euclidean")
+        dt = time.perf_counter() - t0
+        Xk = rng.integers(0, 10, (1000, 500)).astype(np.float32)
+        t0 = time.perf_counter()
+        oracle.ref_host_kendall(Xk[:4], Xk)
+        dk = time.perf_counter() - t0
+        out["host_loops"] = {
+            "cores": 1, "compiled": "g++ -O3 from the reference's src/*.cpp",
+            "distance_host_euclidean_2000x64": {"s": dt, "entries_per_s": 2000 * 2000 / dt},
+            "permHostKendall_500obs": {"sample": "4 x 1000 variable pairs", "s": dk,
+                                       "entries_per_s": 4000 / dk}}
+    if oracle.ref_gpu_available():
+        rec = {"kernels": "the reference's inst/cuda kernels, nvcc --use_fast_math for sm_103a, "
+                          "launched by name; its host code allocates, copies and frees per call"}
+        Xb = Xp.copy()  # R's .C passes two copies of x
+        hc = np.empty((1000, 1000), np.float32); ht = np.empty_like(hc); hp = np.empty_like(hc)
+        oracle.ref_gpu_pmcc(Xp, Xb)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            rc_, _, _ = oracle.ref_gpu_pmcc(Xp, Xb)
+        ref_ms = (time.perf_counter() - t0) / k * 1e3
+        _lib.check(lib.gt_pmcc(0, fp(Xp), 1000, fp(Xb), 1000, 500, fp(hp), fp(hc), fp(ht)))
+        t0 = time.perf_counter()
+        for _ in range(k):
+            _lib.check(lib.gt_pmcc(0, fp(Xp), 1000, fp(Xb), 1000, 500, fp(hp), fp(hc), fp(ht)))
+        ours_ms = (time.perf_counter() - t0) / k * 1e3
+        rec["pearson_500x1000"] = {"reference_ms": ref_ms, "ours_ms": ours_ms,
+                                   "speedup": ref_ms / ours_ms,
+                                   "max_abs_diff_r": float(np.abs(rc_ - hc).max())}
+        hd = np.empty((2000, 2000), np.float32)
+        oracle.ref_gpu_distance(pts, "euclidean")
+        t0 = time.perf_counter()
+        for _ in range(k):
+            rd = oracle.ref_gpu_distance(pts, "euclidean")
+        ref_ms = (time.perf_counter() - t0) / k * 1e3
+        _lib.check(lib.gt_distances(fp(pts), 2000, 64, fp(hd), 0, ctypes.c_float(2.0)))
+        t0 = time.perf_counter()
+        for _ in range(k):
+            _lib.check(lib.gt_distances(fp(pts), 2000, 64, fp(hd), 0, ctypes.c_float(2.0)))
+        ours_ms = (time.perf_counter() - t0) / k * 1e3
+        rec["euclid_2000x64"] = {"reference_ms": ref_ms, "ours_ms": ours_ms,
+                                 "speedup": ref_ms / ours_ms,
+                                 "max_rel_diff": float(np.max(np.abs(rd - hd) / np.maximum(hd, 1e-3)))}
+        out["gpu_path"] = rec
+    return out
+
+
 def run_hclust(g, dev):
     """gpuHclust, average linkage, on the euclidean distances of 10000 points
     in 16 dimensions drawn around 8 centres: the merge loop alone (a fresh
@@ -753,8 +853,14 @@ def run_batches(g, stream, dev, k):
           for p, n in zip(ps, ns)]
     entries = float(np.sum(ps.astype(np.float64) ** 2))
     useful = float(np.sum(2.0 * ps.astype(np.float64) ** 2 * ns))
+    # batches run the f16x3 split (the plan takes the Gram path at creation)
+    old_path = g.get_gram_path()
+    g.set_gram_path("f16x3")
     t0 = time.perf_counter()
-    plan = g.BatchPlan(xs, "pearson", autotune=True)
+    try:
+        plan = g.BatchPlan(xs, "pearson", autotune=True)
+    finally:
+        g.set_gram_path(old_path)
     build_s = time.perf_counter() - t0
     e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
     plan.launch(stream)

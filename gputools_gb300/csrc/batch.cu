@@ -306,6 +306,9 @@ int pearson_batch_plan(const gt_cor_problem *probs, int64_t count, int flags,
   const int path = gt_get_gram_path();
   if (path == GT_GRAM_FP32)
     return fail(GT_EUNSUPPORTED, "batched Pearson runs on the tensor-core Gram paths");
+  if (path == GT_GRAM_TC_F16X6)
+    return fail(GT_EUNSUPPORTED,
+                "batched Pearson runs the f16x3, bf16x3 and bf16x6 splits, not f16x6");
   const bool x6 = path == GT_GRAM_TC_BF16X6;
   const TileConfig *cands = x6 ? kX6Configs : kX3Configs;
   const int ncand = x6 ? int(sizeof(kX6Configs) / sizeof(kX6Configs[0]))

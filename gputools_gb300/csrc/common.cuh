@@ -37,6 +37,21 @@ const char *last_error();
 // Library-private non-blocking stream of the current device (created once).
 cudaStream_t lib_stream();
 
+// Synchronises a stream when it goes out of scope.  A host entry that queues
+// copies from or to the caller's memory holds one, so that no return path
+// -- an error after the first copy included -- leaves copies running on
+// memory the caller owns again.
+class StreamSyncGuard {
+ public:
+  explicit StreamSyncGuard(cudaStream_t s) : s_(s) {}
+  ~StreamSyncGuard() { cudaStreamSynchronize(s_); }
+  StreamSyncGuard(const StreamSyncGuard &) = delete;
+  StreamSyncGuard &operator=(const StreamSyncGuard &) = delete;
+
+ private:
+  cudaStream_t s_;
+};
+
 // Named slots of the per-device workspace.  Each slot is a grow-only device
 // buffer kept across calls and released by gt_release_workspace().
 enum WsSlot {
@@ -70,6 +85,33 @@ class ProfScope {
 // pages, even where the GPU can reach them, may be unpopulated and fault one
 // by one.  GT_DIRECT_HOST=0 disables it.
 void *host_direct_ptr(void *host);
+
+// A host output buffer of a synchronous entry, as its kernels reach it.
+// map() returns the device-usable address of `host` (`bytes` long), or
+// nullptr when it must be staged through device memory:
+//  * page-locked memory is written in place;
+//  * pageable memory from kRegisterMin bytes on (R's .C vectors are such) is
+//    page-locked for the call with cudaHostRegister and written in place --
+//    on GB300 this costs ~1.6 ms per GB and the kernels then write at the
+//    host link's rate, where a staged pageable copy runs at half of it;
+//  * anything else (small, or not registrable) is staged.
+// The registration is released by the destructor: declare the object before
+// the StreamSyncGuard of the call, so that the stream is synchronised first.
+// GT_DIRECT_HOST=0 disables writing in place, GT_REGISTER_HOST=0 only the
+// registration.
+class HostOutput {
+ public:
+  static constexpr size_t kRegisterMin = size_t(1) << 20;
+  HostOutput() = default;
+  ~HostOutput();
+  HostOutput(const HostOutput &) = delete;
+  HostOutput &operator=(const HostOutput &) = delete;
+  void *map(void *host, size_t bytes);
+  bool registered() const { return reg_ != nullptr; }
+
+ private:
+  void *reg_ = nullptr;
+};
 
 // Per-device error word of the kernels with bounded waits (allocated and
 // zeroed on first use, kept until gt_release_workspace).  Kernels only set it;

@@ -744,6 +744,7 @@ extern "C" int gt_hclust(const float *dist, int64_t n, const char *method, int *
   if (n < 2) return gt::fail(GT_EINVAL, "must have n >= 2 objects to cluster");
   if (!dist) return gt::fail(GT_EINVAL, "null pointer");
   cudaStream_t s = gt::lib_stream();
+  gt::StreamSyncGuard guard(s);
   void *dd = nullptr;
   const size_t bytes = size_t(n) * size_t(n) * 4;
   GT_TRY(gt::ws_get(gt::WS_IN_A, bytes, &dd));
@@ -757,6 +758,7 @@ extern "C" int gt_distclust(const float *points, int64_t n, int64_t dim, int dis
   if (n < 2) return gt::fail(GT_EINVAL, "must have n >= 2 objects to cluster");
   if (!points) return gt::fail(GT_EINVAL, "null pointer");
   cudaStream_t s = gt::lib_stream();
+  gt::StreamSyncGuard guard(s);
   void *dp = nullptr, *dd = nullptr;
   const size_t pbytes = size_t(n) * size_t(dim) * 4, dbytes = size_t(n) * size_t(n) * 4;
   GT_TRY(gt::ws_get(gt::WS_IN_A, pbytes, &dp));
@@ -765,5 +767,8 @@ extern "C" int gt_distclust(const float *points, int64_t n, int64_t dim, int dis
   // the distance matrix never leaves the device (distanceLeaveOnGpu)
   GT_TRY(gt_distances_device(static_cast<float *>(dp), n, dim, static_cast<float *>(dd),
                              GT_LAYOUT_FULL, dist_method, 2.f, s));
+  bool failed = false;
+  GT_TRY(gt::device_error_check(s, &failed));
+  if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return gt_hclust_device(static_cast<float *>(dd), n, method, merge, order, height, s);
 }

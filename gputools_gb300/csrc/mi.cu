@@ -299,6 +299,7 @@ extern "C" int gt_mutual_info(int nbins, int order, int64_t n, const float *X, i
   if (nx == 0 || ny == 0) return GT_OK;
   if (!X || !Y || !out) return gt::fail(GT_EINVAL, "null host pointer");
   cudaStream_t s = gt::lib_stream();
+  gt::StreamSyncGuard guard(s);
   const size_t bx = size_t(nx) * size_t(n) * 4, by = size_t(ny) * size_t(n) * 4;
   const size_t bo = size_t(nx) * size_t(ny) * 4;
   const bool sym = X == Y && nx == ny;
@@ -316,5 +317,8 @@ extern "C" int gt_mutual_info(int nbins, int order, int64_t n, const float *X, i
                      static_cast<float *>(dout), s));
   GT_CUDA(cudaMemcpyAsync(out, dout, bo, cudaMemcpyDeviceToHost, s));
   GT_CUDA(cudaStreamSynchronize(s));
+  bool failed = false;
+  GT_TRY(gt::device_error_check(s, &failed));
+  if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
   return GT_OK;
 }

@@ -161,6 +161,7 @@ void rtestT(const float *pairs, const float *coeffs, const int *n, float *ts) {
   } else if (*n > 0) {
     const size_t b = size_t(*n) * 4;
     cudaStream_t s = gt::lib_stream();
+    gt::StreamSyncGuard guard(s);
     void *dp = nullptr, *dc = nullptr, *dt = nullptr;
     st = gt::ws_get(gt::WS_IN_A, b, &dp);
     if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, b, &dc);
@@ -192,6 +193,7 @@ void RgpuCorBackward(const float *X, const int *nobs, const int *nvar, const flo
     const int64_t n = *nobs, p = *nvar;
     const size_t bx = size_t(p) * size_t(n) * 4, bg = size_t(p) * size_t(p) * 4;
     cudaStream_t s = gt::lib_stream();
+    gt::StreamSyncGuard guard(s);
     void *dx = nullptr, *dg = nullptr, *dout = nullptr;
     st = gt::ws_get(gt::WS_IN_A, bx, &dx);
     if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bg, &dg);
@@ -221,6 +223,7 @@ void RgpuDistBackward(const float *points, const int *numPoints, const int *dim,
     const int64_t n = *numPoints, d = *dim;
     const size_t bx = size_t(n) * size_t(d) * 4, bg = size_t(n) * size_t(n) * 4;
     cudaStream_t s = gt::lib_stream();
+    gt::StreamSyncGuard guard(s);
     void *dx = nullptr, *dg = nullptr, *dout = nullptr;
     st = gt::ws_get(gt::WS_IN_A, bx, &dx);
     if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bg, &dg);
@@ -250,6 +253,7 @@ void RgpuMdsStress(const float *points, const int *numPoints, const int *dim, co
     const int64_t n = *numPoints, d = *dim;
     const size_t bx = size_t(n) * size_t(d) * 4, bd = size_t(n) * size_t(n - 1) / 2 * 4;
     cudaStream_t s = gt::lib_stream();
+    gt::StreamSyncGuard guard(s);
     void *dx = nullptr, *dd = nullptr, *dout = nullptr, *dl = nullptr;
     st = gt::ws_get(gt::WS_IN_A, bx, &dx);
     if (st == GT_OK) st = gt::ws_get(gt::WS_IN_B, bd > 0 ? bd : 4, &dd);

@@ -130,6 +130,41 @@ void *host_direct_ptr(void *host) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+HostOutput::~HostOutput() {
+  if (reg_) cudaHostUnregister(reg_);
+}
+
+void *HostOutput::map(void *host, size_t bytes) {
+  static int reg_enabled = -1;
+  if (reg_enabled < 0) {
+    const char *e = std::getenv("GT_REGISTER_HOST");
+    reg_enabled = (e && e[0] == '0') ? 0 : 1;
+  }
+  if (!host || bytes == 0) return nullptr;
+  if (void *d = host_direct_ptr(host)) return d;
+  // host_direct_ptr returned nothing: pageable (or writing in place disabled)
+  const char *e = std::getenv("GT_DIRECT_HOST");
+  if ((e && e[0] == '0') || !reg_enabled || bytes < kRegisterMin || reg_) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeUnregistered) return nullptr;
+  if (cudaHostRegister(host, bytes, cudaHostRegisterMapped) != cudaSuccess) {
+    cudaGetLastError();  // e.g. a page already registered: stage instead
+    return nullptr;
+  }
+  void *d = nullptr;
+  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
+    cudaGetLastError();
+    cudaHostUnregister(host);
+    return nullptr;
+  }
+  reg_ = host;
+  return d;
+}
+
 int sm_count() {
   int dev = 0;
   if (current_device(&dev) != GT_OK) return 148;
@@ -216,8 +251,8 @@ int device_error_check(cudaStream_t s, bool *failed) {
 uint64_t wait_limit_ns() { return g_wait_ns.load(); }
 
 uint32_t wait_sleep_hint_ns() {
-  const uint64_t w = g_wait_ns.load();
-  return w < 100000ull ? uint32_t(w) : 100000u;
+  // a suspending wait may outlast a short limit: below 1 ms the waits poll
+  return g_wait_ns.load() < 1000000ull ? 0u : 100000u;
 }
 
 void ws_release_all() {

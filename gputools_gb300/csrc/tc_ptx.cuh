@@ -69,11 +69,25 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
   return ok != 0;
 }
 
+// Non-blocking test of the phase (mbarrier.test_wait never suspends; a
+// try_wait may suspend until the phase completes, whatever its hint).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 constexpr uint32_t kSleepHintNs = 100000;  // 0.1 ms: well inside every wait limit
 
 // Bounded-wait settings of a launch: the device error word a CTA sets when
-// one of its waits gives up, the limit of each wait, and the sleep hint
-// (at most the limit, so that a short limit is honoured).
+// one of its waits gives up, the limit of each wait, and the sleep hint (0
+// for limits too short for a suspending wait: those waits poll).
 struct WaitCfg {
   int *err;
   uint64_t limit_ns;
@@ -85,6 +99,15 @@ struct WaitCfg {
 // never spins forever on a barrier that will not complete.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           uint64_t limit_ns, uint32_t hint_ns = kSleepHintNs) {
+  if (hint_ns == 0) {
+    // a short limit: poll without suspending, so that the limit holds
+    const uint64_t t0 = globaltimer_ns();
+    while (true) {
+      if (mbar_test_wait(bar, parity)) return true;
+      if (*abort) return false;
+      if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+  }
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   while (true) {

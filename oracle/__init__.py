@@ -14,8 +14,16 @@ Two back ends:
   from the reference tree by ``build_ref.sh`` (``distance_host`` in
   src/distance.cpp:174-207, ``hostKendall``/``permHostKendall`` in
   src/correlation.cpp:488-516, ``hostSignif`` in src/correlation.cpp:51-64).
-  It exists only where the reference tree is present; it pins the
-  restatement (tests/test_oracle.py) and generated tests/golden/.
+  It pins the restatement (tests/test_oracle.py) and generated
+  tests/golden/reference_cpu.npz; on the GPU hosts it is built from the
+  staged copy and timed as the reference's host loops.
+* ``baseline/_ref/libref_gpu.so`` -- the reference's own GPU path (host
+  orchestration in src/*.cpp, kernels in inst/cuda/*.cu) built by
+  ``build_ref_gpu.sh`` from a copy that ``stage_ref.sh`` places in the
+  git-ignored baseline/_ref/ (the GPU hosts receive it, the reference tree
+  itself is absent there).  tests/golden/make_golden_gpu.py runs it on a GPU
+  to record tests/golden/reference_gpu.npz, which pins the restatement of
+  Pearson, gpuMi and the clustering to what the reference itself returns.
 
 Parity pinning: the reference ships no tests or golden vectors, so the oracle
 is pinned (a) against the reference's own CPU loops (float32 arithmetic, so to
@@ -37,11 +45,33 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_cpu.so")
+STAGED = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "gputools")
+REF_GPU_LIB = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "libref_gpu.so")
 
 METHODS = ("euclidean", "maximum", "manhattan", "canberra", "binary", "minkowski")
 
 _lib = None
 _ref = None
+
+
+def reference_root(staged: bool = True) -> Optional[str]:
+    """Where the reference source tree is: $GPUTOOLS_REFERENCE, else the
+    ``reference_path`` recorded in the repository's benchmark spec, else (with
+    ``staged``) the copy stage_ref.sh left in baseline/_ref/gputools; None
+    when none of them exists."""
+    root = os.environ.get("GPUTOOLS_REFERENCE")
+    if not root:
+        try:
+            import json
+            with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
+                root = json.load(f).get("reference_path")
+        except (OSError, ValueError):
+            root = None
+    if root and os.path.isfile(os.path.join(root, "src", "correlation.cpp")):
+        return root
+    if staged and os.path.isfile(os.path.join(STAGED, "src", "correlation.cpp")):
+        return STAGED
+    return None
 
 
 def build(force: bool = False) -> str:
@@ -54,9 +84,16 @@ def build(force: bool = False) -> str:
             ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c11", "-Wall", "-ffp-contract=off",
              "-o", LIB, src, "-lm"])
     ref_script = os.path.join(HERE, "build_ref.sh")
-    if (force or not os.path.exists(REF_LIB)) and os.path.isdir(
-            os.environ.get("GPUTOOLS_REFERENCE", "/root/reference")):
-        subprocess.check_call(["bash", ref_script])
+    real = reference_root(staged=False)
+    if real and os.path.realpath(real) != os.path.realpath(STAGED):
+        # copy the hot path's sources where the GPU hosts receive them
+        subprocess.check_call(["bash", os.path.join(HERE, "stage_ref.sh"), real],
+                              stdout=subprocess.DEVNULL)
+    ref = reference_root()
+    if (force or not os.path.exists(REF_LIB)) and ref:
+        subprocess.check_call(["bash", ref_script], env=dict(os.environ, GPUTOOLS_REFERENCE=ref))
+    if (force or not os.path.exists(REF_GPU_LIB)) and os.path.isdir(STAGED):
+        subprocess.check_call(["bash", os.path.join(HERE, "build_ref_gpu.sh"), STAGED])
     return LIB
 
 
@@ -88,6 +125,95 @@ def _load():
 
 def ref_available() -> bool:
     return os.path.exists(REF_LIB)
+
+
+def ref_gpu_available() -> bool:
+    return os.path.exists(REF_GPU_LIB)
+
+
+_ref_gpu = None
+
+
+def _ref_gpu_lib():
+    """The reference's GPU path (needs a CUDA device to call)."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        if not ref_gpu_available():
+            raise RuntimeError("reference GPU build missing: run oracle/build_ref_gpu.sh on a "
+                               "host with the staged reference tree")
+        lib = ctypes.CDLL(REF_GPU_LIB)
+        sz, fp, ci = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int
+        lib.ref_pmcc.argtypes = [ci, fp, sz, fp, sz, sz, fp, fp, fp]
+        lib.ref_mi.argtypes = [ci, ci, ci, ci, fp, ci, fp, fp]
+        lib.ref_hcluster.argtypes = [fp, sz, ci, fp, fp, fp]
+        lib.ref_distance.argtypes = [fp, sz, sz, fp, ci, ctypes.c_float]
+        lib.ref_kendall.argtypes = [fp, sz, fp, sz, sz, fp]
+        _ref_gpu = lib
+    return _ref_gpu
+
+
+def _check_ref(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"reference {what} failed (CUDA error {rc})")
+
+
+def ref_gpu_pmcc(A: np.ndarray, B: np.ndarray, use: int = 0):
+    """The reference's pmcc() (src/correlation.cpp:66-161) on the GPU: A
+    (na, n), B (nb, n) variable-major, passed as two buffers as R's .C does.
+    Returns (corr, pairs, ts), float32 (na, nb)."""
+    A = np.ascontiguousarray(A, np.float32); B = np.ascontiguousarray(B, np.float32)
+    na, n = A.shape
+    nb = B.shape[0]
+    corr = np.empty((na, nb), np.float32); pairs = np.empty_like(corr); ts = np.empty_like(corr)
+    _check_ref(_ref_gpu_lib().ref_pmcc(int(use), _ptr(A), na, _ptr(B), nb, n, _ptr(pairs),
+                                       _ptr(corr), _ptr(ts)), "pmcc")
+    return corr, pairs, ts
+
+
+def ref_gpu_mi(X: np.ndarray, bins: int, order: int) -> np.ndarray:
+    """The reference's bSplineMutualInfo (src/mi.cpp:33-164) of X with itself
+    (the reference kernel get_mi is only in bounds for nx == ny).  X (nx, n)
+    variable-major; returns out[y, x] (nx, nx) float32."""
+    X = np.ascontiguousarray(X, np.float32)
+    nx, n = X.shape
+    out = np.empty((nx, nx), np.float32)
+    _check_ref(_ref_gpu_lib().ref_mi(int(bins), int(order), n, nx, _ptr(X), nx, _ptr(X),
+                                     _ptr(out)), "bSplineMutualInfo")
+    return out
+
+
+def ref_gpu_hcluster(D: np.ndarray, method: str):
+    """The reference's hcluster (src/hcluster.cpp:15-38) on the full n x n
+    float matrix D; returns the step list (sub, sup, heights)."""
+    D = np.ascontiguousarray(D, np.float32)
+    n = D.shape[0]
+    sub = np.empty(n - 1, np.int32); sup = np.empty(n - 1, np.int32)
+    val = np.empty(n - 1, np.float32)
+    code = _load().orc_hc_method(method.encode())
+    _check_ref(_ref_gpu_lib().ref_hcluster(_ptr(D), n, int(code), _ptr(sub), _ptr(sup),
+                                           _ptr(val)), "hcluster")
+    return sub, sup, val
+
+
+def ref_gpu_distance(P: np.ndarray, method: str, p: float = 2.0) -> np.ndarray:
+    """The reference's distance() (src/distance.cpp:259-316) of the rows of
+    P with themselves; returns the full (n, n) float32 matrix."""
+    P = np.ascontiguousarray(P, np.float32)
+    n, dim = P.shape
+    out = np.empty((n, n), np.float32)
+    _check_ref(_ref_gpu_lib().ref_distance(_ptr(P), n, dim, _ptr(out), method_index(method),
+                                           float(p)), "distance")
+    return out
+
+
+def ref_gpu_kendall(X: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """The reference's masterKendall (src/kendall.cpp:13-55): out[y, x]."""
+    X = np.ascontiguousarray(X, np.float32); Y = np.ascontiguousarray(Y, np.float32)
+    nx, n = X.shape
+    ny = Y.shape[0]
+    out = np.empty((ny, nx), np.float64)
+    _check_ref(_ref_gpu_lib().ref_kendall(_ptr(X), nx, _ptr(Y), ny, n, _ptr(out)), "kendall")
+    return out
 
 
 def _ref_lib():

@@ -4,13 +4,15 @@
 # from the read-only reference tree into oracle/_ref/libref_cpu.so.
 # Only builds where the reference tree exists (not on the GPU hosts); the
 # result is test infrastructure used to pin the oracle, never shipped.
+# The tree's location comes from GPUTOOLS_REFERENCE (oracle.build() sets it
+# from the benchmark's reference_path).
 set -euo pipefail
-REF=${GPUTOOLS_REFERENCE:-/root/reference}
+REF=${GPUTOOLS_REFERENCE:-}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 CUDA=${CUDA_HOME:-/usr/local/cuda}
-if [ ! -f "$REF/src/distance.cpp" ]; then
-  echo "reference tree not found at $REF; skipping oracle/_ref" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/src/distance.cpp" ]; then
+  echo "reference tree not found (GPUTOOLS_REFERENCE='$REF'); skipping oracle/_ref" >&2
   exit 0
 fi
 mkdir -p "$OUT"
