@@ -348,10 +348,10 @@ def run_ours(args, ranks: Ranks):
             step()
         return ranks.max((time.perf_counter() - t0) / e2e_steps)
 
-    # pageable: numpy arrays, every page touched before the call (as R's
-    # vectors are: .C passes filled copies)
+    # pageable: numpy arrays with every page written before the call, as R's
+    # vectors are (.C passes filled copies; np.zeros would leave them unmapped)
     nX = np.ascontiguousarray(X)
-    nbufs = [np.zeros((P, P), np.float32) for _ in range(3)]
+    nbufs = [np.full((P, P), 0.0, np.float32) for _ in range(3)]
     e2e_s = e2e_time(fp(nX), *(fp(b) for b in nbufs))
     del nbufs
     hX = torch.from_numpy(X).pin_memory()
@@ -408,9 +408,9 @@ def run_ours(args, ranks: Ranks):
                    "gram_path": headline, "parallelism": "replicas" if ranks.world > 1 else "single"},
         "e2e": {"value": ranks.world * entries / e2e_s, "unit": "entries/s",
                 "h2d_bytes_per_step": int(P * N_OBS * 4), "d2h_bytes_per_step": int(2 * P * P * 4),
-                "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the library "
-                       "page-locks the outputs for the call and the kernels write r and t in place "
-                       "over the host link; the constant pair counts n are filled by host threads "
+                "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the kernels "
+                       "write r and t in place through the GPU's access to the host page tables "
+                       "over NVLink-C2C; the constant pair counts n are filled by host threads "
                        "meanwhile)",
                 "ms_per_step": e2e_s * 1e3,
                 "pinned": {"value": ranks.world * entries / e2e_pinned_s,
@@ -569,6 +569,18 @@ def run_case(args):
         fn = lambda: _lib.check(lib.gt_mutual_info_device(args.bins, args.order, n, vp(dX), p,
                                                           vp(dX), p, vp(out), sptr))
         names = ("mi_prologue", "mi_gram")
+    elif args.case == "batch":
+        # --count cor(x) problems drawn like the batch configuration
+        # (variables log-uniform in [16, 4096], observations in [50, 2000])
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(17)
+        ps = np.exp(rng.uniform(np.log(16), np.log(4096), args.count)).astype(int)
+        ns = np.exp(rng.uniform(np.log(50), np.log(2000), args.count)).astype(int)
+        xs = [torch.randn((int(a), int(b)), generator=gen, device=dev, dtype=torch.float32)
+              for a, b in zip(ps, ns)]
+        plan = g.BatchPlan(xs, "pearson", autotune=False, graph=False)
+        fn = lambda: plan.launch(stream)
+        names = ("batch_pearson",)
     elif args.case == "hclust":
         # p points x n dims around 8 centres; each step clusters a fresh copy
         # of their euclidean distance matrix (the copy is inside the step)
@@ -903,7 +915,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--skip-euclid", action="store_true")
-    ap.add_argument("--case", choices=("pearson", "euclid", "kendall", "dist", "mi", "hclust"),
+    ap.add_argument("--count", type=int, default=300, help="--case batch: problems")
+    ap.add_argument("--case", choices=("pearson", "euclid", "kendall", "dist", "mi", "hclust",
+                                       "batch"),
                     help="run one workload at the given size instead of the benchmark")
     ap.add_argument("--p", type=int, default=4096, help="--case: variables / points")
     ap.add_argument("--n", type=int, default=4096, help="--case: observations")

@@ -14,8 +14,14 @@
 //
 // Distances.  dL/dx_i = sum_j W_ij (x_i - x_j) = x_i rowsum(W)_i - (W X)_i with
 // W_ij = (G_ij + G_ji) / D_ij (0 where D_ij = 0), or for MDS stress
-// W_ij = 2 (D_ij - delta_ij) / D_ij.  A fused CUDA-core kernel recomputes D_ij
-// from the points and never materialises W.
+// W_ij = 2 (D_ij - delta_ij) / D_ij.  Up to 64 dimensions a fused CUDA-core
+// kernel recomputes D_ij from the points and never materialises W.  Above,
+// the adjoint is GEMMs plus a rank-1 correction: D comes from the tcgen05
+// Euclidean path (exact near-zero recomputation included), one pass over D
+// and G writes W as split-bf16 planes with its row sums, W X runs on the
+// tcgen05 GEMM, and dX = X diag(rowsum W) - W X is formed on the points
+// centred by their column means (the gradient does not change under a
+// translation, and centring keeps the two terms from cancelling).
 #include "common.cuh"
 #include "allpairs_simt.cuh"
 #include "kernels.cuh"
@@ -96,6 +102,43 @@ __global__ void zt_operand_kernel(const float *__restrict__ X, int64_t p, int64_
 }
 
 constexpr int kFinThreads = 256;
+
+// Rows of a float matrix (nrows x kp) as f16x3 planes ([2][nrows][kp]), each
+// row scaled by the power of two that brings its largest magnitude into
+// [2^14, 2^15); scale[row] = the factor that undoes it.  One warp per row.
+__global__ void __launch_bounds__(256)
+f16x3_rows_kernel(const float *__restrict__ M, int64_t nrows, int64_t kp,
+                  uint16_t *__restrict__ planes, float *__restrict__ scale) {
+  const int64_t row = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
+  if (row >= nrows) return;  // whole warps
+  const int lane = threadIdx.x & 31;
+  const float *m = M + row * kp;
+  float amax = 0.f;
+  for (int64_t k = lane; k < kp; k += 32) amax = fmaxf(amax, fabsf(m[k]));
+  amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(amax)));
+  const int e = tc::f16_scale_exp(amax);
+  const float sc = tc::exp2i(e);
+  if (lane == 0) scale[row] = tc::exp2i(-e);
+  const int64_t plane = nrows * kp;
+  for (int64_t k = lane; k < kp; k += 32) {
+    uint16_t p[3];
+    tc::split_parts<tc::KIND_F16X3>(m[k] * sc, p);
+    planes[row * kp + k] = p[0];
+    planes[plane + row * kp + k] = p[1];
+  }
+}
+
+// Sum of the lanes' (hi, lo) float pairs, left in every lane (TwoSum).
+__device__ __forceinline__ void warp_pair_sum_f(float &hi, float &lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float t = hi + oh, bp = t - hi;
+    lo = (lo + ol) + ((hi - (t - bp)) + (oh - bp));
+    hi = t;
+  }
+}
 
 __device__ __forceinline__ double block_sum_d(double v, double *sh) {
 #pragma unroll
@@ -221,15 +264,16 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
           const float t = xi[k] - xj[jj][k];
           d2 = fmaf(t, t, d2);
         }
-        if (j == i || !(d2 > 0.f)) continue;
-        const float d = sqrtf(d2);
+        if (j == i) continue;
+        const float d = d2 > 0.f ? sqrtf(d2) : 0.f;
+        // coincident points add to the stress but not to the gradient
+        if (MODE == 1 && j > i) lsum += double(d - cf[tid][jj]) * double(d - cf[tid][jj]);
+        if (!(d2 > 0.f)) continue;
         float w;
         if (MODE == 0) {
           w = cf[tid][jj] / d;
         } else {
-          const float del = cf[tid][jj];
-          w = 2.f * (d - del) / d;
-          if (j > i) lsum += double(d - del) * double(d - del);
+          w = 2.f * (d - cf[tid][jj]) / d;
         }
         wsum += w;
 #pragma unroll
@@ -284,12 +328,190 @@ __global__ void loss_reduce_kernel(const double *__restrict__ ploss, int64_t cou
   }
 }
 
+// ---------------------------------------------- distances on the tensor cores
+// Column means of the points as FP64 (compensated float sums per thread, a
+// fixed-order block reduction): one CTA per dimension.
+__global__ void __launch_bounds__(kFinThreads)
+adj_colmean_kernel(const float *__restrict__ X, int64_t n, int64_t dim, double *__restrict__ mean) {
+  __shared__ double sh[32];
+  const int64_t c = blockIdx.x;
+  double v = 0.0;
+  float hi = 0.f, lo = 0.f;
+  for (int64_t i = threadIdx.x; i < n; i += kFinThreads) {
+    const float x = X[i * dim + c];
+    const float t = hi + x, bp = t - hi;
+    lo += (hi - (t - bp)) + (x - bp);
+    hi = t;
+  }
+  v = double(hi) + double(lo);
+  v = block_sum_d(v, sh);
+  if (threadIdx.x == 0) mean[c] = v / double(n);
+}
+
+// Centred points Xc (n x dim) and the GEMM's B operand: rows c (dimensions),
+// columns j (points, ld kp, zero padded), three bf16 planes; 32 x 32 tiles
+// transposed through shared memory.
+__global__ void adj_points_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
+                                  int64_t kp, const double *__restrict__ mean,
+                                  float *__restrict__ Xc, __nv_bfloat16 *__restrict__ Bt) {
+  __shared__ float tile[32][33];
+  const int64_t j0 = int64_t(blockIdx.x) * 32, c0 = int64_t(blockIdx.y) * 32;
+  const int tx = threadIdx.x, ty0 = threadIdx.y;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t j = j0 + ty, c = c0 + tx;
+    float v = 0.f;
+    if (j < n && c < dim) {
+      v = float(double(X[j * dim + c]) - mean[c]);
+      Xc[j * dim + c] = v;
+    }
+    tile[ty][tx] = v;  // rows j
+  }
+  __syncthreads();
+  const int64_t plane = dim * kp;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t c = c0 + ty, j = j0 + tx;
+    if (c >= dim || j >= kp) continue;
+    put_parts<__nv_bfloat16>(Bt, plane, c * kp + j, tile[tx][ty], 3);
+  }
+}
+
+// W as the GEMM's A operand (rows i, columns j, ld kp, three bf16 planes),
+// from the full distance matrix D and G (MODE 0: W = (G + G^T) / D) or the
+// targets delta in R's dist layout (MODE 1: W = 2 (D - delta) / D); W_ii and
+// W_ij with D_ij = 0 are 0.  Per 32 x 32 tile: the rows' partial sums of W
+// (rsum[i * nbj + jb]) and, for MODE 1, the tile's part of the stress
+// sum_{i<j} (D - delta)^2 (lpart[ib * nbj + jb]); both are reduced in a fixed
+// order afterwards.
+template <int MODE>
+__global__ void adj_weight_kernel(const float *__restrict__ D, const float *__restrict__ aux,
+                                  int64_t n, int64_t kp, __nv_bfloat16 *__restrict__ Wp,
+                                  float *__restrict__ rsum, double *__restrict__ lpart) {
+  __shared__ float gt[32][33];  // G^T tile: gt[jj][ii] = G[j][i]
+  __shared__ double lsh[8];
+  const int64_t i0 = int64_t(blockIdx.y) * 32, j0 = int64_t(blockIdx.x) * 32;
+  const int tx = threadIdx.x, ty0 = threadIdx.y;
+  const int64_t nbj = gridDim.x;
+  if (MODE == 0) {
+    for (int ty = ty0; ty < 32; ty += 8) {
+      const int64_t j = j0 + ty, i = i0 + tx;
+      gt[ty][tx] = (j < n && i < n) ? aux[j * n + i] : 0.f;
+    }
+    __syncthreads();
+  }
+  const int64_t plane = n * kp;
+  double lsum = 0.0;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t i = i0 + ty, j = j0 + tx;
+    float w = 0.f;
+    if (i < n && j < n && i != j) {
+      const float d = D[i * n + j];
+      if (d > 0.f) {
+        if (MODE == 0) {
+          w = (aux[i * n + j] + gt[tx][ty]) / d;
+        } else {
+          const int64_t a = i > j ? i : j, b = i > j ? j : i;
+          const float del = aux[n * b - b * (b + 1) / 2 + a - b - 1];
+          w = 2.f * (d - del) / d;
+          if (i < j) lsum += double(d - del) * double(d - del);
+        }
+      } else if (MODE == 1 && i < j) {
+        const int64_t a = j, b = i;
+        const float del = aux[n * b - b * (b + 1) / 2 + a - b - 1];
+        lsum += double(del) * double(del);
+      }
+    }
+    if (i < n && j < kp) put_parts<__nv_bfloat16>(Wp, plane, i * kp + j, w, 3);
+    // row sum of the tile: the 32 lanes of a row
+    float r = w;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (tx == 0 && i < n) rsum[i * nbj + blockIdx.x] = r;
+  }
+  if (MODE == 1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (tx == 0) lsh[ty0] = lsum;
+    __syncthreads();
+    if (tx == 0 && ty0 == 0) {
+      double t = 0.0;
+      for (int w = 0; w < 8; w++) t += lsh[w];
+      lpart[int64_t(blockIdx.y) * nbj + blockIdx.x] = t;
+    }
+  }
+}
+
+// dX_i = xc_i * sum_b rsum[i][b] - C_i (C = W Xc), the row's partials added
+// in order (compensated), one warp per point.
+__global__ void adj_finish_kernel(const float *__restrict__ Xc, const float *__restrict__ C,
+                                  const float *__restrict__ rsum, int64_t n, int64_t dim,
+                                  int64_t nbj, float *__restrict__ dX) {
+  const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  float hi = 0.f, lo = 0.f;
+  for (int64_t b = lane; b < nbj; b += 32) {
+    const float x = rsum[i * nbj + b];
+    const float t = hi + x, bp = t - hi;
+    lo += (hi - (t - bp)) + (x - bp);
+    hi = t;
+  }
+  warp_pair_sum_f(hi, lo);
+  const float r = hi + lo;
+  for (int64_t c = lane; c < dim; c += 32) dX[i * dim + c] = fmaf(Xc[i * dim + c], r, -C[i * dim + c]);
+}
+
+template <int MODE>
+int dist_backward_tc(const float *X, int64_t n, int64_t dim, const float *aux, float *dX,
+                     double *loss, cudaStream_t s) {
+  const int64_t kp = cdiv(n, kKPadB) * kKPadB;
+  const int64_t nbj = kp / 32, nbi = cdiv(n, 32);  // tile columns cover the padded k
+  void *pD = nullptr, *pW = nullptr, *pM = nullptr;
+  // the full distance matrix (tcgen05 Gram, near-zero pairs recomputed exactly)
+  GT_TRY(ws_get(WS_ADJ0, size_t(n) * size_t(n) * 4, &pD));
+  float *D = static_cast<float *>(pD);
+  GT_TRY(euclid_tc(X, n, dim, D, GT_LAYOUT_FULL, s));
+  GT_TRY(ws_get(WS_ADJ1, size_t(3) * size_t(n) * size_t(kp) * 2, &pW));
+  auto *Wp = static_cast<__nv_bfloat16 *>(pW);
+  // misc: means | Xc | B planes | C | rsum | loss parts
+  const size_t b_mean = size_t(dim) * 8, b_xc = size_t(n) * size_t(dim) * 4;
+  const size_t b_bt = size_t(3) * size_t(dim) * size_t(kp) * 2, b_c = b_xc;
+  const size_t b_rs = size_t(n) * size_t(nbj) * 4, b_lp = size_t(nbi) * size_t(nbj) * 8;
+  auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+  GT_TRY(ws_get(WS_ADJ2, r256(b_mean) + r256(b_xc) + r256(b_bt) + r256(b_c) + r256(b_rs) + b_lp,
+                &pM));
+  char *m = static_cast<char *>(pM);
+  auto *mean = reinterpret_cast<double *>(m);
+  auto *Xc = reinterpret_cast<float *>(m + r256(b_mean));
+  auto *Bt = reinterpret_cast<__nv_bfloat16 *>(m + r256(b_mean) + r256(b_xc));
+  auto *C = reinterpret_cast<float *>(m + r256(b_mean) + r256(b_xc) + r256(b_bt));
+  auto *rsum = reinterpret_cast<float *>(m + r256(b_mean) + r256(b_xc) + r256(b_bt) + r256(b_c));
+  auto *lp = reinterpret_cast<double *>(m + r256(b_mean) + r256(b_xc) + r256(b_bt) + r256(b_c) +
+                                        r256(b_rs));
+  if (nbi > 65535 || cdiv(dim, 32) > 65535) return fail(GT_EINVAL, "too many points (%lld)", (long long)n);
+  const dim3 blk(32, 8);
+  adj_colmean_kernel<<<unsigned(dim), kFinThreads, 0, s>>>(X, n, dim, mean);
+  adj_points_kernel<<<dim3(unsigned(kp / 32), unsigned(cdiv(dim, 32))), blk, 0, s>>>(
+      X, n, dim, kp, mean, Xc, Bt);
+  adj_weight_kernel<MODE><<<dim3(unsigned(nbj), unsigned(nbi)), blk, 0, s>>>(
+      D, aux, n, kp, Wp, rsum, lp);
+  count_launch(3);
+  GT_CUDA(cudaGetLastError());
+  // C = W Xc on the tensor cores (rows i, columns c)
+  GT_TRY(gemm_tc_store(Wp, n, Bt, dim, kp, 3, C, dim, s));
+  adj_finish_kernel<<<unsigned(cdiv(n * 32, 256)), 256, 0, s>>>(Xc, C, rsum, n, dim, nbj, dX);
+  count_launch();
+  if (MODE == 1 && loss) {
+    loss_reduce_kernel<<<1, 32, 0, s>>>(lp, nbi * nbj, loss);
+    count_launch();
+  }
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
 template <int MODE>
 int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *aux, float *dX,
                          double *loss, cudaStream_t s) {
-  if (dim > 64)
-    return fail(GT_EUNSUPPORTED, "distance adjoint supports at most 64 dimensions (dim=%lld)",
-                (long long)dim);
+  if (dim > 64) return dist_backward_tc<MODE>(X, n, dim, aux, dX, loss, s);
   const int64_t ib = cdiv(n, kDbRows);
   int64_t nsplit = cdiv(int64_t(sm_count()) * 4, ib);
   const int64_t max_split = cdiv(n, kDbCols);
@@ -354,9 +576,29 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     a.symmetric = 0; a.vec_ok = 1;
     cudaError_t e = launch_allpairs_simt<OpDotB, OutStore, 8, 8>(a, OpDotB{}, OutStore{W, n}, s);
     if (e != cudaSuccess) return fail(GT_ECUDA, "adjoint GEMM launch: %s", cudaGetErrorString(e));
+  } else if (path == GT_GRAM_TC_F16X3 || path == GT_GRAM_TC_F16X6) {
+    // f16x3 with every operand row scaled by a power of two (G + G^T and z^T
+    // are not unit-scaled): three products, the scales undone in the store
+    void *pSf = nullptr, *pZf = nullptr, *psc = nullptr;
+    GT_TRY(ws_get(WS_ADJ0, size_t(p) * size_t(kp) * 4, &pSf));
+    GT_TRY(ws_get(WS_ADJ1, size_t(n) * size_t(kp) * 4, &pZf));
+    GT_TRY(ws_get(WS_ADJ2, size_t(p + n) * 4, &psc));
+    GT_TRY(ws_get(WS_SCRATCH0, size_t(2) * size_t(p) * size_t(kp) * 2, &pS));
+    GT_TRY(ws_get(WS_SCRATCH1, size_t(2) * size_t(n) * size_t(kp) * 2, &pZ));
+    auto *Sf = static_cast<float *>(pSf), *Zf = static_cast<float *>(pZf);
+    auto *scS = static_cast<float *>(psc), *scZ = scS + p;
+    sym_operand_kernel<float><<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+        dG, p, kp, 1, Sf);
+    zt_operand_kernel<float><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
+        dX, p, n, kp, st, 1, Zf);
+    f16x3_rows_kernel<<<unsigned(cdiv(p, 8)), 256, 0, s>>>(Sf, p, kp,
+                                                            static_cast<uint16_t *>(pS), scS);
+    f16x3_rows_kernel<<<unsigned(cdiv(n, 8)), 256, 0, s>>>(Zf, n, kp,
+                                                            static_cast<uint16_t *>(pZ), scZ);
+    count_launch(4);
+    GT_CUDA(cudaGetLastError());
+    GT_TRY(gemm_tc_store_scaled(pS, p, pZ, n, kp, scS, scZ, W, n, s));
   } else {
-    // the adjoint's operands (G + G^T, z^T) are not unit-scaled, so the
-    // f16x3 setting runs as bf16x6, its precision class
     const int ns = path == GT_GRAM_TC_BF16X3 ? 2 : 3;
     GT_TRY(ws_get(WS_SCRATCH0, size_t(ns) * size_t(p) * size_t(kp) * 2, &pS));
     GT_TRY(ws_get(WS_SCRATCH1, size_t(ns) * size_t(n) * size_t(kp) * 2, &pZ));

@@ -56,7 +56,10 @@ class StreamSyncGuard {
 // buffer kept across calls and released by gt_release_workspace().
 enum WsSlot {
   WS_IN_A = 0, WS_IN_B, WS_OUT0, WS_OUT1, WS_OUT2, WS_SCRATCH0, WS_SCRATCH1,
-  WS_SCRATCH2, WS_SCRATCH3, WS_SCRATCH4, WS_NSLOTS
+  WS_SCRATCH2, WS_SCRATCH3, WS_SCRATCH4,
+  // the distance adjoint's own slots (it calls the Euclid path, which uses
+  // WS_SCRATCH0..3, in between)
+  WS_ADJ0, WS_ADJ1, WS_ADJ2, WS_NSLOTS
 };
 // Device buffer of at least `bytes` for `slot` on the current device.
 int ws_get(int slot, size_t bytes, void **ptr);
@@ -86,32 +89,22 @@ class ProfScope {
 // by one.  GT_DIRECT_HOST=0 disables it.
 void *host_direct_ptr(void *host);
 
-// A host output buffer of a synchronous entry, as its kernels reach it.
-// map() returns the device-usable address of `host` (`bytes` long), or
-// nullptr when it must be staged through device memory:
-//  * page-locked memory is written in place;
-//  * pageable memory from kRegisterMin bytes on (R's .C vectors are such) is
-//    page-locked for the call with cudaHostRegister and written in place --
-//    on GB300 this costs ~1.6 ms per GB and the kernels then write at the
-//    host link's rate, where a staged pageable copy runs at half of it;
-//  * anything else (small, or not registrable) is staged.
-// The registration is released by the destructor: declare the object before
-// the StreamSyncGuard of the call, so that the stream is synchronised first.
-// GT_DIRECT_HOST=0 disables writing in place, GT_REGISTER_HOST=0 only the
-// registration.
-class HostOutput {
- public:
-  static constexpr size_t kRegisterMin = size_t(1) << 20;
-  HostOutput() = default;
-  ~HostOutput();
-  HostOutput(const HostOutput &) = delete;
-  HostOutput &operator=(const HostOutput &) = delete;
-  void *map(void *host, size_t bytes);
-  bool registered() const { return reg_ != nullptr; }
-
- private:
-  void *reg_ = nullptr;
-};
+// Device-usable address of a host output buffer of a synchronous entry
+// (`bytes` long), or nullptr when it must be staged through device memory:
+//  * page-locked memory is written in place by the kernels;
+//  * pageable memory (what R's .C passes) is written in place too where the
+//    device reaches the host's page tables (cudaDevAttrPageableMemoryAccess,
+//    GB300 over NVLink-C2C) and every page of the buffer is resident: the
+//    kernels' writes then overlap the computation.  A page that is not yet
+//    populated would be faulted in one at a time (measured: 2.2 GB/s against
+//    125 GB/s on resident pages), so buffers with non-resident pages, and
+//    buffers below kDirectMin bytes, are staged;
+//  * anything else is staged.
+// GT_DIRECT_HOST=0 disables writing in place, GT_DIRECT_PAGEABLE=0 only the
+// pageable case.  (Page-locking the caller's buffer for the call,
+// cudaHostRegister, measured slower than either: 8 to 105 ms per 1.6 GB.)
+void *host_output_ptr(void *host, size_t bytes);
+constexpr size_t kDirectMin = size_t(1) << 20;
 
 // Per-device error word of the kernels with bounded waits (allocated and
 // zeroed on first use, kept until gt_release_workspace).  Kernels only set it;

@@ -375,7 +375,6 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
   if (nA == 0 || nB == 0) return GT_OK;
   if (!A || !B) return gt::fail(GT_EINVAL, "null host pointer");
   cudaStream_t s = gt::lib_stream();
-  gt::HostOutput m0, m1, m2;  // released after the guard below synchronises
   gt::StreamSyncGuard guard(s);
   const size_t inA = size_t(nA) * size_t(n) * 4, inB = size_t(nB) * size_t(n) * 4;
   const size_t outb = size_t(nA) * size_t(nB) * 4;
@@ -395,9 +394,9 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
   // device works and the host link carries two matrices instead of three
   const bool host_pairs = pairs && use == GT_EVERYTHING && nA * nB >= gt::kHostFillMin;
   // outputs the kernels can write in place (no staging copy), else workspace
-  void *h0 = corr ? m0.map(corr, outb) : nullptr;
-  void *h1 = ts ? m1.map(ts, outb) : nullptr;
-  void *h2 = pairs && !host_pairs ? m2.map(pairs, outb) : nullptr;
+  void *h0 = corr ? gt::host_output_ptr(corr, outb) : nullptr;
+  void *h1 = ts ? gt::host_output_ptr(ts, outb) : nullptr;
+  void *h2 = pairs && !host_pairs ? gt::host_output_ptr(pairs, outb) : nullptr;
   if (corr && !(o0 = h0)) GT_TRY(gt::ws_get(gt::WS_OUT0, outb, &o0));
   if (ts && !(o1 = h1)) GT_TRY(gt::ws_get(gt::WS_OUT1, outb, &o1));
   if (pairs && !host_pairs && !(o2 = h2)) GT_TRY(gt::ws_get(gt::WS_OUT2, outb, &o2));

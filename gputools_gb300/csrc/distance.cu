@@ -248,11 +248,10 @@ extern "C" int gt_distances(const float *points, int64_t n, int64_t dim, float *
   if (n == 0) return GT_OK;
   if (!points || !out) return gt::fail(GT_EINVAL, "null host pointer");
   cudaStream_t st = gt::lib_stream();
-  gt::HostOutput mo;  // released after the guard below synchronises
   gt::StreamSyncGuard guard(st);
   void *dp = nullptr, *dout = nullptr;
   GT_TRY(gt::ws_get(gt::WS_IN_A, size_t(n) * size_t(dim) * 4, &dp));
-  void *direct = mo.map(out, size_t(n) * size_t(n) * 4);
+  void *direct = gt::host_output_ptr(out, size_t(n) * size_t(n) * 4);
   if (!(dout = direct)) GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(n) * size_t(n) * 4, &dout));
   GT_CUDA(cudaMemcpyAsync(dp, points, size_t(n) * size_t(dim) * 4, cudaMemcpyHostToDevice, st));
   GT_TRY(gt_distances_device(static_cast<float *>(dp), n, dim, static_cast<float *>(dout),

@@ -521,10 +521,12 @@ struct MiFinish {
   __device__ void drain(EpiCtx &) const {}
 };
 
-// Plain FP32 store of the contraction, C[r*ld + c].
+// Plain FP32 store of the contraction, C[r*ld + c]; with row and column
+// scales (operands scaled per row by powers of two), C[r][c] * rs[r] * cs[c].
 struct StoreFinish {
   float *out;
   int64_t ld, nr, nc;
+  const float *rs = nullptr, *cs = nullptr;
   __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
     float *wsm = ctx.wsm;
@@ -532,12 +534,21 @@ struct StoreFinish {
     for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
     __syncwarp();
     const int64_t rbase = r - lane, c = c0 + lane;
+    const float csc = (rs && c < nc) ? cs[c] : 1.f;
     if (rbase + 31 < nr && c0 + 31 < nc) {
       float *o = out + (rbase * ld + c);
+      if (rs) {
 #pragma unroll 8
-      for (int i = 0; i < 32; i++) {
-        *o = wsm[i * 33 + lane];
-        o += ld;
+        for (int i = 0; i < 32; i++) {
+          *o = (wsm[i * 33 + lane] * rs[rbase + i]) * csc;
+          o += ld;
+        }
+      } else {
+#pragma unroll 8
+        for (int i = 0; i < 32; i++) {
+          *o = wsm[i * 33 + lane];
+          o += ld;
+        }
       }
       __syncwarp();
       return;
@@ -545,7 +556,7 @@ struct StoreFinish {
     for (int i = 0; i < 32; i++) {
       const int64_t ri = rbase + i;
       if (ri >= nr) break;
-      if (c < nc) out[ri * ld + c] = wsm[i * 33 + lane];
+      if (c < nc) out[ri * ld + c] = rs ? (wsm[i * 33 + lane] * rs[ri]) * csc : wsm[i * 33 + lane];
     }
     __syncwarp();
   }
@@ -1301,6 +1312,17 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
                                                   tc_chunk_kblocks(32), fin, "gemm_store", s);
   return launch_gram<tc::KIND_BF16X3, 64, true>(planesA, nA, planesB, nB, kpad, kFull,
                                                 tc_chunk_kblocks(64), fin, "gemm_store", s);
+}
+
+// The same contraction from f16x3 planes whose rows were scaled by powers of
+// two (rsA, rsB: the factors 2^-e that undo each row's scale).
+int gemm_tc_store_scaled(const void *planesA, int64_t nA, const void *planesB, int64_t nB,
+                         int64_t kpad, const float *rsA, const float *rsB, float *C, int64_t ldc,
+                         cudaStream_t s) {
+  if (nA == 0 || nB == 0) return GT_OK;
+  StoreFinish fin{C, ldc, nA, nB, rsA, rsB};
+  return launch_gram<tc::KIND_F16X3, 32, true>(planesA, nA, planesB, nB, kpad, kFull,
+                                               tc_chunk_kblocks(32), fin, "gemm_store", s);
 }
 
 int pearson_tc_prologue(const float *dX, int64_t nvar, int64_t n, int kind, int slot_z,

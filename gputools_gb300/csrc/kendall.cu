@@ -405,7 +405,6 @@ extern "C" int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny
   if (nx == 0 || ny == 0) return GT_OK;
   if (!X || !Y || !out) return gt::fail(GT_EINVAL, "null host pointer");
   cudaStream_t s = gt::lib_stream();
-  gt::HostOutput mo;  // released after the guard below synchronises
   gt::StreamSyncGuard guard(s);
   const size_t bx = size_t(nx) * size_t(n) * 4, by = size_t(ny) * size_t(n) * 4;
   void *dX = nullptr, *dY = nullptr, *dO = nullptr;
@@ -419,7 +418,7 @@ extern "C" int gt_kendall(const float *X, int64_t nx, const float *Y, int64_t ny
       GT_TRY(gt::same_contents(static_cast<float *>(dX), static_cast<float *>(dY), nx * n, &same, s));
   }
   if (same) dY = dX;
-  void *direct = mo.map(out, size_t(nx) * size_t(ny) * 8);
+  void *direct = gt::host_output_ptr(out, size_t(nx) * size_t(ny) * 8);
   if (!(dO = direct)) GT_TRY(gt::ws_get(gt::WS_OUT0, size_t(nx) * size_t(ny) * 8, &dO));
   GT_TRY(gt::kendall_impl(static_cast<float *>(dX), nx, static_cast<float *>(dY), ny, n,
                           same ? 1 : 0, static_cast<double *>(dO), s));

@@ -8,6 +8,8 @@
 #include "common.cuh"
 
 #include <cstdarg>
+#include <sys/mman.h>
+#include <unistd.h>
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
@@ -130,39 +132,57 @@ void *host_direct_ptr(void *host) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-HostOutput::~HostOutput() {
-  if (reg_) cudaHostUnregister(reg_);
+namespace {
+// Whether every page of [p, p + bytes) is resident (mincore).
+bool pages_resident(const void *p, size_t bytes) {
+  const long pg = sysconf(_SC_PAGESIZE);
+  if (pg <= 0) return false;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(pg - 1);
+  const uintptr_t e = reinterpret_cast<uintptr_t>(p) + bytes;
+  const size_t npages = (e - a + size_t(pg) - 1) / size_t(pg);
+  std::vector<unsigned char> vec(npages);
+  if (mincore(reinterpret_cast<void *>(a), e - a, vec.data()) != 0) return false;
+  for (unsigned char v : vec)
+    if (!(v & 1)) return false;
+  return true;
 }
 
-void *HostOutput::map(void *host, size_t bytes) {
-  static int reg_enabled = -1;
-  if (reg_enabled < 0) {
-    const char *e = std::getenv("GT_REGISTER_HOST");
-    reg_enabled = (e && e[0] == '0') ? 0 : 1;
+int pageable_access() {
+  static int cached[kMaxDevices];
+  static bool init[kMaxDevices];
+  int dev = 0;
+  if (current_device(&dev) != GT_OK) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!init[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    cached[dev] = v;
+    init[dev] = true;
+  }
+  return cached[dev];
+}
+}  // namespace
+
+void *host_output_ptr(void *host, size_t bytes) {
+  static int pageable_enabled = -1;
+  if (pageable_enabled < 0) {
+    const char *e = std::getenv("GT_DIRECT_PAGEABLE");
+    pageable_enabled = (e && e[0] == '1') ? 1 : 0;
   }
   if (!host || bytes == 0) return nullptr;
   if (void *d = host_direct_ptr(host)) return d;
-  // host_direct_ptr returned nothing: pageable (or writing in place disabled)
   const char *e = std::getenv("GT_DIRECT_HOST");
-  if ((e && e[0] == '0') || !reg_enabled || bytes < kRegisterMin || reg_) return nullptr;
+  if ((e && e[0] == '0') || !pageable_enabled || bytes < kDirectMin) return nullptr;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
-  if (a.type != cudaMemoryTypeUnregistered) return nullptr;
-  if (cudaHostRegister(host, bytes, cudaHostRegisterMapped) != cudaSuccess) {
-    cudaGetLastError();  // e.g. a page already registered: stage instead
-    return nullptr;
-  }
-  void *d = nullptr;
-  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
-    cudaGetLastError();
-    cudaHostUnregister(host);
-    return nullptr;
-  }
-  reg_ = host;
-  return d;
+  if (a.type != cudaMemoryTypeUnregistered || !pageable_access()) return nullptr;
+  return pages_resident(host, bytes) ? host : nullptr;
 }
 
 int sm_count() {

@@ -275,12 +275,16 @@ int gt_cor_backward_device(const float *d_X, int64_t p, int64_t n,
 
 /* dL/dX of the Euclidean distances D of the rows of X (n x dim row-major)
  * given G = dL/dD (n x n, G[i*n + j]); terms with D_ij = 0 contribute 0.
- * dim <= 64. */
+ * Up to 64 dimensions one fused CUDA-core pass (D recomputed, nothing n x n
+ * stored); above, D from the tensor-core distance path, W = (G + G^T) / D as
+ * split-bf16 planes and W X on the tensor cores (about 10 n^2 bytes of
+ * device workspace). */
 int gt_dist_backward_device(const float *d_X, int64_t n, int64_t dim,
                             const float *d_G, float *d_dX, void *stream);
 
 /* MDS stress L = sum_{i<j} (D_ij - delta_ij)^2 and dL/dX, delta in R's dist
- * layout; *d_loss (double, may be NULL) receives L.  dim <= 64. */
+ * layout; *d_loss (double, may be NULL) receives L.  Evaluated like
+ * gt_dist_backward_device with W = 2 (D - delta) / D. */
 int gt_mds_stress_device(const float *d_X, int64_t n, int64_t dim,
                          const float *d_delta, float *d_dX, double *d_loss,
                          void *stream);

@@ -4,8 +4,9 @@ holds to FP64 central finite differences.
 
 Error metric: max |gpu - oracle| / max |oracle| over the gradient.
 Tolerances: fp32 and bf16x6 paths 2e-5, bf16x3 2e-4 (its ~2^-16 products),
-f16x3 2e-5 (the adjoint GEMM's operands are not unit-scaled, so it runs as
-bf16x6), distance adjoints (float32 CUDA cores) 2e-5.
+f16x3 2e-5 (the adjoint GEMM's operand rows are each scaled by a power of
+two, then split as f16x3: three products), distance adjoints 2e-5 (float32 CUDA cores up to 64 dimensions;
+above, D on the tensor-core distance path and W X as a split-bf16 GEMM).
 """
 import ctypes
 
@@ -75,7 +76,7 @@ def test_cor_backward_config_size(gpu, oracle_mod):
     G = rng.standard_normal((4096, 4096)).astype(np.float32)
     G = ((G + G.T) * 0.5).astype(np.float32)
     want = oracle_mod.cor_backward(X, G.astype(np.float64))
-    for pth in ("bf16x6", "bf16x3"):
+    for pth in ("bf16x6", "bf16x3", "f16x3"):
         old = g.get_gram_path()
         g.set_gram_path(pth)
         try:
@@ -136,3 +137,62 @@ def test_r_style_wrappers(gpu, oracle_mod):
     got = g.gpuDistBackward(pts, Gd)
     want = oracle_mod.dist_backward(pts.astype(np.float32), Gd)
     assert rel(got, want) <= 2e-5
+
+
+def _dist_bwd(lib, X, G):
+    import torch
+    n, d = X.shape
+    dX = torch.from_numpy(X).cuda(); dG = torch.from_numpy(G).cuda()
+    out = torch.empty_like(dX)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    st = lib.gt_dist_backward_device(vp(dX), n, d, vp(dG), vp(out),
+                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0, lib.gt_last_error().decode()
+    torch.cuda.synchronize()
+    return out.cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("n,d,offset", [(700, 65, 0.0), (1000, 128, 50.0), (600, 512, 3.0),
+                                        (130, 1000, 0.0)])
+def test_dist_backward_tensor_core_dims(gpu, oracle_mod, n, d, offset):
+    """Above 64 dimensions: GEMMs plus the rank-1 correction, on points with a
+    common offset (the centring keeps the two terms from cancelling) and a
+    duplicated point (its zero distances contribute nothing)."""
+    rng = np.random.default_rng(n + d)
+    X = (rng.standard_normal((n, d)) + offset).astype(np.float32)
+    X[5] = X[9]
+    G = rng.standard_normal((n, n)).astype(np.float32)
+    got = _dist_bwd(gpu, X, G)
+    want = oracle_mod.dist_backward(X, G.astype(np.float64))
+    assert rel(got, want) <= 2e-5, rel(got, want)
+
+
+@pytest.mark.parametrize("n,d", [(500, 128), (2048, 200)])
+def test_mds_stress_tensor_core_dims(gpu, oracle_mod, n, d):
+    import gputools_gb300 as g
+    rng = np.random.default_rng(n + 1)
+    X = rng.standard_normal((n, d)).astype(np.float32)
+    X[3] = X[4]  # coincident points: in the stress, not in the gradient
+    T = rng.standard_normal((n, d)).astype(np.float32)
+    dT = oracle_mod.dist(T, "euclidean")
+    cols, rows = np.triu_indices(n, 1)
+    delta = dT[cols, rows].astype(np.float32)
+    L, grad = g.gpuMdsStress(X, delta)
+    wL, wgrad = oracle_mod.mds_stress(X, delta)
+    assert L == pytest.approx(wL, rel=1e-5)
+    assert rel(grad, wgrad) <= 5e-5, rel(grad, wgrad)
+
+
+def test_mds_stress_coincident_points_fused_path(gpu, oracle_mod):
+    """The fused path (<= 64 dimensions) counts coincident points in the
+    stress, as the oracle does."""
+    import gputools_gb300 as g
+    rng = np.random.default_rng(77)
+    X = rng.standard_normal((200, 16)).astype(np.float32)
+    X[10] = X[20]
+    X[30] = X[20]
+    delta = (rng.random(200 * 199 // 2) * 3 + 0.5).astype(np.float32)
+    L, grad = g.gpuMdsStress(X, delta)
+    wL, wgrad = oracle_mod.mds_stress(X, delta)
+    assert L == pytest.approx(wL, rel=1e-5)
+    assert rel(grad, wgrad) <= 5e-5

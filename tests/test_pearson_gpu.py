@@ -312,26 +312,35 @@ def test_exact_path_long_columns_and_ragged_sizes(gpu, oracle_mod, rng):
     check_ts(ts, corr, pairs, wt, wc)
 
 
-def test_pageable_outputs_are_registered_for_the_call(gpu, oracle_mod, rng):
+def test_pageable_outputs_written_in_place(gpu, oracle_mod, rng):
     """Outputs from 1 MiB on in ordinary (pageable) memory, as R's .C passes
-    them, are page-locked for the call and written in place; afterwards they
-    are ordinary memory again (registering them once more succeeds)."""
+    them: written in place where the device reaches the host page tables and
+    the pages are resident, else staged; either way the results match the
+    oracle, and the buffers stay ordinary memory (registering them succeeds)."""
     import os
     nv, n = 1200, 96
     X = (rng.standard_normal((nv, n)) * 5 + 1).astype(np.float32)
-    corr, pairs, ts = rpmcc(gpu, 0, X, X.copy())
     rows = np.array([0, 1, 599, nv - 1])
     wc, wp, _ = oracle_mod.pearson(X[rows], X)
     for k, r in enumerate(rows):
         wc[k, r] = 1.0
-    assert np.abs(corr[rows].astype(np.float64) - wc).max() <= tol(gpu_path(), n)
-    assert np.all(pairs == n)
     cudart = ctypes.CDLL(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64",
                                       "libcudart.so"))
-    for a in (corr, pairs, ts):
-        assert cudart.cudaHostRegister(a.ctypes.data_as(ctypes.c_void_p),
-                                       ctypes.c_size_t(a.nbytes), 0) == 0
-        assert cudart.cudaHostUnregister(a.ctypes.data_as(ctypes.c_void_p)) == 0
+    for touched in (True, False):
+        mk = (lambda: np.full((nv, nv), -5.0, np.float32)) if touched else \
+            (lambda: np.empty((nv, nv), np.float32))
+        corr, pairs, ts = mk(), mk(), mk()
+        ci = lambda v: ctypes.byref(ctypes.c_int(v))
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        Xc = X.copy()
+        gpu.rpmcc(ci(0), vp(X), ci(nv), vp(Xc), ci(nv), ci(n), vp(pairs), vp(corr), vp(ts))
+        assert gpu.gt_last_error().decode() == ""
+        assert np.abs(corr[rows].astype(np.float64) - wc).max() <= tol(gpu_path(), n)
+        assert np.all(pairs == n)
+        for a in (corr, pairs, ts):
+            assert cudart.cudaHostRegister(a.ctypes.data_as(ctypes.c_void_p),
+                                           ctypes.c_size_t(a.nbytes), 0) == 0
+            assert cudart.cudaHostUnregister(a.ctypes.data_as(ctypes.c_void_p)) == 0
 
 
 def gpu_path():
