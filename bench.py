@@ -408,10 +408,11 @@ def run_ours(args, ranks: Ranks):
                    "gram_path": headline, "parallelism": "replicas" if ranks.world > 1 else "single"},
         "e2e": {"value": ranks.world * entries / e2e_s, "unit": "entries/s",
                 "h2d_bytes_per_step": int(P * N_OBS * 4), "d2h_bytes_per_step": int(2 * P * P * 4),
-                "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the kernels "
-                       "write r and t in place through the GPU's access to the host page tables "
-                       "over NVLink-C2C; the constant pair counts n are filled by host threads "
-                       "meanwhile)",
+                "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the Gram "
+                       "runs in 16 bands of rows; the kernels write r and t into page-locked "
+                       "staging over the host link and host threads copy each finished band "
+                       "into the caller's buffers while the next band runs; the constant pair "
+                       "counts n are filled by the same threads)",
                 "ms_per_step": e2e_s * 1e3,
                 "pinned": {"value": ranks.world * entries / e2e_pinned_s,
                            "ms_per_step": e2e_pinned_s * 1e3}},

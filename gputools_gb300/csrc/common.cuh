@@ -59,11 +59,16 @@ enum WsSlot {
   WS_SCRATCH2, WS_SCRATCH3, WS_SCRATCH4,
   // the distance adjoint's own slots (it calls the Euclid path, which uses
   // WS_SCRATCH0..3, in between)
-  WS_ADJ0, WS_ADJ1, WS_ADJ2, WS_NSLOTS
+  WS_ADJ0, WS_ADJ1, WS_ADJ2,
+  WS_TILES,  // tile tables of banded launches
+  WS_NSLOTS
 };
 // Device buffer of at least `bytes` for `slot` on the current device.
 int ws_get(int slot, size_t bytes, void **ptr);
 void ws_release_all();
+// Page-locked host buffer of at least `bytes` for the current device
+// (grow-only, kept across calls, released with the device workspace).
+int host_ws_get(size_t bytes, void **ptr);
 
 // Counts kernel launches (gt_kernel_launches); call once per launch.
 void count_launch(int n = 1);

@@ -26,7 +26,9 @@
 #include "stats.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -368,6 +370,107 @@ void host_fill(float *out, int64_t count, float v) {
 }  // namespace
 }  // namespace gt
 
+namespace gt {
+namespace {
+
+// Outputs from this size on (bytes per matrix; 64 MB) that the kernels cannot
+// write in place (pageable memory, as R's .C passes) go through the banded
+// pipeline below when the Gram path supports it.
+constexpr size_t kBandMinBytes = size_t(64) << 20;
+constexpr int kBands = 16;
+
+// "everything" Pearson into host outputs the kernels cannot write in place
+// (pageable memory): the Gram runs in kBands bands of rows
+// (pearson_band_tiles; once band b has run, its rows are complete, mirror
+// entries included) into device workspace, and each band's rows go to the
+// caller's buffers by a device-to-host copy on a second stream as soon as the
+// band's event completes, while the device computes the next bands.  The copy
+// of a whole matrix after the computation (measured at 4096 x 20000, f16x6:
+// 31 ms per call) then overlaps it instead; the constant pair counts are
+// filled by host threads meanwhile.  (Kernels writing page-locked staging
+// with host threads copying it out measured slower, 41 ms: the host copies
+// and the fill share the host's memory bandwidth and cores.)
+int pmcc_banded(const float *dA, int64_t nA, const float *dB, int64_t nB, int64_t n, int sym,
+                int path, float *pairs, float *corr, float *ts, cudaStream_t s) {
+  const size_t outb = size_t(nA) * size_t(nB) * 4;
+  float *c_dev = corr ? static_cast<float *>(host_direct_ptr(corr)) : nullptr;
+  float *t_dev = ts ? static_cast<float *>(host_direct_ptr(ts)) : nullptr;
+  const bool stage_c = corr && !c_dev, stage_t = ts && !t_dev;
+  void *o0 = nullptr, *o1 = nullptr;
+  if (stage_c) GT_TRY(ws_get(WS_OUT0, outb, &o0));
+  if (stage_t) GT_TRY(ws_get(WS_OUT1, outb, &o1));
+  if (stage_c) c_dev = static_cast<float *>(o0);
+  if (stage_t) t_dev = static_cast<float *>(o1);
+  // operand planes, then the bands
+  void *zA = nullptr, *zB = nullptr;
+  int64_t kpad = 0;
+  GT_TRY(pearson_tc_prologue(dA, nA, n, path, WS_SCRATCH0, WS_SCRATCH2, &zA, &kpad, s));
+  if (sym) zB = zA;
+  else GT_TRY(pearson_tc_prologue(dB, nB, n, path, WS_SCRATCH1, WS_SCRATCH3, &zB, &kpad, s));
+  const int64_t tr = cdiv(nA, kGramRows);
+  const int64_t band_blocks = cdiv(tr, kBands);
+  std::vector<int2> tiles;
+  std::vector<int64_t> off;
+  pearson_band_tiles(nA, nB, sym != 0, band_blocks, tiles, off);
+  const int64_t nbands = int64_t(off.size()) - 1;
+  void *dt = nullptr;
+  GT_TRY(ws_get(WS_TILES, tiles.size() * sizeof(int2), &dt));
+  GT_CUDA(cudaMemcpyAsync(dt, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  struct Resources {
+    std::vector<cudaEvent_t> ev;
+    cudaStream_t cs = nullptr;
+    ~Resources() {
+      if (cs) {
+        cudaStreamSynchronize(cs);
+        cudaStreamDestroy(cs);
+      }
+      for (auto x : ev)
+        if (x) cudaEventDestroy(x);
+    }
+  } res;
+  res.ev.assign(size_t(nbands), nullptr);
+  for (auto &e : res.ev) GT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  GT_CUDA(cudaStreamCreateWithFlags(&res.cs, cudaStreamNonBlocking));
+  PearsonOut po{c_dev, t_dev, nullptr, nB, float(n), sym};
+  for (int64_t b = 0; b < nbands; b++) {
+    GT_TRY(pearson_tc_band(zA, nA, zB, nB, kpad, path, po, static_cast<const int2 *>(dt) + off[b],
+                           off[b + 1] - off[b], s));
+    GT_CUDA(cudaEventRecord(res.ev[size_t(b)], s));
+  }
+  // the pair counts on host threads while the bands run and are copied
+  std::thread filler;
+  bool filler_started = false;
+  if (pairs) {
+    try {
+      filler = std::thread([=] { host_fill(pairs, nA * nB, float(n)); });
+      filler_started = true;
+    } catch (...) {
+    }
+  }
+  const int64_t rows_per_band = band_blocks * kGramRows;
+  int st = GT_OK;
+  for (int64_t b = 0; b < nbands && st == GT_OK; b++) {
+    const int64_t r0 = b * rows_per_band, r1 = std::min(nA, r0 + rows_per_band);
+    const size_t e0 = size_t(r0) * size_t(nB), bytes = size_t(r1 - r0) * size_t(nB) * 4;
+    cudaError_t e = cudaStreamWaitEvent(res.cs, res.ev[size_t(b)], 0);
+    if (e == cudaSuccess && stage_c)
+      e = cudaMemcpyAsync(corr + e0, c_dev + e0, bytes, cudaMemcpyDeviceToHost, res.cs);
+    if (e == cudaSuccess && stage_t)
+      e = cudaMemcpyAsync(ts + e0, t_dev + e0, bytes, cudaMemcpyDeviceToHost, res.cs);
+    if (e != cudaSuccess) st = fail(GT_ECUDA, "banded Pearson copy: %s", cudaGetErrorString(e));
+  }
+  if (st == GT_OK) {
+    cudaError_t e = cudaStreamSynchronize(res.cs);
+    if (e != cudaSuccess) st = fail(GT_ECUDA, "banded Pearson copy: %s", cudaGetErrorString(e));
+  }
+  if (filler_started) filler.join();
+  else if (pairs) host_fill(pairs, nA * nB, float(n));
+  return st;
+}
+
+}  // namespace
+}  // namespace gt
+
 extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int64_t nB, int64_t n,
                        float *pairs, float *corr, float *ts) {
   gt::clear_error();
@@ -389,6 +492,18 @@ extern "C" int gt_pmcc(int use, const float *A, int64_t nA, const float *B, int6
       GT_TRY(gt::same_contents(static_cast<float *>(dA), static_cast<float *>(dB), nA * n, &sym, s));
   }
   if (sym) dB = dA;
+  const int path = gt_get_gram_path();
+  if (use == GT_EVERYTHING && n > 0 && outb >= gt::kBandMinBytes &&
+      (path == GT_GRAM_TC_F16X3 || path == GT_GRAM_TC_F16X6) &&
+      ((corr && !gt::host_direct_ptr(corr)) || (ts && !gt::host_direct_ptr(ts)))) {
+    GT_TRY(gt::pmcc_banded(static_cast<float *>(dA), nA, static_cast<float *>(dB), nB, n,
+                           sym ? 1 : 0, path, pairs, corr, ts, s));
+    GT_CUDA(cudaStreamSynchronize(s));
+    bool failed = false;
+    GT_TRY(gt::device_error_check(s, &failed));
+    if (failed) return gt::fail(GT_ETIMEOUT, "a tensor-core kernel wait timed out");
+    return GT_OK;
+  }
   // "everything": every pair count is n (src/correlation.cpp:66-161 counts
   // all observations), so for large outputs the host fills `pairs` while the
   // device works and the host link carries two matrices instead of three

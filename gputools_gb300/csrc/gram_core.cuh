@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdint>
 #include <type_traits>
+#include <vector>
 
 namespace gt {
 
@@ -333,6 +334,63 @@ struct SingleWork {
     tc::prefetch_tensormap(&mb);
   }
 };
+
+// One problem whose tiles come from a table of (row0, col0) built on the host
+// (a band of rows at a time, in the order the table lists them); the cursor
+// looks each entry up a tile ahead.
+template <class Fin>
+struct TableWork {
+  CUtensorMap ma, mb;
+  const int2 *tiles;
+  int64_t ntiles;
+  int64_t nk;
+  Fin fin;
+  __device__ bool tile(int64_t cursor, TileRef &ref) const {
+    const int64_t u = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
+    if (u >= ntiles) return false;
+    const int2 t = tiles[u];
+    ref.row0 = t.x;
+    ref.col0 = t.y;
+    ref.ma = &ma;
+    ref.mb = &mb;
+    ref.nk = nk;
+    ref.prob = 0;
+    return true;
+  }
+  static constexpr bool kPrefetch = true;
+  __device__ bool skip() const {
+    if constexpr (std::is_same<Fin, PearsonFinish>::value) return fin.skip();
+    return false;
+  }
+  __device__ const Fin &finish(const TileRef &) const { return fin; }
+  __device__ void drain(EpiCtx &ctx) const { fin.drain(ctx); }
+  __device__ void prefetch() const {
+    tc::prefetch_tensormap(&ma);
+    tc::prefetch_tensormap(&mb);
+  }
+};
+
+// The tiles (128 x 256) of a Pearson problem grouped in bands of row blocks:
+// band b holds the tiles whose row block lies in [b * band_blocks,
+// (b + 1) * band_blocks); for a symmetric problem only those meeting the
+// upper triangle (row block ti <= 2 tj + 1).  Within a band, column block by
+// column block.  After the bands 0 .. b have run, every row of band b is
+// complete, mirror entries included (an entry (r, c), r <= c, is written by
+// the tile of row r's block).  offsets[b] .. offsets[b + 1] index band b.
+inline void band_tiles(int64_t nr, int64_t nc, bool symmetric, int64_t band_blocks,
+                       std::vector<int2> &tiles, std::vector<int64_t> &offsets) {
+  const int64_t tr = cdiv(nr, kBM), tc_ = cdiv(nc, kBN);
+  tiles.clear();
+  offsets.assign(1, 0);
+  for (int64_t b0 = 0; b0 < tr; b0 += band_blocks) {
+    const int64_t b1 = b0 + band_blocks < tr ? b0 + band_blocks : tr;
+    for (int64_t tj = 0; tj < tc_; tj++)
+      for (int64_t ti = b0; ti < b1; ti++)
+        if (!symmetric || ti <= 2 * tj + 1)
+          tiles.push_back(make_int2(int(ti * kBM), int(tj * kBN)));
+    offsets.push_back(int64_t(tiles.size()));
+  }
+}
 
 __device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ prefix, int64_t n,
                                                 int64_t x) {

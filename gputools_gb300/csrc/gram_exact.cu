@@ -390,6 +390,48 @@ int pearson_exact_prologue(const float *dX, int64_t nvar, int64_t n, int slot_z,
   return GT_OK;
 }
 
+namespace {
+
+template <class W>
+int launch_exact(const W &w, int64_t ntiles, cudaStream_t s) {
+  if (ntiles == 0) return GT_OK;
+  tc::WaitCfg wc;
+  GT_TRY(make_wait_cfg(&wc));
+  auto kern = gram_exact_kernel<W>;
+  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kXSmem));
+  const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
+  ProfScope prof("pearson_gram", s);
+  kern<<<unsigned(grid), kXThreads, kXSmem, s>>>(w, wc);
+  count_launch();
+  GT_CUDA(cudaGetLastError());
+  return GT_OK;
+}
+
+PearsonFinish exact_finish(const PearsonOut &out, int64_t nA, int64_t nB) {
+  // r = 4 (S0 + 2^-12 S1 + 2^-24 S2): the finish's scale is 4
+  PearsonFinish fin{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
+                    std::sqrt(out.npairs - 2.f), 4.f, out.symmetric};
+  fin.gate = out.gate;
+  return fin;
+}
+
+}  // namespace
+
+int pearson_exact_band(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
+                       const PearsonOut &out, const int2 *tiles, int64_t ntiles, cudaStream_t s) {
+  if (nA == 0 || nB == 0 || ntiles == 0) return GT_OK;
+  if (kpad <= 0 || kpad % kKPad) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
+  using W = TableWork<PearsonFinish>;
+  W w;
+  GT_TRY(tc_plane_map(&w.ma, zA, nA, kpad, kXPlanes, kBM, kXBK, true));
+  GT_TRY(tc_plane_map(&w.mb, zB, nB, kpad, kXPlanes, kXB, kXBK, true));
+  w.tiles = tiles;
+  w.ntiles = ntiles;
+  w.nk = kpad / kXBK;
+  w.fin = exact_finish(out, nA, nB);
+  return launch_exact(w, ntiles, s);
+}
+
 int pearson_exact(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
                   const PearsonOut &out, cudaStream_t s) {
   if (nA == 0 || nB == 0) return GT_OK;
@@ -404,21 +446,8 @@ int pearson_exact(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_
   if (w.ts.ntiles > 2147483647LL)
     return fail(GT_EINVAL, "problem too large (%lld tiles)", (long long)w.ts.ntiles);
   w.nk = kpad / kXBK;
-  // r = 4 (S0 + 2^-12 S1 + 2^-24 S2): the finish's scale is 4
-  w.fin = PearsonFinish{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
-                        std::sqrt(out.npairs - 2.f), 4.f, out.symmetric};
-  w.fin.gate = out.gate;
-  if (w.ts.ntiles == 0) return GT_OK;
-  tc::WaitCfg wc;
-  GT_TRY(make_wait_cfg(&wc));
-  auto kern = gram_exact_kernel<W>;
-  GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kXSmem));
-  const int64_t grid = w.ts.ntiles < sm_count() ? w.ts.ntiles : sm_count();
-  ProfScope prof("pearson_gram", s);
-  kern<<<unsigned(grid), kXThreads, kXSmem, s>>>(w, wc);
-  count_launch();
-  GT_CUDA(cudaGetLastError());
-  return GT_OK;
+  w.fin = exact_finish(out, nA, nB);
+  return launch_exact(w, w.ts.ntiles, s);
 }
 
 }  // namespace gt

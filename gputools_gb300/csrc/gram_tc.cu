@@ -1378,6 +1378,31 @@ int pearson_tc(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t k
                                                 fin, "pearson_gram", s);
 }
 
+void pearson_band_tiles(int64_t nr, int64_t nc, bool symmetric, int64_t band_blocks,
+                        std::vector<int2> &tiles, std::vector<int64_t> &offsets) {
+  band_tiles(nr, nc, symmetric, band_blocks, tiles, offsets);
+}
+
+// The Pearson Gram on the tiles tiles[0 .. ntiles) (device table of
+// (row0, col0), band_tiles): f16x3 (k-block 32) and f16x6 only.
+int pearson_tc_band(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int kind,
+                    const PearsonOut &out, const int2 *tiles, int64_t ntiles, cudaStream_t s) {
+  if (kind == tc::KIND_F16X6) return pearson_exact_band(zA, nA, zB, nB, kpad, out, tiles, ntiles, s);
+  if (kind != tc::KIND_F16X3) return fail(GT_EUNSUPPORTED, "banded Gram: f16x3 and f16x6 only");
+  if (ntiles == 0) return GT_OK;
+  using W = TableWork<PearsonFinish>;
+  W w;
+  GT_TRY(make_plane_map(&w.ma, zA, nA, kpad, 2, kBM, 32, true));
+  GT_TRY(make_plane_map(&w.mb, zB, nB, kpad, 2, kBN, 32, true));
+  w.tiles = tiles;
+  w.ntiles = ntiles;
+  w.nk = kpad / 32;
+  w.fin = PearsonFinish{out.corr, out.ts, out.pairs, out.ld, nA, nB, out.npairs,
+                        std::sqrt(out.npairs - 2.f), 1.f / 268435456.f, out.symmetric};
+  w.fin.gate = out.gate;
+  return launch_work<tc::KIND_F16X3, 32, true>(w, ntiles, tc_chunk_kblocks(32), "pearson_gram", s);
+}
+
 namespace {
 
 template <int KIND>

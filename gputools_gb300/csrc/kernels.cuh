@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <functional>
+#include <vector>
 
 #include "gputools_gb300.h"
 
@@ -61,6 +62,17 @@ int pearson_exact_prologue(const float *dX, int64_t nvar, int64_t n, int slot_z,
                            int64_t *kpad, cudaStream_t s);
 int pearson_exact(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
                   const PearsonOut &out, cudaStream_t s);
+// The Pearson Gram on a device table of tiles (row0, col0) of 128 x 256 (see
+// band_tiles in gram_core.cuh): f16x3 and f16x6; others GT_EUNSUPPORTED.
+int pearson_tc_band(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad, int kind,
+                    const PearsonOut &out, const int2 *tiles, int64_t ntiles, cudaStream_t s);
+// band_tiles for callers outside the Gram sources: the tile table of a
+// Pearson problem in bands of `band_blocks` row blocks of kGramRows rows.
+constexpr int kGramRows = 128;
+void pearson_band_tiles(int64_t nr, int64_t nc, bool symmetric, int64_t band_blocks,
+                        std::vector<int2> &tiles, std::vector<int64_t> &offsets);
+int pearson_exact_band(const void *zA, int64_t nA, const void *zB, int64_t nB, int64_t kpad,
+                       const PearsonOut &out, const int2 *tiles, int64_t ntiles, cudaStream_t s);
 
 // pairwise_tc.cu: pairwise-complete Pearson on the tensor cores (masked
 // Gram of the six sums); every launch gated on the device flag run_if.

@@ -29,6 +29,8 @@ struct DeviceState {
   void *slot[WS_NSLOTS] = {};
   size_t bytes[WS_NSLOTS] = {};
   int *err = nullptr;  // error word of the kernels with bounded waits
+  void *host = nullptr;  // page-locked staging of host outputs
+  size_t host_bytes = 0;
   int sms = 0;
 };
 
@@ -230,6 +232,34 @@ int ws_get(int slot, size_t bytes, void **ptr) {
   return GT_OK;
 }
 
+int host_ws_get(size_t bytes, void **ptr) {
+  int dev = 0;
+  GT_TRY(current_device(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState &d = g_dev[dev];
+  if (d.host_bytes < bytes) {
+    if (d.host) {
+      cudaDeviceSynchronize();
+      cudaFreeHost(d.host);
+      d.host = nullptr;
+      d.host_bytes = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    want = (want + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+    void *p = nullptr;
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GT_ENOMEM, "page-locked staging of %zu bytes unavailable: %s", want,
+                  cudaGetErrorString(e));
+    }
+    d.host = p;
+    d.host_bytes = want;
+  }
+  *ptr = d.host;
+  return GT_OK;
+}
+
 int device_error_word(int **p) {
   int dev = 0;
   GT_TRY(current_device(&dev));
@@ -281,7 +311,7 @@ void ws_release_all() {
   cudaGetDevice(&cur);
   for (int dev = 0; dev < kMaxDevices; dev++) {
     DeviceState &d = g_dev[dev];
-    bool any = d.err != nullptr;
+    bool any = d.err != nullptr || d.host != nullptr;
     for (int s = 0; s < WS_NSLOTS; s++) any |= d.slot[s] != nullptr;
     if (!any) continue;
     cudaSetDevice(dev);
@@ -293,6 +323,9 @@ void ws_release_all() {
     }
     if (d.err) cudaFree(d.err);
     d.err = nullptr;
+    if (d.host) cudaFreeHost(d.host);
+    d.host = nullptr;
+    d.host_bytes = 0;
   }
   if (cur >= 0) cudaSetDevice(cur);
 }

@@ -346,3 +346,44 @@ def test_pageable_outputs_written_in_place(gpu, oracle_mod, rng):
 def gpu_path():
     import gputools_gb300 as g
     return g.get_gram_path()
+
+
+@pytest.mark.parametrize("pth", ["f16x3", "f16x6"])
+@pytest.mark.parametrize("sym", [True, False])
+def test_banded_pipeline_into_pageable_outputs(gpu, oracle_mod, pth, sym):
+    """Outputs of 64 MB and more in ordinary (pageable) memory: the Gram runs
+    in bands of rows whose results host threads copy out of page-locked
+    staging while the next band runs.  Checked against the oracle on rows at
+    the band edges, with every pair count n and (cor(x)) an exactly
+    symmetric result with a unit diagonal."""
+    import gputools_gb300 as g
+    rng = np.random.default_rng(4242 + sym)
+    p, n = 4160, 80  # 4160 rows: 33 row blocks, so the 16 bands are uneven
+    X = (rng.standard_normal((p, n)) * 3 + 100).astype(np.float32)
+    X[:, :5] += np.linspace(0, 2, p, dtype=np.float32)[:, None]
+    Y = X.copy() if sym else (rng.standard_normal((p, n)) + 1).astype(np.float32)
+    corr = np.full((p, p), -9.0, np.float32)
+    ts = np.full((p, p), -9.0, np.float32)
+    pairs = np.full((p, p), -9.0, np.float32)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    old = g.get_gram_path()
+    g.set_gram_path(pth)
+    try:
+        st = gpu.gt_pmcc(0, vp(X), p, vp(Y), p, n, vp(pairs), vp(corr), vp(ts))
+    finally:
+        g.set_gram_path(old)
+    assert st == 0, gpu.gt_last_error().decode()
+    assert np.all(pairs == n)
+    rows = np.array([0, 255, 256, 511, 512, 2047, 2048, p - 129, p - 128, p - 1])
+    wc, _, wt = oracle_mod.pearson(X[rows], Y, use=0)
+    if sym:
+        for k, r in enumerate(rows):
+            wc[k, r] = 1.0
+        assert np.array_equal(corr, corr.T)
+        assert np.all(np.diag(corr) == 1.0)
+    assert np.abs(corr[rows].astype(np.float64) - wc).max() <= tol(pth, n)
+    r = corr[rows]
+    rule = np.where(r >= np.float32(0.999), np.float32(10000),
+                    r * np.sqrt(np.float32(n - 2) / (np.float32(1) - r * r)))
+    good = ~np.isnan(rule)
+    np.testing.assert_allclose(ts[rows][good], rule[good], rtol=2e-6, atol=1e-6)
