@@ -255,35 +255,46 @@ struct PearsonFinish {
       __syncwarp();
       return;
     }
+    // Edge and diagonal blocks: the interior path's unrolled loops with
+    // predicated stores (a loop with per-entry branches stored at a third of
+    // the rate).  Columns past nc (j >= jn) and rows past nr (i >= in_) are
+    // skipped; a symmetric problem keeps entries on and above the diagonal.
+    const int jn = nc - c0 >= 32 ? 32 : int(nc - c0);
+    const int in_ = nr - rbase >= 32 ? 32 : int(nr - rbase);
     // mirror orientation (lanes hold consecutive rows): coalesced from registers
     if (symmetric && r < nr) {
+      int64_t o = c0 * ld + r;
+      const int dj = int(r - c0);  // the lane's diagonal column, relative to c0
 #pragma unroll
       for (int j = 0; j < 32; j++) {
-        const int64_t c = c0 + j;
-        if (c < nc && r < c) {
+        if (j < jn && j > dj) {
           const float v = clamp_r(g[j] * gscale);
-          const int64_t o = c * ld + r;
           if (corr) corr[o] = v;
           if (ts) ts[o] = signif_fast(v, sq_nm2);
           if (pairs) pairs[o] = npairs;
         }
+        o += ld;
       }
     }
     // row orientation through the staging tile
 #pragma unroll
     for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
     __syncwarp();
-    const int64_t c = c0 + lane;
-    int64_t o = rbase * ld + c;
-    for (int i = 0; i < 32; i++, o += ld) {
-      const int64_t ri = rbase + i;
-      if (ri >= nr) break;
-      if (c >= nc || (symmetric && c < ri)) continue;
-      float v = clamp_r(wsm[i * 33 + lane] * gscale);
-      if (symmetric && c == ri && v == v) v = 1.f;
-      if (corr) corr[o] = v;
-      if (ts) ts[o] = signif_fast(v, sq_nm2);
-      if (pairs) pairs[o] = npairs;
+    if (lane < jn) {
+      const int64_t c = c0 + lane;
+      const int64_t di = symmetric ? c - rbase : 31;  // rows i <= di are kept
+      int64_t o = rbase * ld + c;
+#pragma unroll 8
+      for (int i = 0; i < 32; i++) {
+        if (i < in_ && i <= di) {
+          float v = clamp_r(wsm[i * 33 + lane] * gscale);
+          if (symmetric && i == di && v == v) v = 1.f;
+          if (corr) corr[o] = v;
+          if (ts) ts[o] = signif_fast(v, sq_nm2);
+          if (pairs) pairs[o] = npairs;
+        }
+        o += ld;
+      }
     }
     __syncwarp();
   }
@@ -412,28 +423,27 @@ struct PearsonBatchProblem {  // aligned as CUtensorMap
   PearsonFinish fin;
 };
 
+// Each CTA walks its own list of tiles, built on the host: per tile one
+// entry {problem, row0, col0, k-blocks}, so a lookup is one 16-byte load that
+// the cursor issues a tile ahead.
 struct PearsonBatchWork {
   const PearsonBatchProblem *probs;
-  const int64_t *tile_prefix;
-  int64_t nprob;
-  const int64_t *cta_tiles, *cta_off;
+  const int4 *table;     // the CTAs' tile lists, one after the other
+  const int64_t *cta_off;  // CTA c's tiles: table[cta_off[c] .. cta_off[c + 1])
   __device__ bool tile(int64_t cursor, TileRef &ref) const {
     const int64_t idx = cta_off[blockIdx.x] + cursor;
     if (idx >= cta_off[blockIdx.x + 1]) return false;
-    const int64_t t = cta_tiles[idx];
-    const int64_t pi = find_segment(tile_prefix, nprob, t);
-    const PearsonBatchProblem &pr = probs[pi];
-    int64_t ti, tj;
-    tile_coords(pr.ts, t - tile_prefix[pi], ti, tj);
-    ref.row0 = ti * kBM;
-    ref.col0 = tj * kBN;
+    const int4 t = table[idx];
+    const PearsonBatchProblem &pr = probs[t.x];
+    ref.row0 = t.y;
+    ref.col0 = t.z;
     ref.ma = &pr.map_a;
     ref.mb = &pr.map_b;
-    ref.nk = pr.nk;
-    ref.prob = pi;
+    ref.nk = t.w;
+    ref.prob = t.x;
     return true;
   }
-  static constexpr bool kPrefetch = false;
+  static constexpr bool kPrefetch = true;
   __device__ bool skip() const { return false; }
   __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
   __device__ void drain(EpiCtx &) const {}

@@ -1519,6 +1519,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
   std::vector<PearsonBatchInput> inputs;
   std::vector<PearsonBatchProblem> descs;
   std::vector<int64_t> var_prefix{0}, tile_prefix{0}, cost;
+  std::vector<int4> table_all;  // {problem, row0, col0, k-blocks} per global tile
   int64_t plane_elems = 0, vars = 0;
   // first pass: shapes and offsets
   for (int64_t i = 0; i < count; i++) {
@@ -1556,25 +1557,57 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     std::memset(&d, 0, sizeof(d));
     GT_TRY(make_plane_map(&d.map_a, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk, f16));
     GT_TRY(make_plane_map(&d.map_b, planes + b.plane_off, b.p, b.kpad, nsplit, kBN, bk, f16));
-    d.ts = make_tiles(b.p, b.p, kUpper, 1);
+    d.ts = make_tiles(b.p, b.p, kUpper, band_group(int64_t(kBN) * b.kpad * 2 * nsplit));
     d.nk = b.kpad / bk;
     d.fin = PearsonFinish{q.corr, q.ts, q.pairs, b.p, b.p, b.p, float(b.n),
                           std::sqrt(float(b.n) - 2.f), gscale, 1};
     descs.push_back(d);
     tile_prefix.push_back(tile_prefix.back() + d.ts.ntiles);
-    const int64_t nch = (d.nk + ckb - 1) / ckb;
-    for (int64_t t = 0; t < d.ts.ntiles; t++) cost.push_back(d.nk + 2 * nch + 4);
+    // Cost of a tile (ns, on one SM): its MMAs, or its epilogue when that
+    // takes longer -- tiles of few observations are bound by their stores
+    // (12 bytes per entry and orientation, ~24 bytes per ns per SM measured
+    // on single problems) -- plus a fixed part per tile.
+    const int64_t prods = nsplit == 3 ? 6 : 3;
+    const double mma_ns = double(d.nk) * (bk / 16) * prods * 128.0 / 1.9;
+    for (int64_t t = 0; t < d.ts.ntiles; t++) {
+      int64_t ti, tj;
+      tile_coords(d.ts, t, ti, tj);
+      const int64_t r0 = ti * kBM, r1 = std::min(b.p, r0 + kBM);
+      const int64_t c0 = tj * kBN, c1 = std::min(b.p, c0 + kBN);
+      int64_t upper = 0, diag = 0;
+      for (int64_t r = r0; r < r1; r++) {
+        upper += std::max<int64_t>(0, c1 - std::max(c0, r));
+        diag += (r >= c0 && r < c1) ? 1 : 0;
+      }
+      const double epi_ns = 12.0 * double(2 * upper - diag) / 24.0;
+      cost.push_back(int64_t(std::max(mma_ns, epi_ns) + 1500.0));
+      table_all.push_back(make_int4(int(pidx - 1), int(r0), int(c0), int(d.nk)));
+    }
   }
   const int64_t ntiles = tile_prefix.back();
   int64_t ncta = sm_count();
   if (ncta > ntiles) ncta = ntiles;
-  std::vector<int64_t> cta_tiles, cta_off;
+  std::vector<int4> cta_tiles;
+  std::vector<int64_t> cta_off;
   if (ntiles > 0) {
-    // longest-processing-time first over the CTAs
-    std::vector<int64_t> order(ntiles);
-    for (int64_t t = 0; t < ntiles; t++) order[t] = t;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int64_t a, int64_t c) { return cost[a] > cost[c]; });
+    // list scheduling in an order that keeps operand panels shared: the
+    // problems by decreasing total cost, each problem's tiles in its band
+    // order, every tile to the CTA with the least work so far -- so the CTAs
+    // running at one time work on neighbouring tiles of one problem and read
+    // its panels from L2 (a longest-tile-first order spread every problem over
+    // the whole run)
+    std::vector<int64_t> porder(descs.size());
+    std::vector<int64_t> pcost(descs.size(), 0);
+    for (size_t q = 0; q < descs.size(); q++) {
+      porder[q] = int64_t(q);
+      for (int64_t t = tile_prefix[q]; t < tile_prefix[q + 1]; t++) pcost[q] += cost[t];
+    }
+    std::stable_sort(porder.begin(), porder.end(),
+                     [&](int64_t a, int64_t c) { return pcost[a] > pcost[c]; });
+    std::vector<int64_t> order;
+    order.reserve(size_t(ntiles));
+    for (int64_t q : porder)
+      for (int64_t t = tile_prefix[q]; t < tile_prefix[q + 1]; t++) order.push_back(t);
     std::vector<std::vector<int64_t>> lists(ncta);
     using Item = std::pair<int64_t, int64_t>;
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
@@ -1589,7 +1622,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     cta_off.assign(ncta + 1, 0);
     for (int64_t c = 0; c < ncta; c++) {
       cta_off[c] = int64_t(cta_tiles.size());
-      cta_tiles.insert(cta_tiles.end(), lists[c].begin(), lists[c].end());
+      for (int64_t t : lists[c]) cta_tiles.push_back(table_all[t]);
     }
     cta_off[ncta] = int64_t(cta_tiles.size());
   }
@@ -1598,21 +1631,18 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     if (bytes) GT_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
     return GT_OK;
   };
-  void *d_desc = nullptr, *d_tp = nullptr, *d_ct = nullptr, *d_co = nullptr;
+  void *d_desc = nullptr, *d_ct = nullptr, *d_co = nullptr;
   GT_TRY(upload(inputs.data(), inputs.size() * sizeof(PearsonBatchInput), &d_in));
   GT_TRY(upload(var_prefix.data(), var_prefix.size() * 8, &d_vp));
   GT_TRY(upload(descs.data(), descs.size() * sizeof(PearsonBatchProblem), &d_desc));
-  GT_TRY(upload(tile_prefix.data(), tile_prefix.size() * 8, &d_tp));
-  GT_TRY(upload(cta_tiles.data(), cta_tiles.size() * 8, &d_ct));
+  GT_TRY(upload(cta_tiles.data(), cta_tiles.size() * sizeof(int4), &d_ct));
   GT_TRY(upload(cta_off.data(), cta_off.size() * 8, &d_co));
   // the device's error word; the wait limit is the one in force when the plan is built
   tc::WaitCfg wc;
   GT_TRY(make_wait_cfg(&wc));
   PearsonBatchWork w;
   w.probs = static_cast<const PearsonBatchProblem *>(d_desc);
-  w.tile_prefix = static_cast<const int64_t *>(d_tp);
-  w.nprob = nprob;
-  w.cta_tiles = static_cast<const int64_t *>(d_ct);
+  w.table = static_cast<const int4 *>(d_ct);
   w.cta_off = static_cast<const int64_t *>(d_co);
   auto *in = static_cast<const PearsonBatchInput *>(d_in);
   auto *vp = static_cast<const int64_t *>(d_vp);
