@@ -707,14 +707,42 @@ def run_configs(lib, g, _lib, stream, dev, steps):
     dXb = torch.empty_like(Xb)
     ms = ev_time(lambda: _lib.check(lib.gt_cor_backward_device(vp(Xb), 4096, 1024, vp(Gb),
                                                                vp(dXb), sptr)), k)
-    out["cor_backward_1024x4096"] = {"ms": ms, "useful_tflops": 2 * 4096 * 4096 * 1024 / (ms * 1e-3) / 1e12}
+    peaks, peaks_kind = load_peaks()
+    useful = 2 * 4096 * 4096 * 1024 / (ms * 1e-3) / 1e12
+    prods = {"f16x3": 3, "f16x6": 3, "bf16x3": 3, "bf16x6": 6}.get(g.get_gram_path(), 1)
+    out["cor_backward_1024x4096"] = {
+        "ms": ms, "useful_tflops": useful,
+        "roofline": {"bound": "tensor", "achieved": useful * prods, "peak": peaks["bf16_tflops"],
+                     "unit": "TFLOP/s", "frac": useful * prods / peaks["bf16_tflops"],
+                     "peak_kind": f"{peaks_kind} bf16 burst",
+                     "flops": f"whole call: the W = (G + G^T) Z GEMM's {prods} split products "
+                              "x 2 p^2 n, over the call's time (prologue, operand splits and "
+                              "the rank-1 finish included)"}}
     Xm = torch.from_numpy(rng.standard_normal((8192, 32), dtype=np.float32)).to(dev)
     delta = torch.from_numpy(rng.random(8192 * 8191 // 2, dtype=np.float32) * 8).to(dev)
     gm = torch.empty_like(Xm)
     loss = torch.zeros(1, dtype=torch.float64, device=dev)
     ms = ev_time(lambda: _lib.check(lib.gt_mds_stress_device(vp(Xm), 8192, 32, vp(delta), vp(gm),
                                                              vp(loss), sptr)), k)
-    out["mds_stress_8192x32"] = {"ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3)}
+    # fused CUDA-core pass: per ordered pair the distance (3 flop per
+    # dimension), the weight and the accumulation (2 flop per dimension)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sms * 128 * 2 * 2070e6 / 1e12
+    mds_tf = 8192 * 8191 * (5 * 32 + 8) / (ms * 1e-3) / 1e12
+    out["mds_stress_8192x32"] = {
+        "ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3),
+        "roofline": {"bound": "fp32-simt", "achieved": mds_tf, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": mds_tf / fp32_peak,
+                     "peak_kind": "nominal FP32 FMA rate at 2070 MHz",
+                     "flops": "5 flop per dimension + 8 per ordered pair"}}
+    # above 64 dimensions: GEMMs plus the rank-1 correction on the tensor cores
+    Xw = torch.from_numpy(rng.standard_normal((8192, 256), dtype=np.float32)).to(dev)
+    gw = torch.empty_like(Xw)
+    ms = ev_time(lambda: _lib.check(lib.gt_mds_stress_device(vp(Xw), 8192, 256, vp(delta),
+                                                             vp(gw), vp(loss), sptr)), k)
+    out["mds_stress_8192x256"] = {"ms": ms, "pairs_per_s": 8192 * 8191 / (ms * 1e-3),
+                                  "path": "tcgen05: distances, W planes, W X"}
+    del Xw, gw
     del Xb, Gb, dXb, Xm, delta, gm
     # gpuMi: 2000 variables x 1000 samples, 10 bins, cubic B-splines (order 3),
     # the symmetric all-pairs matrix; tensor cores and the CUDA-core path, and

@@ -11,6 +11,7 @@
 
 #include <cuda.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <type_traits>
 #include <vector>
@@ -163,6 +164,8 @@ inline TileSpace make_tiles(int64_t nr, int64_t nc, int mode, int64_t group) {
 // Band width for operand planes of `panel_bytes` per 256-row B panel: as
 // many B panels as fit in about 40 MB of L2, at most 16.
 inline int64_t band_group(int64_t panel_bytes) {
+  const char *e = std::getenv("GT_TC_GROUP");
+  if (e && std::atoi(e) > 0) return std::atoi(e);
   const int64_t g = (int64_t(40) << 20) / (panel_bytes > 0 ? panel_bytes : 1);
   return g < 1 ? 1 : (g > 16 ? 16 : g);
 }
