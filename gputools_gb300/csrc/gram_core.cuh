@@ -199,6 +199,14 @@ struct EpiCtx {
   }
 };
 
+// Whether a finish takes a block from the warp's staging tile (block()), not
+// only from registers (operator()).
+template <class Fin, class = void>
+struct staged_block : std::false_type {};
+template <class Fin>
+struct staged_block<Fin, std::void_t<decltype(Fin::kStagedBlock)>>
+    : std::integral_constant<bool, Fin::kStagedBlock> {};
+
 __device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
 
 // hostSignif's rule (src/correlation.cpp:51-64), t = r sqrt(n-2) / sqrt(1-r^2)
@@ -209,6 +217,7 @@ __device__ __forceinline__ float signif_fast(float r, float sq_nm2) {
 }
 
 struct PearsonFinish {
+  static constexpr bool kStagedBlock = true;  // has block(): entries from the staging tile
   float *corr, *ts, *pairs;
   int64_t ld, nr, nc;
   float npairs, sq_nm2;
@@ -224,31 +233,41 @@ struct PearsonFinish {
     if (pairs) *pp = npairs;
   }
 
+  // A block from registers: g[j] = entry (r, c0 + j), lanes on consecutive rows.
   __device__ void operator()(int64_t r, int64_t c0, const float (&g)[32], EpiCtx &ctx) const {
     const int lane = threadIdx.x & 31;
-    float *wsm = ctx.wsm;
+#pragma unroll
+    for (int j = 0; j < 32; j++) ctx.wsm[lane * 33 + j] = g[j];
+    __syncwarp();
+    block(r, c0, ctx);
+  }
+
+  // A block staged in the warp's tile: wsm[lane * 33 + j] = entry (r, c0 + j).
+  // Both orientations read the tile (the padding keeps either read free of
+  // bank conflicts), so the body is compact: loops of four, not unrolled
+  // copies per entry.  Ends with the warp converged and the tile free.
+  __device__ void block(int64_t r, int64_t c0, EpiCtx &ctx) const {
+    const int lane = threadIdx.x & 31;
+    const float *wsm = ctx.wsm;
     const int64_t rbase = r - lane;
     // interior block: every entry exists and (symmetric) lies above the diagonal
     const bool interior = (c0 + 31 < nc) && (symmetric ? (rbase + 31 < c0) : (rbase + 31 < nr));
     if (interior) {
-      // branch-free stores with pointer increments
       if (symmetric) {
+        // mirror orientation: lanes hold consecutive rows of column c0 + j
         const int64_t o = c0 * ld + r;
         float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
-#pragma unroll
+#pragma unroll 4
         for (int j = 0; j < 32; j++) {
-          put(pc, pt, pp, clamp_r(g[j] * gscale));
+          put(pc, pt, pp, clamp_r(wsm[lane * 33 + j] * gscale));
           pc += ld;
           pt += ld;
           pp += ld;
         }
       }
-#pragma unroll
-      for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-      __syncwarp();
       const int64_t o = rbase * ld + c0 + lane;
       float *pc = corr + o, *pt = ts + o, *pp = pairs + o;
-#pragma unroll 8
+#pragma unroll 4
       for (int i = 0; i < 32; i++) {
         put(pc, pt, pp, clamp_r(wsm[i * 33 + lane] * gscale));
         pc += ld;
@@ -258,20 +277,18 @@ struct PearsonFinish {
       __syncwarp();
       return;
     }
-    // Edge and diagonal blocks: the interior path's unrolled loops with
-    // predicated stores (a loop with per-entry branches stored at a third of
-    // the rate).  Columns past nc (j >= jn) and rows past nr (i >= in_) are
-    // skipped; a symmetric problem keeps entries on and above the diagonal.
+    // Edge and diagonal blocks: the same loops with predicated stores.
+    // Columns past nc (j >= jn) and rows past nr (i >= in_) are skipped; a
+    // symmetric problem keeps entries on and above the diagonal.
     const int jn = nc - c0 >= 32 ? 32 : int(nc - c0);
     const int in_ = nr - rbase >= 32 ? 32 : int(nr - rbase);
-    // mirror orientation (lanes hold consecutive rows): coalesced from registers
     if (symmetric && r < nr) {
       int64_t o = c0 * ld + r;
       const int dj = int(r - c0);  // the lane's diagonal column, relative to c0
-#pragma unroll
+#pragma unroll 4
       for (int j = 0; j < 32; j++) {
         if (j < jn && j > dj) {
-          const float v = clamp_r(g[j] * gscale);
+          const float v = clamp_r(wsm[lane * 33 + j] * gscale);
           if (corr) corr[o] = v;
           if (ts) ts[o] = signif_fast(v, sq_nm2);
           if (pairs) pairs[o] = npairs;
@@ -279,15 +296,11 @@ struct PearsonFinish {
         o += ld;
       }
     }
-    // row orientation through the staging tile
-#pragma unroll
-    for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = g[j];
-    __syncwarp();
     if (lane < jn) {
       const int64_t c = c0 + lane;
       const int64_t di = symmetric ? c - rbase : 31;  // rows i <= di are kept
       int64_t o = rbase * ld + c;
-#pragma unroll 8
+#pragma unroll 4
       for (int i = 0; i < 32; i++) {
         if (i < in_ && i <= di) {
           float v = clamp_r(wsm[i * 33 + lane] * gscale);

@@ -634,6 +634,15 @@ struct EuclidLineWork {
   }
 };
 
+// Block I (columns 32 I .. 32 I + 31) of a lane's running sums into the
+// warp's staging tile, row = lane.
+template <int I>
+__device__ __forceinline__ void stage_block(const float (&acc)[128], float *wsm) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = acc[32 * I + j];
+}
+
 template <int KIND, int BK, bool CHUNKED, class Work>
 __global__ void __launch_bounds__(TcCfg<KIND, BK, !CHUNKED>::THREADS, 1)
 gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg wc) {
@@ -811,12 +820,30 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
           if (lane == 0) tc::mbar_arrive(&acce[buf]);
         }
         if (!ok) break;
+        using FinT = std::decay_t<decltype(fin)>;
+        if constexpr (staged_block<FinT>::value) {
+          // One copy of the finish for the four 32-column blocks, each staged
+          // in the warp's tile first: four inlined copies outgrow the
+          // instruction cache once the epilogue bounds the kernel (small n).
+#pragma unroll 1
+          for (int i = 0; i < 4; i++) {
+            switch (i) {
+              case 0: stage_block<0>(acc, ctx.wsm); break;
+              case 1: stage_block<1>(acc, ctx.wsm); break;
+              case 2: stage_block<2>(acc, ctx.wsm); break;
+              default: stage_block<3>(acc, ctx.wsm); break;
+            }
+            __syncwarp();
+            fin.block(r, col + 32 * i, ctx);
+          }
+        } else {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-          float g[32];
+          for (int i = 0; i < 4; i++) {
+            float g[32];
 #pragma unroll
-          for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
-          fin(r, col + 32 * i, g, ctx);
+            for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
+            fin(r, col + 32 * i, g, ctx);
+          }
         }
         fin.end_tile(ctx);
       } else {

@@ -38,7 +38,10 @@ def test_pearson_batch_matches_single_and_oracle(gpu, oracle_mod, gram_path, gra
     import torch
     import gputools_gb300 as g
     rng = np.random.default_rng(31)
-    shapes = _shapes(rng, 40, 600, 3, 900) + [(1, 10), (128, 64), (257, 129), (300, 2)]
+    # p of every residue mod 8 (row strides off the 32-byte sectors) and
+    # problems of several tile rows and columns
+    shapes = _shapes(rng, 40, 600, 3, 900) + [(1, 10), (128, 64), (257, 129), (300, 2),
+                                              (1023, 70), (777, 300), (520, 33)]
     xs = [rng.standard_normal((p, n)).astype(np.float32) * 2 + 5 for p, n in shapes]
     dxs = [torch.from_numpy(x).cuda() for x in xs]
     with g.BatchPlan(dxs, "pearson", graph=graph) as plan:
@@ -53,6 +56,17 @@ def test_pearson_batch_matches_single_and_oracle(gpu, oracle_mod, gram_path, gra
             if ok.any():
                 assert np.abs(corr[ok] - want[ok]).max() <= _tol(gram_path, x.shape[1])
             assert np.all(o["pairs"].cpu().numpy() == x.shape[1])
+            # t-scores in both orientations: hostSignif's rule on the stored r
+            r = corr.astype(np.float32)
+            ts = o["ts"].cpu().numpy()
+            rule = np.where(r >= np.float32(0.999), np.float32(10000),
+                            r * np.sqrt((np.float32(x.shape[1]) - 2) / (np.float32(1) - r * r)))
+            # 1 - r^2 cancels near |r| = 1: there the rounding of r * r (the
+            # kernel fuses it) moves t by ~eps / (1 - r^2) relative
+            fin = ~np.isnan(rule)
+            well = fin & (np.abs(r) < 0.99)
+            np.testing.assert_allclose(ts[well], rule[well], rtol=2e-6, atol=1e-6)
+            np.testing.assert_allclose(ts[fin], rule[fin], rtol=1e-3, atol=1e-6)
             single = g.pmcc_device(dx)["corr"].cpu().numpy()
             assert np.allclose(corr, single, atol=1e-6, equal_nan=True)
 
