@@ -8,7 +8,10 @@
 //   W = S Z  (S = G + G^T, Z the p x n matrix of the z_j),
 //   dL/dx_j = (w_j - z_j (z_j . w_j)) / s_j,
 // i.e. one GEMM plus a rank-1 correction per variable.  Means and norms are
-// recomputed in FP64 (not stored by the forward pass); S and Z^T are split
+// recomputed (not stored by the forward pass) with compensated float sums;
+// the centring, z_j . w_j and the correction run in float arithmetic with the
+// mean as a float pair and the dot product compensated (GB300's FP64 pipe is
+// a small fraction of its FP32 pipe).  S and Z^T are split
 // into bf16 planes and W runs on the tcgen05 chunked-accumulation kernel
 // (gram_tc.cu), or on the CUDA-core engine for GT_GRAM_FP32.
 //
@@ -25,6 +28,7 @@
 #include "common.cuh"
 #include "allpairs_simt.cuh"
 #include "kernels.cuh"
+#include "stats.cuh"
 #include "tc_ptx.cuh"
 
 #include <cuda_bf16.h>
@@ -35,12 +39,13 @@ namespace {
 
 constexpr int64_t kKPadB = 64;
 
-__device__ __forceinline__ float zval(const float *X, const ColStats *st, int64_t n, int64_t i,
-                                      int64_t k) {
-  const ColStats s = st[i];
-  if (s.flags) return 0.f;
-  return float((double(X[i * n + k]) - s.mean) * s.inv_norm);
-}
+// z of a variable in float arithmetic (0 for a flagged variable).
+struct ZCenter {
+  Centerer cen;
+  bool zero;
+  __device__ __forceinline__ explicit ZCenter(const ColStats &s) : cen(s), zero(s.flags != 0) {}
+  __device__ __forceinline__ float operator()(float x) const { return zero ? 0.f : cen(x); }
+};
 
 template <class T>
 __device__ __forceinline__ void put_parts(T *dst, int64_t plane, int64_t idx, float v, int ns);
@@ -60,24 +65,54 @@ __device__ __forceinline__ void put_parts<__nv_bfloat16>(__nv_bfloat16 *dst, int
 }
 
 // S = G + G^T as rows j, columns i (ld kp >= p, zero padded), float or bf16
-// planes.  32 x 32 tiles transposed through shared memory.
+// planes.  64 x 64 tiles: the transposed operand goes through shared memory,
+// loads and stores in pairs along the rows when p is even.
 template <class T>
-__global__ void sym_operand_kernel(const float *__restrict__ G, int64_t p, int64_t kp, int ns,
-                                   T *__restrict__ S) {
-  __shared__ float tile[32][33];
-  const int64_t i0 = int64_t(blockIdx.x) * 32, j0 = int64_t(blockIdx.y) * 32;
-  const int tx = threadIdx.x, ty0 = threadIdx.y;
-  for (int ty = ty0; ty < 32; ty += 8) {
-    const int64_t i = i0 + ty, j = j0 + tx;
-    tile[ty][tx] = (i < p && j < p) ? G[i * p + j] : 0.f;  // G[i][j], rows i
+__global__ void __launch_bounds__(256)
+sym_operand_kernel(const float *__restrict__ G, int64_t p, int64_t kp, int ns, T *__restrict__ S) {
+  __shared__ float tile[64][65];
+  const int64_t i0 = int64_t(blockIdx.x) * 64, j0 = int64_t(blockIdx.y) * 64;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool pairs = (p & 1) == 0 && (reinterpret_cast<uintptr_t>(G) & 7u) == 0;
+  // tile[a][b] = G[i0 + a][j0 + b]
+#pragma unroll 4
+  for (int r = 0; r < 8; r++) {
+    const int a = ty + 8 * r;
+    const int64_t i = i0 + a, j = j0 + 2 * tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (i < p) {
+      if (pairs && j + 1 < p) {
+        v = *reinterpret_cast<const float2 *>(G + i * p + j);
+      } else {
+        if (j < p) v.x = G[i * p + j];
+        if (j + 1 < p) v.y = G[i * p + j + 1];
+      }
+    }
+    tile[a][2 * tx] = v.x;
+    tile[a][2 * tx + 1] = v.y;
   }
   __syncthreads();
   const int64_t plane = p * kp;
-  for (int ty = ty0; ty < 32; ty += 8) {
-    const int64_t j = j0 + ty, i = i0 + tx;
+#pragma unroll 4
+  for (int r = 0; r < 8; r++) {
+    const int b = ty + 8 * r;
+    const int64_t j = j0 + b, i = i0 + 2 * tx;
     if (j >= p || i >= kp) continue;
-    const float v = (i < p) ? G[j * p + i] + tile[tx][ty] : 0.f;
-    put_parts<T>(S, plane, j * kp + i, v, ns);
+    float2 g = make_float2(0.f, 0.f);
+    if (pairs && i + 1 < p) {
+      g = *reinterpret_cast<const float2 *>(G + j * p + i);
+    } else {
+      if (i < p) g.x = G[j * p + i];
+      if (i + 1 < p) g.y = G[j * p + i + 1];
+    }
+    const float s0 = i < p ? g.x + tile[2 * tx][b] : 0.f;
+    const float s1 = i + 1 < p ? g.y + tile[2 * tx + 1][b] : 0.f;
+    if constexpr (std::is_same<T, float>::value) {
+      *reinterpret_cast<float2 *>(S + j * kp + i) = make_float2(s0, s1);  // kp is even
+    } else {
+      put_parts<T>(S, plane, j * kp + i, s0, ns);
+      put_parts<T>(S, plane, j * kp + i + 1, s1, ns);
+    }
   }
 }
 
@@ -86,11 +121,27 @@ template <class T>
 __global__ void zt_operand_kernel(const float *__restrict__ X, int64_t p, int64_t n, int64_t kp,
                                   const ColStats *__restrict__ st, int ns, T *__restrict__ Zt) {
   __shared__ float tile[32][33];
+  __shared__ float cen[32][4];  // the block's 32 variables: mean pair, inverse norm, flag
   const int64_t k0 = int64_t(blockIdx.x) * 32, i0 = int64_t(blockIdx.y) * 32;
   const int tx = threadIdx.x, ty0 = threadIdx.y;
+  if (ty0 == 0) {
+    const int64_t i = i0 + tx;
+    if (i < p) {
+      const ColStats s = st[i];
+      const Centerer c(s);
+      cen[tx][0] = c.mhi;
+      cen[tx][1] = c.mlo;
+      cen[tx][2] = c.inv;
+      cen[tx][3] = s.flags ? 1.f : 0.f;
+    }
+  }
+  __syncthreads();
   for (int ty = ty0; ty < 32; ty += 8) {
     const int64_t i = i0 + ty, k = k0 + tx;
-    tile[ty][tx] = (i < p && k < n) ? zval(X, st, n, i, k) : 0.f;  // rows i
+    float z = 0.f;
+    if (i < p && k < n && cen[ty][3] == 0.f)
+      z = ((X[i * n + k] - cen[ty][0]) - cen[ty][1]) * cen[ty][2];
+    tile[ty][tx] = z;  // rows i
   }
   __syncthreads();
   const int64_t plane = n * kp;
@@ -105,26 +156,42 @@ constexpr int kFinThreads = 256;
 
 // Rows of a float matrix (nrows x kp) as f16x3 planes ([2][nrows][kp]), each
 // row scaled by the power of two that brings its largest magnitude into
-// [2^14, 2^15); scale[row] = the factor that undoes it.  One warp per row.
+// [2^14, 2^15); scale[row] = the factor that undoes it.  One warp per row,
+// four consecutive values per lane (kp is a multiple of 64 and the rows are
+// 16-byte aligned).
 __global__ void __launch_bounds__(256)
 f16x3_rows_kernel(const float *__restrict__ M, int64_t nrows, int64_t kp,
                   uint16_t *__restrict__ planes, float *__restrict__ scale) {
   const int64_t row = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
   if (row >= nrows) return;  // whole warps
   const int lane = threadIdx.x & 31;
-  const float *m = M + row * kp;
+  const float4 *m = reinterpret_cast<const float4 *>(M + row * kp);
+  const int64_t k4 = kp >> 2;
   float amax = 0.f;
-  for (int64_t k = lane; k < kp; k += 32) amax = fmaxf(amax, fabsf(m[k]));
+  for (int64_t k = lane; k < k4; k += 32) {
+    const float4 v = m[k];
+    amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+  }
   amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(amax)));
   const int e = tc::f16_scale_exp(amax);
   const float sc = tc::exp2i(e);
   if (lane == 0) scale[row] = tc::exp2i(-e);
   const int64_t plane = nrows * kp;
-  for (int64_t k = lane; k < kp; k += 32) {
-    uint16_t p[3];
-    tc::split_parts<tc::KIND_F16X3>(m[k] * sc, p);
-    planes[row * kp + k] = p[0];
-    planes[plane + row * kp + k] = p[1];
+  uint2 *p0 = reinterpret_cast<uint2 *>(planes + row * kp);
+  uint2 *p1 = reinterpret_cast<uint2 *>(planes + plane + row * kp);
+  for (int64_t k = lane; k < k4; k += 32) {
+    const float4 v = m[k];
+    const float e4[4] = {v.x, v.y, v.z, v.w};
+    uint32_t h[2] = {0u, 0u}, l[2] = {0u, 0u};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint16_t pp[3];
+      tc::split_parts<tc::KIND_F16X3>(e4[q] * sc, pp);
+      h[q >> 1] |= uint32_t(pp[0]) << (16 * (q & 1));
+      l[q >> 1] |= uint32_t(pp[1]) << (16 * (q & 1));
+    }
+    p0[k] = make_uint2(h[0], h[1]);
+    p1[k] = make_uint2(l[0], l[1]);
   }
 }
 
@@ -157,24 +224,67 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh) {
   return sh[0];
 }
 
-// dX_j = (w_j - z_j (z_j . w_j)) * inv_norm_j, one CTA per variable.
+// dX_j = (w_j - z_j (z_j . w_j)) * inv_norm_j, one warp per variable: the
+// dot product as a compensated float pair (each product's exact residual by
+// FMA, the sums by TwoSum), the correction in float.
 __global__ void __launch_bounds__(kFinThreads)
-cor_backward_finish_kernel(const float *__restrict__ X, int64_t n, const ColStats *__restrict__ st,
-                           const float *__restrict__ W, float *__restrict__ dX) {
-  __shared__ double sh[32];
-  const int64_t j = blockIdx.x;
+cor_backward_finish_kernel(const float *__restrict__ X, int64_t p, int64_t n,
+                           const ColStats *__restrict__ st, const float *__restrict__ W,
+                           float *__restrict__ dX) {
+  const int64_t j = (int64_t(blockIdx.x) * kFinThreads + threadIdx.x) >> 5;
+  if (j >= p) return;  // whole warps
+  const int lane = threadIdx.x & 31;
   const ColStats s = st[j];
-  double d = 0.0;
-  for (int64_t k = threadIdx.x; k < n; k += kFinThreads)
-    d = fma(double(zval(X, st, n, j, k)), double(W[j * n + k]), d);
-  d = block_sum_d(d, sh);
-  for (int64_t k = threadIdx.x; k < n; k += kFinThreads) {
-    float v = 0.f;
-    if (!s.flags) {
-      const double z = (double(X[j * n + k]) - s.mean) * s.inv_norm;
-      v = float((double(W[j * n + k]) - z * d) * s.inv_norm);
+  const float *x = X + j * n;
+  const float *w = W + j * n;
+  float *o = dX + j * n;
+  if (s.flags) {
+    for (int64_t k = lane; k < n; k += 32) o[k] = 0.f;
+    return;
+  }
+  const Centerer cen(s);
+  const float inv = float(s.inv_norm);
+  float hi = 0.f, lo = 0.f;
+  auto acc = [&](float xv, float wv) {
+    const float z = cen(xv);
+    const float pr = z * wv;
+    const float pe = fmaf(z, wv, -pr);
+    const float t = hi + pr, bp = t - hi;
+    lo += ((hi - (t - bp)) + (pr - bp)) + pe;
+    hi = t;
+  };
+  const bool v4 = (n & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(w) |
+                                    reinterpret_cast<uintptr_t>(o)) & 15u) == 0;
+  if (v4) {
+    const float4 *x4 = reinterpret_cast<const float4 *>(x);
+    const float4 *w4 = reinterpret_cast<const float4 *>(w);
+    for (int64_t k = lane; k < (n >> 2); k += 32) {
+      const float4 a = x4[k], b = w4[k];
+      acc(a.x, b.x);
+      acc(a.y, b.y);
+      acc(a.z, b.z);
+      acc(a.w, b.w);
     }
-    dX[j * n + k] = v;
+  } else {
+    for (int64_t k = lane; k < n; k += 32) acc(x[k], w[k]);
+  }
+  warp_pair_sum(hi, lo);
+  const float d = hi + lo;
+  if (v4) {
+    const float4 *x4 = reinterpret_cast<const float4 *>(x);
+    const float4 *w4 = reinterpret_cast<const float4 *>(w);
+    float4 *o4 = reinterpret_cast<float4 *>(o);
+    for (int64_t k = lane; k < (n >> 2); k += 32) {
+      const float4 a = x4[k], b = w4[k];
+      float4 r;
+      r.x = fmaf(-cen(a.x), d, b.x) * inv;
+      r.y = fmaf(-cen(a.y), d, b.y) * inv;
+      r.z = fmaf(-cen(a.z), d, b.z) * inv;
+      r.w = fmaf(-cen(a.w), d, b.w) * inv;
+      o4[k] = r;
+    }
+  } else {
+    for (int64_t k = lane; k < n; k += 32) o[k] = fmaf(-cen(x[k]), d, w[k]) * inv;
   }
 }
 
@@ -564,7 +674,7 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
   if (path == GT_GRAM_FP32) {
     GT_TRY(ws_get(WS_SCRATCH0, size_t(p) * size_t(kp) * 4, &pS));
     GT_TRY(ws_get(WS_SCRATCH1, size_t(n) * size_t(kp) * 4, &pZ));
-    sym_operand_kernel<float><<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+    sym_operand_kernel<float><<<dim3(unsigned(kp / 64), unsigned(cdiv(p, 64))), blk, 0, s>>>(
         dG, p, kp, 1, static_cast<float *>(pS));
     zt_operand_kernel<float><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
         dX, p, n, kp, st, 1, static_cast<float *>(pZ));
@@ -587,7 +697,7 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     GT_TRY(ws_get(WS_SCRATCH1, size_t(2) * size_t(n) * size_t(kp) * 2, &pZ));
     auto *Sf = static_cast<float *>(pSf), *Zf = static_cast<float *>(pZf);
     auto *scS = static_cast<float *>(psc), *scZ = scS + p;
-    sym_operand_kernel<float><<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+    sym_operand_kernel<float><<<dim3(unsigned(kp / 64), unsigned(cdiv(p, 64))), blk, 0, s>>>(
         dG, p, kp, 1, Sf);
     zt_operand_kernel<float><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
         dX, p, n, kp, st, 1, Zf);
@@ -603,7 +713,7 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     GT_TRY(ws_get(WS_SCRATCH0, size_t(ns) * size_t(p) * size_t(kp) * 2, &pS));
     GT_TRY(ws_get(WS_SCRATCH1, size_t(ns) * size_t(n) * size_t(kp) * 2, &pZ));
     sym_operand_kernel<__nv_bfloat16>
-        <<<dim3(unsigned(kp / 32), unsigned(cdiv(p, 32))), blk, 0, s>>>(
+        <<<dim3(unsigned(kp / 64), unsigned(cdiv(p, 64))), blk, 0, s>>>(
             dG, p, kp, ns, static_cast<__nv_bfloat16 *>(pS));
     zt_operand_kernel<__nv_bfloat16><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
         dX, p, n, kp, st, ns, static_cast<__nv_bfloat16 *>(pZ));
@@ -611,7 +721,8 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     GT_CUDA(cudaGetLastError());
     GT_TRY(gemm_tc_store(pS, p, pZ, n, kp, ns, W, n, s));
   }
-  cor_backward_finish_kernel<<<unsigned(p), kFinThreads, 0, s>>>(dX, n, st, W, d_dX);
+  cor_backward_finish_kernel<<<unsigned(cdiv(p, kFinThreads / 32)), kFinThreads, 0, s>>>(
+      dX, p, n, st, W, d_dX);
   count_launch();
   GT_CUDA(cudaGetLastError());
   return GT_OK;
