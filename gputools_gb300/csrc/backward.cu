@@ -311,12 +311,16 @@ constexpr int kDbCols = 32;    // points j per shared tile
 // CTA (ib, js): rows i of block ib against points j of split js.  Writes the
 // split's partial sums sum_j W_ij x_j (pacc) and sum_j W_ij (pw), and its
 // partial loss; a second kernel reduces the splits in a fixed order.
+// Every thread reads the same point j at a time (a broadcast), so the point
+// tile needs no padding and is read 16 bytes at a time; 1 / D_ij comes from
+// the hardware reciprocal square root (D_ij = D_ij^2 / D_ij), and the stress
+// sums as a compensated float pair.
 template <int DMAX, int MODE>
 __global__ void __launch_bounds__(kDbRows)
 dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
                      const float *__restrict__ aux, int64_t jchunk, float *__restrict__ pacc,
                      float *__restrict__ pw, double *__restrict__ ploss) {
-  __shared__ float xj[kDbCols][DMAX + 1];
+  __shared__ __align__(16) float xj[kDbCols][DMAX];
   __shared__ float cf[kDbRows][kDbCols + 1];  // G_ij + G_ji, or delta_ij
   __shared__ double sh[kDbRows / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -332,7 +336,7 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
     acc[k] = 0.f;
   }
   float wsum = 0.f;
-  double lsum = 0.0;
+  FloatPairSum lsum;
   for (int64_t j0 = jbeg; j0 < jend; j0 += kDbCols) {
     __syncthreads();
     for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
@@ -368,26 +372,50 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
       const int jmax = (jend - j0 < kDbCols) ? int(jend - j0) : kDbCols;
       for (int jj = 0; jj < jmax; jj++) {
         const int64_t j = j0 + jj;
-        float d2 = 0.f;
+        const float4 *x4 = reinterpret_cast<const float4 *>(&xj[jj][0]);
+        // four partial sums: four short dependency chains instead of one
+        float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
 #pragma unroll
-        for (int k = 0; k < DMAX; k++) {
-          const float t = xi[k] - xj[jj][k];
-          d2 = fmaf(t, t, d2);
+        for (int k = 0; k < DMAX / 4; k++) {
+          const float4 v = x4[k];
+          const float t0 = xi[4 * k] - v.x, t1 = xi[4 * k + 1] - v.y;
+          const float t2 = xi[4 * k + 2] - v.z, t3 = xi[4 * k + 3] - v.w;
+          q0 = fmaf(t0, t0, q0);
+          q1 = fmaf(t1, t1, q1);
+          q2 = fmaf(t2, t2, q2);
+          q3 = fmaf(t3, t3, q3);
         }
+        const float d2 = (q0 + q1) + (q2 + q3);
         if (j == i) continue;
-        const float d = d2 > 0.f ? sqrtf(d2) : 0.f;
-        // coincident points add to the stress but not to the gradient
-        if (MODE == 1 && j > i) lsum += double(d - cf[tid][jj]) * double(d - cf[tid][jj]);
-        if (!(d2 > 0.f)) continue;
-        float w;
-        if (MODE == 0) {
-          w = cf[tid][jj] / d;
-        } else {
-          w = 2.f * (d - cf[tid][jj]) / d;
+        // 1 / d: the reciprocal square root estimate above the normal range's
+        // floor, IEEE operations below it
+        float inv_d = 0.f, d = 0.f;
+        if (d2 >= 1e-30f) {
+          inv_d = rsqrtf(d2);
+          d = d2 * inv_d;
+        } else if (d2 > 0.f) {
+          d = sqrtf(d2);
+          inv_d = 1.f / d;
         }
+        const float c = cf[tid][jj];
+        // coincident points add to the stress but not to the gradient
+        if (MODE == 1 && j > i) {
+          const float e = d - c;
+          const float q = e * e;
+          lsum.add(q);
+          lsum.lo += fmaf(e, e, -q);
+        }
+        if (!(d2 > 0.f)) continue;
+        const float w = MODE == 0 ? c * inv_d : 2.f * (d - c) * inv_d;
         wsum += w;
 #pragma unroll
-        for (int k = 0; k < DMAX; k++) acc[k] = fmaf(w, xj[jj][k], acc[k]);
+        for (int k = 0; k < DMAX / 4; k++) {
+          const float4 v = x4[k];
+          acc[4 * k] = fmaf(w, v.x, acc[4 * k]);
+          acc[4 * k + 1] = fmaf(w, v.y, acc[4 * k + 1]);
+          acc[4 * k + 2] = fmaf(w, v.z, acc[4 * k + 2]);
+          acc[4 * k + 3] = fmaf(w, v.w, acc[4 * k + 3]);
+        }
       }
     }
   }
@@ -399,9 +427,9 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
     pw[js * n + i] = wsum;
   }
   if (MODE == 1) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if (lane == 0) sh[warp] = lsum;
+    float lh = lsum.hi, ll = lsum.lo;
+    warp_pair_sum(lh, ll);
+    if (lane == 0) sh[warp] = double(lh) + double(ll);
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
@@ -623,7 +651,29 @@ int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *au
                          double *loss, cudaStream_t s) {
   if (dim > 64) return dist_backward_tc<MODE>(X, n, dim, aux, dX, loss, s);
   const int64_t ib = cdiv(n, kDbRows);
-  int64_t nsplit = cdiv(int64_t(sm_count()) * 4, ib);
+  // one wave: as many splits as the resident CTAs (SMs x CTAs per SM) allow
+  int per_sm = 0;
+  if (dim <= 16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<16, MODE>, kDbRows, 0);
+  else if (dim <= 32)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<32, MODE>, kDbRows, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<64, MODE>, kDbRows, 0);
+  if (per_sm < 1) per_sm = 1;
+  // the split count whose CTAs fill whole waves best (up to four waves; more
+  // splits only when they fill clearly better)
+  const int64_t slots = int64_t(sm_count()) * per_sm;
+  int64_t nsplit = 1;
+  double best_fill = 0.0;
+  for (int64_t w = 1; w <= 4; w++) {
+    const int64_t ns = w * slots / ib;
+    if (ns < 1) continue;
+    const double fill = double(ns * ib) / double(w * slots);
+    if (fill > best_fill + 0.02) {
+      best_fill = fill;
+      nsplit = ns;
+    }
+  }
   const int64_t max_split = cdiv(n, kDbCols);
   if (nsplit > max_split) nsplit = max_split;
   if (nsplit < 1) nsplit = 1;
