@@ -85,7 +85,8 @@ SIGNATURES = {
 class CorProblem(ctypes.Structure):
     """gt_cor_problem: one cor(x) of a batch (device pointers)."""
     _fields_ = [("X", ctypes.c_void_p), ("p", ctypes.c_int64), ("n", ctypes.c_int64),
-                ("corr", ctypes.c_void_p), ("ts", ctypes.c_void_p), ("pairs", ctypes.c_void_p)]
+                ("corr", ctypes.c_void_p), ("ts", ctypes.c_void_p), ("pairs", ctypes.c_void_p),
+                ("ld", ctypes.c_int64)]
 
 
 class KendallProblem(ctypes.Structure):

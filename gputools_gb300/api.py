@@ -459,10 +459,14 @@ class BatchPlan:
     """A batch of independent cor(x) problems (pearson or kendall) prepared
     once and replayed from a CUDA graph.  Inputs are variable-major CUDA
     float32 tensors (p, n); outputs are allocated here.  `launch()`
-    recomputes every output from the current contents of the inputs."""
+    recomputes every output from the current contents of the inputs.
+
+    Pearson outputs are p x p views of pitched storage (rows a multiple of 8
+    floats apart, so every row starts on a 32-byte sector) unless
+    `pitched=False`, which allocates contiguous p x p tensors."""
 
     def __init__(self, inputs, method: str = "pearson", autotune: bool = False,
-                 graph: bool = True):
+                 graph: bool = True, pitched: bool = True):
         import torch
         self.method = method
         self.inputs = list(inputs)
@@ -474,11 +478,12 @@ class BatchPlan:
             arr = (_lib.CorProblem * max(1, len(self.inputs)))()
             for i, x in enumerate(self.inputs):
                 p, n = x.shape
-                o = {k: torch.empty((p, p), dtype=torch.float32, device=x.device)
+                ld = (p + 7) // 8 * 8 if pitched else p
+                o = {k: torch.empty((p, ld), dtype=torch.float32, device=x.device)[:, :p]
                      for k in ("corr", "ts", "pairs")}
                 self.outputs.append(o)
                 arr[i] = _lib.CorProblem(x.data_ptr(), p, n, o["corr"].data_ptr(),
-                                         o["ts"].data_ptr(), o["pairs"].data_ptr())
+                                         o["ts"].data_ptr(), o["pairs"].data_ptr(), ld)
             check(lib.gt_pmcc_batch_plan_create(arr, len(self.inputs), flags, ctypes.byref(handle)))
         elif method == "kendall":
             arr = (_lib.KendallProblem * max(1, len(self.inputs)))()

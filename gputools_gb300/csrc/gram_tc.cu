@@ -1555,6 +1555,9 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     if (q.p == 0) continue;
     if (!q.X) return fail(GT_EINVAL, "problem %lld: null input", (long long)i);
     if (q.n == 0) return fail(GT_EINVAL, "problem %lld: no observations", (long long)i);
+    if (q.ld != 0 && q.ld < q.p)
+      return fail(GT_EINVAL, "problem %lld: output row stride %lld below p", (long long)i,
+                  (long long)q.ld);
     PearsonBatchInput b;
     b.X = q.X;
     b.p = q.p;
@@ -1586,7 +1589,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     GT_TRY(make_plane_map(&d.map_b, planes + b.plane_off, b.p, b.kpad, nsplit, kBN, bk, f16));
     d.ts = make_tiles(b.p, b.p, kUpper, band_group(int64_t(kBN) * b.kpad * 2 * nsplit));
     d.nk = b.kpad / bk;
-    d.fin = PearsonFinish{q.corr, q.ts, q.pairs, b.p, b.p, b.p, float(b.n),
+    d.fin = PearsonFinish{q.corr, q.ts, q.pairs, q.ld != 0 ? q.ld : b.p, b.p, b.p, float(b.n),
                           std::sqrt(float(b.n) - 2.f), gscale, 1};
     descs.push_back(d);
     tile_prefix.push_back(tile_prefix.back() + d.ts.ntiles);

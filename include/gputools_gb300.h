@@ -303,11 +303,16 @@ void RgpuMdsStress(const float *points, const int *numPoints, const int *dim,
 /* ---- batches (no counterpart in the reference) --------------------------- */
 
 /* One Pearson problem of a batch: cor(x) of a variable-major p x n device
- * matrix, outputs p x p on the device (any may be NULL). */
+ * matrix, outputs p x p on the device (any may be NULL), rows `ld` floats
+ * apart (ld >= p; 0 means p).  A row stride that is a multiple of 8 floats
+ * keeps every row on 32-byte sectors: with ld = p and p not a multiple of 8
+ * the rows straddle sectors, and the partially written sectors cost the
+ * output stores up to half their rate. */
 typedef struct gt_cor_problem {
   const float *X;
   int64_t p, n;
   float *corr, *ts, *pairs;
+  int64_t ld;
 } gt_cor_problem;
 
 /* One Kendall problem of a batch: tau-b of cor(x), out p x p doubles. */

@@ -71,6 +71,45 @@ def test_pearson_batch_matches_single_and_oracle(gpu, oracle_mod, gram_path, gra
             assert np.allclose(corr, single, atol=1e-6, equal_nan=True)
 
 
+def test_pearson_batch_pitched_outputs(gpu):
+    """Pitched outputs (rows a multiple of 8 floats apart) hold the same
+    values as contiguous ones and leave the padding columns alone; a stride
+    below p is refused."""
+    import ctypes
+    import torch
+    import gputools_gb300 as g
+    from gputools_gb300 import _lib
+    rng = np.random.default_rng(12)
+    xs = [torch.from_numpy(rng.standard_normal((p, 90)).astype(np.float32)).cuda()
+          for p in (1, 7, 129, 300, 515)]
+    with g.BatchPlan(xs, "pearson", pitched=False) as plain:
+        want = [{k: v.clone() for k, v in o.items()} for o in plain.launch()]
+    with g.BatchPlan(xs, "pearson") as plan:
+        bases = []
+        for x, o in zip(xs, plan.outputs):
+            p = x.shape[0]
+            ld = (p + 7) // 8 * 8
+            assert o["corr"].shape == (p, p) and o["corr"].stride() == (ld, 1)
+            base = {k: torch.as_strided(v, (p, ld), (ld, 1)) for k, v in o.items()}
+            for b in base.values():
+                b.fill_(-7.0)
+            bases.append(base)
+        outs = plan.launch()
+        torch.cuda.synchronize()
+        for x, o, w, base in zip(xs, outs, want, bases):
+            p = x.shape[0]
+            for k in ("corr", "ts", "pairs"):
+                assert torch.equal(o[k], w[k]) or torch.allclose(o[k], w[k], equal_nan=True, atol=0)
+                assert bool((base[k][:, p:] == -7.0).all())
+    x = xs[2]
+    out = torch.empty((129, 129), device="cuda")
+    arr = (_lib.CorProblem * 1)()
+    arr[0] = _lib.CorProblem(x.data_ptr(), 129, 90, out.data_ptr(), 0, 0, 100)
+    h = ctypes.c_void_p()
+    assert g.load().gt_pmcc_batch_plan_create(arr, 1, 0, ctypes.byref(h)) != 0
+    assert b"stride" in g.load().gt_last_error()
+
+
 def test_pearson_batch_replay_sees_new_inputs(gpu, oracle_mod):
     import torch
     import gputools_gb300 as g
