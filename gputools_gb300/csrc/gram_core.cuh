@@ -242,6 +242,14 @@ struct PearsonFinish {
     block(r, c0, ctx);
   }
 
+  // Whether the block of rows rbase .. rbase + 31, columns c0 .. c0 + 31 has
+  // anything to write: not past the problem's edge and (symmetric) not
+  // entirely below the diagonal, whose entries the mirror stores of other
+  // blocks write.
+  __device__ __forceinline__ bool block_live(int64_t rbase, int64_t c0) const {
+    return c0 < nc && rbase < nr && !(symmetric && rbase > c0 + 31);
+  }
+
   // A block staged in the warp's tile: wsm[lane * 33 + j] = entry (r, c0 + j).
   // Both orientations read the tile (the padding keeps either read free of
   // bank conflicts), so the body is compact: loops of four, not unrolled

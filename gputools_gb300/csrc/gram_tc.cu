@@ -827,6 +827,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
           // instruction cache once the epilogue bounds the kernel (small n).
 #pragma unroll 1
           for (int i = 0; i < 4; i++) {
+            if (!fin.block_live(r - lane, col + 32 * i)) continue;
             switch (i) {
               case 0: stage_block<0>(acc, ctx.wsm); break;
               case 1: stage_block<1>(acc, ctx.wsm); break;
