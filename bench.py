@@ -912,9 +912,25 @@ def run_batches(g, stream, dev, k):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / k
+    peaks, peaks_kind = load_peaks()
+    # algorithmic bytes: r, t and pairs written (12 bytes per entry), the
+    # inputs read, the two f16 operand planes written and read once
+    kpad = (ns.astype(np.float64) + 63) // 64 * 64
+    pf = ps.astype(np.float64)
+    nbytes = 12 * entries + 4 * float(np.sum(pf * ns)) + 8 * float(np.sum(pf * kpad))
+    out_gbs = nbytes / (ms * 1e-3) / 1e9
     res["pearson_2000"] = {"ms": ms, "entries": entries, "entries_per_s": entries / (ms * 1e-3),
                            "useful_tflops": useful / (ms * 1e-3) / 1e12, "plan": plan.describe(),
-                           "plan_build_s": build_s, "launches_per_step": "1 graph"}
+                           "plan_build_s": build_s, "launches_per_step": "1 graph",
+                           "outputs": "p x p views of pitched storage (rows a multiple of 8 "
+                                      "floats apart)",
+                           "roofline": {"bound": "hbm", "achieved": out_gbs,
+                                        "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                        "frac": out_gbs / peaks["hbm_gbs"],
+                                        "peak_kind": f"{peaks_kind} copy bandwidth",
+                                        "bytes": "outputs (12 B per entry), inputs, operand "
+                                                 "planes written and read once",
+                                        "algorithmic_bytes": nbytes}}
     plan.close()
     del xs
     torch.cuda.empty_cache()
