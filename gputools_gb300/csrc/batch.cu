@@ -223,7 +223,7 @@ struct TileConfig {
 };
 
 const TileConfig kX3Configs[] = {{64, 256, "bk64-chunk256"}, {32, 256, "bk32-chunk256"},
-                                 {64, 512, "bk64-chunk512"}};
+                                 {64, 512, "bk64-chunk512"}, {32, 512, "bk32-chunk512"}};
 const TileConfig kX6Configs[] = {{32, 256, "bk32-chunk256"}, {32, 128, "bk32-chunk128"}};
 
 std::string cache_path() {

@@ -451,6 +451,7 @@ struct PearsonBatchProblem {  // aligned as CUtensorMap
 // entry {problem, row0, col0, k-blocks}, so a lookup is one 16-byte load that
 // the cursor issues a tile ahead.
 struct PearsonBatchWork {
+  static constexpr bool kWideEpi = true;  // sixteen epilogue warps with 32-wide K blocks
   const PearsonBatchProblem *probs;
   const int4 *table;     // the CTAs' tile lists, one after the other
   const int64_t *cta_off;  // CTA c's tiles: table[cta_off[c] .. cta_off[c + 1])

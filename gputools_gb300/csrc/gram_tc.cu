@@ -571,10 +571,12 @@ struct StoreFinish {
 // columns' norms in shared memory.  The chunked kernels keep 8 warps of 128
 // columns (their running sums need the registers) and give the shared
 // memory to the stages.
-template <int KIND, int BK, bool LISTS>
+// WIDE: sixteen epilogue warps of 64 columns for a chunked kernel (the
+// Pearson finish, whose stores are latency-bound at two warps per scheduler).
+template <int KIND, int BK, bool LISTS, bool WIDE = false>
 struct TcCfg {
   static constexpr int NSPLIT = tc::Kind<KIND>::NSPLIT;
-  static constexpr int EPI = LISTS ? 16 : 8;                 // epilogue warps
+  static constexpr int EPI = (LISTS || WIDE) ? 16 : 8;       // epilogue warps
   static constexpr int THREADS = 64 + 32 * EPI;              // + producer and MMA warps
   static constexpr int COLS = 4 * kBN / EPI;                 // columns per epilogue warp
   static constexpr int ROW_BYTES = BK * 2;                // 128 or 64
@@ -636,20 +638,43 @@ struct EuclidLineWork {
 
 // Block I (columns 32 I .. 32 I + 31) of a lane's running sums into the
 // warp's staging tile, row = lane.
-template <int I>
-__device__ __forceinline__ void stage_block(const float (&acc)[128], float *wsm) {
+template <int I, int N>
+__device__ __forceinline__ void stage_block(const float (&acc)[N], float *wsm) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < 32; j++) wsm[lane * 33 + j] = acc[32 * I + j];
 }
 
+// The finish a work source applies.
+template <class Work>
+using FinOf = std::decay_t<decltype(std::declval<const Work &>().finish(std::declval<const TileRef &>()))>;
+
+// Whether a work source asks for sixteen epilogue warps (Work::kWideEpi).
+template <class Work, class = void>
+struct wide_epi : std::false_type {};
+template <class Work>
+struct wide_epi<Work, std::void_t<decltype(Work::kWideEpi)>>
+    : std::integral_constant<bool, Work::kWideEpi> {};
+
+// The configuration a kernel runs: chunked kernels whose work source asks for
+// it and whose finish takes staged blocks run sixteen epilogue warps where the
+// shared memory allows it (32-wide K blocks).  Batches ask for it: their
+// outputs are pitched, and on sector-aligned rows the extra warps hide the
+// store latency (single problems with a row stride off the 32-byte sectors
+// store slower with them).
 template <int KIND, int BK, bool CHUNKED, class Work>
-__global__ void __launch_bounds__(TcCfg<KIND, BK, !CHUNKED>::THREADS, 1)
+using KernelCfg = TcCfg<KIND, BK, !CHUNKED,
+                        CHUNKED && BK == 32 && wide_epi<Work>::value &&
+                            staged_block<FinOf<Work>>::value>;
+
+template <int KIND, int BK, bool CHUNKED, class Work>
+__global__ void __launch_bounds__(KernelCfg<KIND, BK, CHUNKED, Work>::THREADS, 1)
 gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg wc) {
-  using C = TcCfg<KIND, BK, !CHUNKED>;
+  using C = KernelCfg<KIND, BK, CHUNKED, Work>;
   if (work.skip()) return;  // a gated launch whose gate is closed: before any setup
   constexpr int NSPLIT = C::NSPLIT;
-  static_assert(!CHUNKED || C::COLS == 128, "chunked sums hold 128 columns per warp");
+  static_assert(!CHUNKED || C::COLS == 128 || C::COLS == 64,
+                "chunked sums hold 128 or 64 columns per warp");
   static_assert(CHUNKED || C::COLS == kEuclidCols, "the list kernels hold 64 columns per warp");
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -794,9 +819,9 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
       fin.begin_tile(r, ctx);
       if constexpr (CHUNKED) {
         const int64_t nch = (ref.nk + ckb - 1) / ckb;
-        float acc[128];
+        float acc[C::COLS];
 #pragma unroll
-        for (int j = 0; j < 128; j++) acc[j] = 0.f;
+        for (int j = 0; j < C::COLS; j++) acc[j] = 0.f;
         for (int64_t ch = 0; ch < nch; ch++, cc++) {
           const int buf = int(cc & 1);
           const uint32_t ause = uint32_t(cc >> 1);
@@ -809,7 +834,7 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
           const uint32_t tb =
               tmem_base + uint32_t(buf * kBN + part * C::COLS) + (uint32_t(q * 32) << 16);
 #pragma unroll
-          for (int i = 0; i < 8; i++) {
+          for (int i = 0; i < C::COLS / 16; i++) {
             float g[16];
             tc::tmem_ld16(tb + uint32_t(16 * i), g);
 #pragma unroll
@@ -826,20 +851,25 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
           // in the warp's tile first: four inlined copies outgrow the
           // instruction cache once the epilogue bounds the kernel (small n).
 #pragma unroll 1
-          for (int i = 0; i < 4; i++) {
+          for (int i = 0; i < C::COLS / 32; i++) {
             if (!fin.block_live(r - lane, col + 32 * i)) continue;
-            switch (i) {
-              case 0: stage_block<0>(acc, ctx.wsm); break;
-              case 1: stage_block<1>(acc, ctx.wsm); break;
-              case 2: stage_block<2>(acc, ctx.wsm); break;
-              default: stage_block<3>(acc, ctx.wsm); break;
+            if constexpr (C::COLS == 64) {
+              if (i == 0) stage_block<0>(acc, ctx.wsm);
+              else stage_block<1>(acc, ctx.wsm);
+            } else {
+              switch (i) {
+                case 0: stage_block<0>(acc, ctx.wsm); break;
+                case 1: stage_block<1>(acc, ctx.wsm); break;
+                case 2: stage_block<2>(acc, ctx.wsm); break;
+                default: stage_block<3>(acc, ctx.wsm); break;
+              }
             }
             __syncwarp();
             fin.block(r, col + 32 * i, ctx);
           }
         } else {
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
+          for (int i = 0; i < C::COLS / 32; i++) {
             float g[32];
 #pragma unroll
             for (int j = 0; j < 32; j++) g[j] = acc[32 * i + j];
@@ -1216,7 +1246,7 @@ int make_plane_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kpa
 template <int KIND, int BK, bool CHUNKED, class W>
 int launch_work(const W &w, int64_t ntiles, int64_t ckb, const char *prof_name,
                 cudaStream_t s) {
-  using C = TcCfg<KIND, BK, !CHUNKED>;
+  using C = KernelCfg<KIND, BK, CHUNKED, W>;
   if (ntiles == 0) return GT_OK;
   tc::WaitCfg wc;
   GT_TRY(make_wait_cfg(&wc));
@@ -1697,28 +1727,29 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
           <<<unsigned(blocks), 256, 0, s>>>(in, vp, nprob, total_vars, planes);
     count_launch();
     if (ncta == 0) return GT_OK;
-    auto launch = [&](auto kern, int smem) -> int {
+    auto launch = [&](auto kern, int threads, int smem) -> int {
       GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      kern<<<unsigned(ncta), TcCfg<tc::KIND_BF16X3, 32, false>::THREADS, smem, s>>>(w, ckb, wc);
+      kern<<<unsigned(ncta), threads, smem, s>>>(w, ckb, wc);
       return GT_OK;
     };
+    using W = PearsonBatchWork;
     if (kind == tc::KIND_BF16X6) {
-      GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X6, 32, true, PearsonBatchWork>,
-                    TcCfg<tc::KIND_BF16X6, 32, false>::SMEM));
+      using C = KernelCfg<tc::KIND_BF16X6, 32, true, W>;
+      GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X6, 32, true, W>, C::THREADS, C::SMEM));
     } else if (kind == tc::KIND_F16X3) {
+      using C32 = KernelCfg<tc::KIND_F16X3, 32, true, W>;
+      using C64 = KernelCfg<tc::KIND_F16X3, 64, true, W>;
       if (BKc == 32)
-        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 32, true, PearsonBatchWork>,
-                      TcCfg<tc::KIND_F16X3, 32, false>::SMEM));
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 32, true, W>, C32::THREADS, C32::SMEM));
       else
-        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 64, true, PearsonBatchWork>,
-                      TcCfg<tc::KIND_F16X3, 64, false>::SMEM));
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_F16X3, 64, true, W>, C64::THREADS, C64::SMEM));
     } else {
+      using C32 = KernelCfg<tc::KIND_BF16X3, 32, true, W>;
+      using C64 = KernelCfg<tc::KIND_BF16X3, 64, true, W>;
       if (BKc == 32)
-        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 32, true, PearsonBatchWork>,
-                      TcCfg<tc::KIND_BF16X3, 32, false>::SMEM));
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 32, true, W>, C32::THREADS, C32::SMEM));
       else
-        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 64, true, PearsonBatchWork>,
-                      TcCfg<tc::KIND_BF16X3, 64, false>::SMEM));
+        GT_TRY(launch(gram_tc_kernel<tc::KIND_BF16X3, 64, true, W>, C64::THREADS, C64::SMEM));
     }
     count_launch();
     GT_CUDA(cudaGetLastError());
