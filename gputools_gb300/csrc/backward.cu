@@ -307,10 +307,39 @@ struct OutStore {
 constexpr int kDbRows = 128;   // rows i per CTA (one per thread)
 constexpr int kDbCols = 32;    // points j per shared tile
 
+// Asynchronous 4-byte copy global -> shared (cp.async); bytes = 0 fills zero.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, int bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Shared memory of dist_backward_kernel (floats, two buffers of each tile):
+// the point tile [kDbCols][DMAX], the coefficients [kDbRows][kDbCols + 1]
+// (G_ij, or delta_ij from either side of the diagonal) and, for mode 0, the
+// transposed coefficients [kDbCols][kDbRows + 1] (G_ji).
+template <int DMAX, int MODE>
+struct DbSmem {
+  static constexpr int XJ = kDbCols * DMAX;
+  static constexpr int CFA = kDbRows * (kDbCols + 1);
+  static constexpr int CFB = MODE == 0 ? kDbCols * (kDbRows + 1) : 0;
+  static constexpr int FLOATS = 2 * (XJ + CFA + CFB);  // even: the doubles after it align
+  static constexpr int BYTES = FLOATS * 4 + (kDbRows / 32) * 8;
+};
+
 // mode 0: W_ij = (G_ij + G_ji) / D_ij ; mode 1: MDS, W_ij = 2 (D_ij - delta_ij) / D_ij
 // CTA (ib, js): rows i of block ib against points j of split js.  Writes the
 // split's partial sums sum_j W_ij x_j (pacc) and sum_j W_ij (pw), and its
 // partial loss; a second kernel reduces the splits in a fixed order.
+// The tiles of 32 points and their coefficients are double-buffered: the
+// copies of the next tile (cp.async) run while the current one is used.
 // Every thread reads the same point j at a time (a broadcast), so the point
 // tile needs no padding and is read 16 bytes at a time; 1 / D_ij comes from
 // the hardware reciprocal square root (D_ij = D_ij^2 / D_ij), and the stress
@@ -320,15 +349,59 @@ __global__ void __launch_bounds__(kDbRows)
 dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
                      const float *__restrict__ aux, int64_t jchunk, float *__restrict__ pacc,
                      float *__restrict__ pw, double *__restrict__ ploss) {
-  __shared__ __align__(16) float xj[kDbCols][DMAX];
-  __shared__ float cf[kDbRows][kDbCols + 1];  // G_ij + G_ji, or delta_ij
-  __shared__ double sh[kDbRows / 32];
+  using L = DbSmem<DMAX, MODE>;
+  extern __shared__ __align__(16) float dsm[];
+  float *xj = dsm;                      // [2][kDbCols][DMAX]
+  float *cfa = xj + 2 * L::XJ;          // [2][kDbRows][kDbCols + 1]
+  float *cfb = cfa + 2 * L::CFA;        // [2][kDbCols][kDbRows + 1] (mode 0)
+  double *sh = reinterpret_cast<double *>(dsm + L::FLOATS);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i0 = int64_t(blockIdx.x) * kDbRows;
   const int64_t i = i0 + tid;
   const int64_t js = blockIdx.y;
   const int64_t jbeg = js * jchunk;
   const int64_t jend = (jbeg + jchunk < n) ? jbeg + jchunk : n;
+  // copies of the tile of points jt .. jt + 31 into buffer b (one commit group)
+  auto issue = [&](int b, int64_t jt) {
+    float *xb = xj + b * L::XJ;
+    for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
+      const int jj = e / DMAX, k = e - jj * DMAX;
+      const int64_t j = jt + jj;
+      const bool ok = j < jend && k < dim;
+      cp_async4(xb + e, ok ? X + j * dim + k : X, ok ? 4 : 0);
+    }
+    float *ca = cfa + b * L::CFA;
+    if (MODE == 0) {
+      float *cb = cfb + b * L::CFB;
+      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
+        const int64_t gi = i0 + ii, gj = jt + lane;
+        const bool ok = gi < n && gj < jend;
+        cp_async4(ca + ii * (kDbCols + 1) + lane, ok ? aux + gi * n + gj : aux, ok ? 4 : 0);
+      }
+      for (int jj = 0; jj < kDbCols; jj++) {
+        const int64_t gj = jt + jj;
+        const bool ok = gj < jend && i < n;
+        cp_async4(cb + jj * (kDbRows + 1) + tid, ok ? aux + gj * n + i : aux, ok ? 4 : 0);
+      }
+    } else {
+      // delta in R dist layout: (a > b) at n*b - b*(b+1)/2 + a - b - 1; each
+      // cell comes from exactly one side of the diagonal (the diagonal and the
+      // cells past the tile are never read)
+      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
+        const int64_t gi = i0 + ii, gj = jt + lane;
+        if (gi < n && gj < jend && gj > gi)
+          cp_async4(ca + ii * (kDbCols + 1) + lane, aux + (n * gi - gi * (gi + 1) / 2 + gj - gi - 1),
+                    4);
+      }
+      for (int jj = 0; jj < kDbCols; jj++) {
+        const int64_t gj = jt + jj;
+        if (gj < jend && i < n && i > gj)
+          cp_async4(ca + tid * (kDbCols + 1) + jj, aux + (n * gj - gj * (gj + 1) / 2 + i - gj - 1),
+                    4);
+      }
+    }
+    cp_async_commit();
+  };
   float xi[DMAX], acc[DMAX];
 #pragma unroll
   for (int k = 0; k < DMAX; k++) {
@@ -337,42 +410,24 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
   }
   float wsum = 0.f;
   FloatPairSum lsum;
-  for (int64_t j0 = jbeg; j0 < jend; j0 += kDbCols) {
-    __syncthreads();
-    for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
-      const int jj = e / DMAX, k = e - jj * DMAX;
-      const int64_t j = j0 + jj;
-      xj[jj][k] = (j < jend && k < dim) ? X[j * dim + k] : 0.f;
-    }
-    if (MODE == 0) {
-      // rows i, columns j: lanes along j (row-contiguous)
-      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
-        const int64_t gi = i0 + ii, gj = j0 + lane;
-        cf[ii][lane] = (gi < n && gj < jend) ? aux[gi * n + gj] : 0.f;
-      }
-      __syncthreads();
-      // add G_ji: rows j, lanes along i
-      for (int jj = 0; jj < kDbCols; jj++) {
-        const int64_t gj = j0 + jj;
-        if (gj < jend && i < n) cf[tid][jj] += aux[gj * n + i];
-      }
+  if (jbeg < jend) issue(0, jbeg);
+  int b = 0;
+  for (int64_t j0 = jbeg; j0 < jend; j0 += kDbCols, b ^= 1) {
+    if (j0 + kDbCols < jend) {
+      issue(b ^ 1, j0 + kDbCols);  // the other buffer: its last readers passed the barrier below
+      cp_async_wait<1>();
     } else {
-      // delta in R dist layout: (a > b) at n*b - b*(b+1)/2 + a - b - 1
-      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
-        const int64_t gi = i0 + ii, gj = j0 + lane;
-        if (gi < n && gj < jend && gj > gi) cf[ii][lane] = aux[n * gi - gi * (gi + 1) / 2 + gj - gi - 1];
-      }
-      for (int jj = 0; jj < kDbCols; jj++) {
-        const int64_t gj = j0 + jj;
-        if (gj < jend && i < n && i > gj) cf[tid][jj] = aux[n * gj - gj * (gj + 1) / 2 + i - gj - 1];
-      }
+      cp_async_wait<0>();
     }
-    __syncthreads();
+    __syncthreads();  // tile b complete and visible
+    const float *xb = xj + b * L::XJ;
+    const float *ca = cfa + b * L::CFA;
+    const float *cb = cfb + b * L::CFB;
     if (i < n) {
       const int jmax = (jend - j0 < kDbCols) ? int(jend - j0) : kDbCols;
       for (int jj = 0; jj < jmax; jj++) {
         const int64_t j = j0 + jj;
-        const float4 *x4 = reinterpret_cast<const float4 *>(&xj[jj][0]);
+        const float4 *x4 = reinterpret_cast<const float4 *>(xb + jj * DMAX);
         // four partial sums: four short dependency chains instead of one
         float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
 #pragma unroll
@@ -397,7 +452,8 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
           d = sqrtf(d2);
           inv_d = 1.f / d;
         }
-        const float c = cf[tid][jj];
+        const float c = MODE == 0 ? ca[tid * (kDbCols + 1) + jj] + cb[jj * (kDbRows + 1) + tid]
+                                  : ca[tid * (kDbCols + 1) + jj];
         // coincident points add to the stress but not to the gradient
         if (MODE == 1 && j > i) {
           const float e = d - c;
@@ -418,6 +474,7 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
         }
       }
     }
+    __syncthreads();  // every thread is done with tile b before it is refilled
   }
   if (i < n) {
     float *pa = pacc + (js * n + i) * dim;
@@ -651,14 +708,18 @@ int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *au
                          double *loss, cudaStream_t s) {
   if (dim > 64) return dist_backward_tc<MODE>(X, n, dim, aux, dX, loss, s);
   const int64_t ib = cdiv(n, kDbRows);
-  // one wave: as many splits as the resident CTAs (SMs x CTAs per SM) allow
+  // the kernel for the dimension, its shared memory, and the CTAs per SM
+  auto pick = [&](auto kern, int bytes) -> int {
+    int per = 0;
+    if (bytes > 48 * 1024)
+      GT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    GT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kDbRows, bytes));
+    return per;
+  };
   int per_sm = 0;
-  if (dim <= 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<16, MODE>, kDbRows, 0);
-  else if (dim <= 32)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<32, MODE>, kDbRows, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dist_backward_kernel<64, MODE>, kDbRows, 0);
+  if (dim <= 16) per_sm = pick(dist_backward_kernel<16, MODE>, DbSmem<16, MODE>::BYTES);
+  else if (dim <= 32) per_sm = pick(dist_backward_kernel<32, MODE>, DbSmem<32, MODE>::BYTES);
+  else per_sm = pick(dist_backward_kernel<64, MODE>, DbSmem<64, MODE>::BYTES);
   if (per_sm < 1) per_sm = 1;
   // the split count whose CTAs fill whole waves best (up to four waves; more
   // splits only when they fill clearly better)
@@ -688,11 +749,14 @@ int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *au
   float *fa = static_cast<float *>(pa), *fw = static_cast<float *>(pw);
   double *dl = static_cast<double *>(pl);
   if (dim <= 16)
-    dist_backward_kernel<16, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+    dist_backward_kernel<16, MODE><<<grid, kDbRows, DbSmem<16, MODE>::BYTES, s>>>(
+        X, n, dim, aux, jchunk, fa, fw, dl);
   else if (dim <= 32)
-    dist_backward_kernel<32, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+    dist_backward_kernel<32, MODE><<<grid, kDbRows, DbSmem<32, MODE>::BYTES, s>>>(
+        X, n, dim, aux, jchunk, fa, fw, dl);
   else
-    dist_backward_kernel<64, MODE><<<grid, kDbRows, 0, s>>>(X, n, dim, aux, jchunk, fa, fw, dl);
+    dist_backward_kernel<64, MODE><<<grid, kDbRows, DbSmem<64, MODE>::BYTES, s>>>(
+        X, n, dim, aux, jchunk, fa, fw, dl);
   int64_t g = cdiv(n * dim, 256);
   if (g > int64_t(sm_count()) * 8) g = int64_t(sm_count()) * 8;
   dist_backward_reduce_kernel<<<unsigned(g), 256, 0, s>>>(X, n, dim, nsplit, fa, fw, dX);
