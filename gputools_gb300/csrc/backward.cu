@@ -514,12 +514,25 @@ __global__ void dist_backward_reduce_kernel(const float *__restrict__ X, int64_t
   }
 }
 
-__global__ void loss_reduce_kernel(const double *__restrict__ ploss, int64_t count,
-                                   double *__restrict__ loss) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double t = 0.0;
-    for (int64_t i = 0; i < count; i++) t += ploss[i];
-    *loss = t;
+// The partial losses summed by one CTA in a fixed order (thread t takes
+// t, t + 1024, ...; then a butterfly in each warp and across the warps), so
+// the result does not depend on timing.
+constexpr int kLossThreads = 1024;
+__global__ void __launch_bounds__(kLossThreads)
+loss_reduce_kernel(const double *__restrict__ ploss, int64_t count, double *__restrict__ loss) {
+  __shared__ double sh[kLossThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double t = 0.0;
+  for (int64_t i = threadIdx.x; i < count; i += kLossThreads) t += ploss[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) sh[warp] = t;
+  __syncthreads();
+  if (warp == 0) {
+    t = sh[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) *loss = t;
   }
 }
 
@@ -576,43 +589,51 @@ __global__ void adj_points_kernel(const float *__restrict__ X, int64_t n, int64_
 // W_ij with D_ij = 0 are 0.  Per 32 x 32 tile: the rows' partial sums of W
 // (rsum[i * nbj + jb]) and, for MODE 1, the tile's part of the stress
 // sum_{i<j} (D - delta)^2 (lpart[ib * nbj + jb]); both are reduced in a fixed
-// order afterwards.
+// order afterwards.  G^T, and delta below the diagonal (stored by column
+// there), go through shared memory so that every global read is coalesced;
+// the stress sums as compensated float pairs.
 template <int MODE>
 __global__ void adj_weight_kernel(const float *__restrict__ D, const float *__restrict__ aux,
                                   int64_t n, int64_t kp, __nv_bfloat16 *__restrict__ Wp,
                                   float *__restrict__ rsum, double *__restrict__ lpart) {
-  __shared__ float gt[32][33];  // G^T tile: gt[jj][ii] = G[j][i]
+  // MODE 0: tt[jj][ii] = G[j][i]; MODE 1: tt[ii][jj] = delta(i, j), i != j
+  __shared__ float tt[32][33];
   __shared__ double lsh[8];
   const int64_t i0 = int64_t(blockIdx.y) * 32, j0 = int64_t(blockIdx.x) * 32;
   const int tx = threadIdx.x, ty0 = threadIdx.y;
   const int64_t nbj = gridDim.x;
-  if (MODE == 0) {
-    for (int ty = ty0; ty < 32; ty += 8) {
+  for (int ty = ty0; ty < 32; ty += 8) {
+    if (MODE == 0) {
       const int64_t j = j0 + ty, i = i0 + tx;
-      gt[ty][tx] = (j < n && i < n) ? aux[j * n + i] : 0.f;
+      tt[ty][tx] = (j < n && i < n) ? aux[j * n + i] : 0.f;
+    } else {
+      // above the diagonal: row i of the dist layout, consecutive j
+      const int64_t i = i0 + ty, j = j0 + tx;
+      if (i < n && j < n && i < j) tt[ty][tx] = aux[n * i - i * (i + 1) / 2 + j - i - 1];
+      // below: delta(i, j) = delta(j, i), row j of the dist layout, consecutive i
+      const int64_t i2 = i0 + tx, j2 = j0 + ty;
+      if (i2 < n && j2 < n && i2 > j2) tt[tx][ty] = aux[n * j2 - j2 * (j2 + 1) / 2 + i2 - j2 - 1];
     }
-    __syncthreads();
   }
+  __syncthreads();
   const int64_t plane = n * kp;
-  double lsum = 0.0;
+  FloatPairSum lsum;
   for (int ty = ty0; ty < 32; ty += 8) {
     const int64_t i = i0 + ty, j = j0 + tx;
     float w = 0.f;
     if (i < n && j < n && i != j) {
       const float d = D[i * n + j];
-      if (d > 0.f) {
-        if (MODE == 0) {
-          w = (aux[i * n + j] + gt[tx][ty]) / d;
-        } else {
-          const int64_t a = i > j ? i : j, b = i > j ? j : i;
-          const float del = aux[n * b - b * (b + 1) / 2 + a - b - 1];
-          w = 2.f * (d - del) / d;
-          if (i < j) lsum += double(d - del) * double(d - del);
+      if (MODE == 0) {
+        if (d > 0.f) w = __fdividef(aux[i * n + j] + tt[tx][ty], d);
+      } else {
+        const float del = tt[ty][tx];
+        const float e = d > 0.f ? d - del : -del;  // coincident points: in the stress only
+        if (d > 0.f) w = __fdividef(2.f * e, d);
+        if (i < j) {
+          const float q = e * e;
+          lsum.add(q);
+          lsum.lo += fmaf(e, e, -q);
         }
-      } else if (MODE == 1 && i < j) {
-        const int64_t a = j, b = i;
-        const float del = aux[n * b - b * (b + 1) / 2 + a - b - 1];
-        lsum += double(del) * double(del);
       }
     }
     if (i < n && j < kp) put_parts<__nv_bfloat16>(Wp, plane, i * kp + j, w, 3);
@@ -623,9 +644,9 @@ __global__ void adj_weight_kernel(const float *__restrict__ D, const float *__re
     if (tx == 0 && i < n) rsum[i * nbj + blockIdx.x] = r;
   }
   if (MODE == 1) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if (tx == 0) lsh[ty0] = lsum;
+    float lh = lsum.hi, ll = lsum.lo;
+    warp_pair_sum(lh, ll);
+    if (tx == 0) lsh[ty0] = double(lh) + double(ll);
     __syncthreads();
     if (tx == 0 && ty0 == 0) {
       double t = 0.0;
@@ -696,7 +717,7 @@ int dist_backward_tc(const float *X, int64_t n, int64_t dim, const float *aux, f
   adj_finish_kernel<<<unsigned(cdiv(n * 32, 256)), 256, 0, s>>>(Xc, C, rsum, n, dim, nbj, dX);
   count_launch();
   if (MODE == 1 && loss) {
-    loss_reduce_kernel<<<1, 32, 0, s>>>(lp, nbi * nbj, loss);
+    loss_reduce_kernel<<<1, kLossThreads, 0, s>>>(lp, nbi * nbj, loss);
     count_launch();
   }
   GT_CUDA(cudaGetLastError());
@@ -762,7 +783,7 @@ int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *au
   dist_backward_reduce_kernel<<<unsigned(g), 256, 0, s>>>(X, n, dim, nsplit, fa, fw, dX);
   count_launch(2);
   if (MODE == 1 && loss) {
-    loss_reduce_kernel<<<1, 32, 0, s>>>(dl, ib * nsplit, loss);
+    loss_reduce_kernel<<<1, kLossThreads, 0, s>>>(dl, ib * nsplit, loss);
     count_launch();
   }
   GT_CUDA(cudaGetLastError());
