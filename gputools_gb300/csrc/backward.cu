@@ -656,11 +656,12 @@ __global__ void adj_weight_kernel(const float *__restrict__ D, const float *__re
   }
 }
 
-// dX_i = xc_i * sum_b rsum[i][b] - C_i (C = W Xc), the row's partials added
-// in order (compensated), one warp per point.
+// dX_i = xc_i * sum_b rsum[i][b] - C_i (C = W Xc, the sum of `parts` pieces
+// of n x dim), the row's partials added in order (compensated), one warp per
+// point.
 __global__ void adj_finish_kernel(const float *__restrict__ Xc, const float *__restrict__ C,
-                                  const float *__restrict__ rsum, int64_t n, int64_t dim,
-                                  int64_t nbj, float *__restrict__ dX) {
+                                  int parts, const float *__restrict__ rsum, int64_t n,
+                                  int64_t dim, int64_t nbj, float *__restrict__ dX) {
   const int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= n) return;
@@ -673,7 +674,11 @@ __global__ void adj_finish_kernel(const float *__restrict__ Xc, const float *__r
   }
   warp_pair_sum_f(hi, lo);
   const float r = hi + lo;
-  for (int64_t c = lane; c < dim; c += 32) dX[i * dim + c] = fmaf(Xc[i * dim + c], r, -C[i * dim + c]);
+  for (int64_t c = lane; c < dim; c += 32) {
+    float w = C[i * dim + c];
+    for (int q = 1; q < parts; q++) w += C[int64_t(q) * n * dim + i * dim + c];
+    dX[i * dim + c] = fmaf(Xc[i * dim + c], r, -w);
+  }
 }
 
 template <int MODE>
@@ -688,9 +693,13 @@ int dist_backward_tc(const float *X, int64_t n, int64_t dim, const float *aux, f
   GT_TRY(euclid_tc(X, n, dim, D, GT_LAYOUT_FULL, s));
   GT_TRY(ws_get(WS_ADJ1, size_t(3) * size_t(n) * size_t(kp) * 2, &pW));
   auto *Wp = static_cast<__nv_bfloat16 *>(pW);
-  // misc: means | Xc | B planes | C | rsum | loss parts
+  // W Xc in K pieces when its output tiles alone would leave most SMs idle
+  const int64_t out_tiles = cdiv(n, int64_t(128)) * cdiv(dim, int64_t(256));
+  int parts = 1;
+  while (parts < 4 && out_tiles * (parts + 1) <= int64_t(sm_count())) parts++;
+  // misc: means | Xc | B planes | C (parts pieces) | rsum | loss parts
   const size_t b_mean = size_t(dim) * 8, b_xc = size_t(n) * size_t(dim) * 4;
-  const size_t b_bt = size_t(3) * size_t(dim) * size_t(kp) * 2, b_c = b_xc;
+  const size_t b_bt = size_t(3) * size_t(dim) * size_t(kp) * 2, b_c = size_t(parts) * b_xc;
   const size_t b_rs = size_t(n) * size_t(nbj) * 4, b_lp = size_t(nbi) * size_t(nbj) * 8;
   auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
   GT_TRY(ws_get(WS_ADJ2, r256(b_mean) + r256(b_xc) + r256(b_bt) + r256(b_c) + r256(b_rs) + b_lp,
@@ -713,8 +722,12 @@ int dist_backward_tc(const float *X, int64_t n, int64_t dim, const float *aux, f
   count_launch(3);
   GT_CUDA(cudaGetLastError());
   // C = W Xc on the tensor cores (rows i, columns c)
-  GT_TRY(gemm_tc_store(Wp, n, Bt, dim, kp, 3, C, dim, s));
-  adj_finish_kernel<<<unsigned(cdiv(n * 32, 256)), 256, 0, s>>>(Xc, C, rsum, n, dim, nbj, dX);
+  if (parts > 1)
+    GT_TRY(gemm_tc_store_ksplit(Wp, n, Bt, dim, kp, parts, &parts, C, dim, s));
+  else
+    GT_TRY(gemm_tc_store(Wp, n, Bt, dim, kp, 3, C, dim, s));
+  adj_finish_kernel<<<unsigned(cdiv(n * 32, 256)), 256, 0, s>>>(Xc, C, parts, rsum, n, dim, nbj,
+                                                                  dX);
   count_launch();
   if (MODE == 1 && loss) {
     loss_reduce_kernel<<<1, kLossThreads, 0, s>>>(lp, nbi * nbj, loss);

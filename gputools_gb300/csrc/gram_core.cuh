@@ -335,6 +335,7 @@ struct TileRef {
   const CUtensorMap *ma, *mb;
   int64_t row0, col0;  // first operand row of the A and B boxes (A may start below 0)
   int64_t nk, prob;
+  int64_t k0 = 0;      // first k-block (a contraction whose K range is split)
 };
 
 // One problem: maps and finish as kernel parameters, tiles dealt round-robin.

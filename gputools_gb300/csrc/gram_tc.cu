@@ -649,6 +649,44 @@ __device__ __forceinline__ void stage_block(const float (&acc)[N], float *wsm) {
 template <class Work>
 using FinOf = std::decay_t<decltype(std::declval<const Work &>().finish(std::declval<const TileRef &>()))>;
 
+// One contraction whose K range is cut into `parts` pieces, so that a
+// contraction of few output tiles still occupies the SMs: work item u is
+// output tile u / parts over the k-blocks of piece u % parts, stored by
+// fins[piece] (each piece into its own partial output).
+template <class Fin>
+struct KSplitWork {
+  static constexpr int kMaxParts = 4;
+  CUtensorMap ma, mb;
+  TileSpace ts;
+  int64_t nk_total, nk_part;
+  int parts;
+  Fin fins[kMaxParts];
+  __device__ bool tile(int64_t cursor, TileRef &ref) const {
+    const int64_t u = int64_t(blockIdx.x) + cursor * int64_t(gridDim.x);
+    if (u >= ts.ntiles * parts) return false;
+    const int64_t t = u / parts;
+    const int64_t piece = u - t * parts;
+    int64_t ti, tj;
+    tile_coords(ts, t, ti, tj);
+    ref.row0 = ti * kBM;
+    ref.col0 = tj * kBN;
+    ref.ma = &ma;
+    ref.mb = &mb;
+    ref.k0 = piece * nk_part;
+    ref.nk = nk_total - ref.k0 < nk_part ? nk_total - ref.k0 : nk_part;
+    ref.prob = piece;
+    return true;
+  }
+  static constexpr bool kPrefetch = false;
+  __device__ bool skip() const { return false; }
+  __device__ const Fin &finish(const TileRef &ref) const { return fins[ref.prob]; }
+  __device__ void drain(EpiCtx &ctx) const { fins[0].drain(ctx); }
+  __device__ void prefetch() const {
+    tc::prefetch_tensormap(&ma);
+    tc::prefetch_tensormap(&mb);
+  }
+};
+
 // Whether a work source asks for sixteen epilogue warps (Work::kWideEpi).
 template <class Work, class = void>
 struct wide_epi : std::false_type {};
@@ -727,12 +765,12 @@ gram_tc_kernel(const __grid_constant__ Work work, int64_t ckb, const tc::WaitCfg
           tc::mbar_arrive_expect_tx(&full[s], C::STAGE);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
-            tc::tma_load_3d(st + p * C::A_TILE, ref.ma, &full[s], int32_t(kb * BK),
+            tc::tma_load_3d(st + p * C::A_TILE, ref.ma, &full[s], int32_t((ref.k0 + kb) * BK),
                             int32_t(ref.row0), p);
 #pragma unroll
           for (int p = 0; p < NSPLIT; p++)
             tc::tma_load_3d(st + NSPLIT * C::A_TILE + p * C::B_TILE, ref.mb, &full[s],
-                            int32_t(kb * BK), int32_t(ref.col0), p);
+                            int32_t((ref.k0 + kb) * BK), int32_t(ref.col0), p);
         }
       }
       // drain: no bulk copy may still be writing shared memory at exit
@@ -1370,6 +1408,35 @@ int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t 
                                                   tc_chunk_kblocks(32), fin, "gemm_store", s);
   return launch_gram<tc::KIND_BF16X3, 64, true>(planesA, nA, planesB, nB, kpad, kFull,
                                                 tc_chunk_kblocks(64), fin, "gemm_store", s);
+}
+
+// C_q = A B^T over the q-th of up to `parts` pieces of the K range (bf16x6
+// planes), each piece into C + q * nA * ldc, all in one launch (the caller
+// adds the pieces); parts is at most 4, every piece gets at least one k-block,
+// and *used says how many pieces were written.
+int gemm_tc_store_ksplit(const void *planesA, int64_t nA, const void *planesB, int64_t nB,
+                         int64_t kpad, int parts, int *used, float *C, int64_t ldc,
+                         cudaStream_t s) {
+  *used = 0;
+  if (nA == 0 || nB == 0) return GT_OK;
+  using W = KSplitWork<StoreFinish>;
+  constexpr int BK = 32;
+  if (kpad <= 0 || kpad % BK) return fail(GT_EINVAL, "bad padded K (%lld)", (long long)kpad);
+  const int64_t nk = kpad / BK;
+  if (parts < 1 || parts > W::kMaxParts) return fail(GT_EINVAL, "bad K split (%d)", parts);
+  if (parts > nk) parts = int(nk);
+  W w;
+  GT_TRY(make_plane_map(&w.ma, planesA, nA, kpad, 3, kBM, BK, false));
+  GT_TRY(make_plane_map(&w.mb, planesB, nB, kpad, 3, kBN, BK, false));
+  w.ts = make_tiles(nA, nB, kFull, band_group(int64_t(kBN) * kpad * 2 * 3));
+  w.nk_total = nk;
+  w.nk_part = cdiv(nk, int64_t(parts));
+  w.parts = int(cdiv(nk, w.nk_part));  // every piece non-empty
+  for (int q = 0; q < w.parts; q++)
+    w.fins[q] = StoreFinish{C + int64_t(q) * nA * ldc, ldc, nA, nB};
+  *used = w.parts;
+  return launch_work<tc::KIND_BF16X6, BK, true>(w, w.ts.ntiles * w.parts, tc_chunk_kblocks(BK),
+                                                "gemm_store", s);
 }
 
 // The same contraction from f16x3 planes whose rows were scaled by powers of

@@ -90,6 +90,12 @@ int mi_tc(const void *planesX, int64_t rowsX, const void *planesY, int64_t rowsY
 // planes ([part][row][kpad], kpad a multiple of 64), stored as row-major float.
 int gemm_tc_store(const void *planesA, int64_t nA, const void *planesB, int64_t nB, int64_t kpad,
                   int nsplit, float *C, int64_t ldc, cudaStream_t s);
+// The bf16x6 contraction with its K range in up to `parts` (<= 4) pieces, one
+// launch; piece q is stored into C + q * nA * ldc (*used pieces) and the
+// caller adds them.
+int gemm_tc_store_ksplit(const void *planesA, int64_t nA, const void *planesB, int64_t nB,
+                         int64_t kpad, int parts, int *used, float *C, int64_t ldc,
+                         cudaStream_t s);
 // The same from f16x3 planes of rows scaled by powers of two; rsA / rsB hold
 // the factors that undo each row's scale (C[r][c] * rsA[r] * rsB[c]).
 int gemm_tc_store_scaled(const void *planesA, int64_t nA, const void *planesB, int64_t nB,
