@@ -579,9 +579,26 @@ def run_case(args):
         ns = np.exp(rng.uniform(np.log(50), np.log(2000), args.count)).astype(int)
         xs = [torch.randn((int(a), int(b)), generator=gen, device=dev, dtype=torch.float32)
               for a, b in zip(ps, ns)]
-        plan = g.BatchPlan(xs, "pearson", autotune=False, graph=False)
+        plan = g.BatchPlan(xs, "pearson", autotune=args.tune, graph=False)
         fn = lambda: plan.launch(stream)
         names = ("batch_pearson",)
+    elif args.case == "cor_backward":
+        # gpuCorBackward: p variables x n observations N(0,1), a symmetric p x p upstream
+        dX = torch.from_numpy(rng.standard_normal((p, n), dtype=np.float32)).to(dev)
+        G = torch.from_numpy(rng.standard_normal((p, p), dtype=np.float32)).to(dev)
+        G = ((G + G.T) * 0.5).contiguous()
+        out = torch.empty_like(dX)
+        fn = lambda: _lib.check(lib.gt_cor_backward_device(vp(dX), p, n, vp(G), vp(out), sptr))
+        names = ("cor_backward",)
+    elif args.case == "mds":
+        # MDS stress and gradient: p points x n dims N(0,1), targets uniform in [0, 8)
+        dX = torch.from_numpy(rng.standard_normal((p, n), dtype=np.float32)).to(dev)
+        delta = torch.from_numpy(rng.random(p * (p - 1) // 2, dtype=np.float32) * 8).to(dev)
+        out = torch.empty_like(dX)
+        loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        fn = lambda: _lib.check(lib.gt_mds_stress_device(vp(dX), p, n, vp(delta), vp(out),
+                                                         vp(loss), sptr))
+        names = ("mds_stress",)
     elif args.case == "hclust":
         # p points x n dims around 8 centres; each step clusters a fresh copy
         # of their euclidean distance matrix (the copy is inside the step)
@@ -961,8 +978,9 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--skip-euclid", action="store_true")
     ap.add_argument("--count", type=int, default=300, help="--case batch: problems")
+    ap.add_argument("--tune", action="store_true", help="--case batch: autotune the plan")
     ap.add_argument("--case", choices=("pearson", "euclid", "kendall", "dist", "mi", "hclust",
-                                       "batch"),
+                                       "batch", "cor_backward", "mds"),
                     help="run one workload at the given size instead of the benchmark")
     ap.add_argument("--p", type=int, default=4096, help="--case: variables / points")
     ap.add_argument("--n", type=int, default=4096, help="--case: observations")
