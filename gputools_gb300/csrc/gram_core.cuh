@@ -475,7 +475,9 @@ struct PearsonBatchWork {
     ref.prob = t.x;
     return true;
   }
-  static constexpr bool kPrefetch = true;
+  // the next tile is looked up when reached: holding it costs the sixteen-warp
+  // kernel (96 registers) spills that outweigh the lookup
+  static constexpr bool kPrefetch = false;
   __device__ bool skip() const { return false; }
   __device__ PearsonFinish finish(const TileRef &ref) const { return probs[ref.prob].fin; }
   __device__ void drain(EpiCtx &) const {}
