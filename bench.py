@@ -409,10 +409,10 @@ def run_ours(args, ranks: Ranks):
         "e2e": {"value": ranks.world * entries / e2e_s, "unit": "entries/s",
                 "h2d_bytes_per_step": int(P * N_OBS * 4), "d2h_bytes_per_step": int(2 * P * P * 4),
                 "api": "gt_pmcc with pageable host buffers, as R's .C passes them (the Gram "
-                       "runs in 16 bands of rows; the kernels write r and t into page-locked "
-                       "staging over the host link and host threads copy each finished band "
-                       "into the caller's buffers while the next band runs; the constant pair "
-                       "counts n are filled by the same threads)",
+                       "runs in 16 bands of rows into device memory; each finished band's r "
+                       "and t go to the caller's buffers by a device-to-host copy on a second "
+                       "stream while the next bands run; host threads fill the constant pair "
+                       "counts n meanwhile)",
                 "ms_per_step": e2e_s * 1e3,
                 "pinned": {"value": ranks.world * entries / e2e_pinned_s,
                            "ms_per_step": e2e_pinned_s * 1e3}},
