@@ -116,6 +116,160 @@ sym_operand_kernel(const float *__restrict__ G, int64_t p, int64_t kp, int ns, T
   }
 }
 
+// The f16x3 operands of the Pearson adjoint without float intermediates.
+// S = G + G^T is taken in 64 x 64 tile pairs: the block of (I, J), I <= J,
+// loads G[I][J] and G[J][I] once and has both S[I][J] and S[J][I] = S[I][J]^T.
+// Pass 1 (sym_rowmax_kernel) folds every row's largest finite |S| into
+// rowmax (float bits, atomicMax); pass 2 (sym_split_kernel) scales each row
+// by the power of two that brings that maximum into [2^14, 2^15) and writes
+// the two f16 planes ([2][p][kp], zero padded) and the factors that undo the
+// scales.  G is read twice in all, S never stored in float.
+template <int PASS>
+__device__ __forceinline__ void sym_pair_tiles(const float *__restrict__ G, int64_t p,
+                                               float (&ta)[64][65], float (&tb)[64][65],
+                                               int64_t &I0, int64_t &J0) {
+  I0 = int64_t(blockIdx.y) * 64;
+  J0 = int64_t(blockIdx.x) * 64;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  // ta[a][b] = G[I0 + a][J0 + b], tb[a][b] = G[J0 + a][I0 + b]
+#pragma unroll 4
+  for (int r = 0; r < 8; r++) {
+    const int a = ty + 8 * r;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int b = 2 * tx + h;
+      const int64_t i = I0 + a, j = J0 + b;
+      ta[a][b] = (i < p && j < p) ? G[i * p + j] : 0.f;
+      const int64_t jj = J0 + a, ii = I0 + b;
+      tb[a][b] = (jj < p && ii < p) ? G[jj * p + ii] : 0.f;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ float finite_abs(float v) {
+  const float a = fabsf(v);
+  return a == a ? a : 0.f;  // NaN does not count, as fmaxf would skip it
+}
+
+__global__ void __launch_bounds__(256)
+sym_rowmax_kernel(const float *__restrict__ G, int64_t p, unsigned *__restrict__ rowmax) {
+  if (blockIdx.y > blockIdx.x) return;  // the pair (J, I) is done by block (I, J)
+  __shared__ float ta[64][65], tb[64][65];
+  __shared__ float cm[8][64];
+  int64_t I0, J0;
+  sym_pair_tiles<1>(G, p, ta, tb, I0, J0);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  float c0 = 0.f, c1 = 0.f;  // this thread's columns b = 2 tx, 2 tx + 1 (rows J0 + b of S)
+#pragma unroll 4
+  for (int r = 0; r < 8; r++) {
+    const int a = ty + 8 * r;
+    const float s0 = finite_abs(ta[a][2 * tx] + tb[2 * tx][a]);
+    const float s1 = finite_abs(ta[a][2 * tx + 1] + tb[2 * tx + 1][a]);
+    c0 = fmaxf(c0, s0);
+    c1 = fmaxf(c1, s1);
+    // row I0 + a of S: the warp's 64 columns
+    float m = fmaxf(s0, s1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (tx == 0 && I0 + a < p) atomicMax(rowmax + I0 + a, __float_as_uint(m));
+  }
+  cm[ty][2 * tx] = c0;
+  cm[ty][2 * tx + 1] = c1;
+  __syncthreads();
+  const int t = ty * 32 + tx;
+  if (t < 64 && J0 + t < p) {
+    float m = cm[0][t];
+#pragma unroll
+    for (int q = 1; q < 8; q++) m = fmaxf(m, cm[q][t]);
+    atomicMax(rowmax + J0 + t, __float_as_uint(m));
+  }
+}
+
+__global__ void __launch_bounds__(256)
+sym_split_kernel(const float *__restrict__ G, int64_t p, int64_t kp,
+                 const unsigned *__restrict__ rowmax, uint16_t *__restrict__ planes,
+                 float *__restrict__ scale) {
+  if (blockIdx.y > blockIdx.x) return;
+  __shared__ float ta[64][65], tb[64][65];
+  int64_t I0, J0;
+  sym_pair_tiles<2>(G, p, ta, tb, I0, J0);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t plane = p * kp;
+  // rows I0 + a, columns J0 + b (and, off the diagonal, rows J0 + a, columns I0 + b)
+#pragma unroll 2
+  for (int r = 0; r < 8; r++) {
+    const int a = ty + 8 * r;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+      if (side == 1 && I0 == J0) break;
+      const int64_t row = (side == 0 ? I0 : J0) + a;
+      const int64_t col = (side == 0 ? J0 : I0) + 2 * tx;
+      if (row >= p || col >= kp) continue;
+      const int e = tc::f16_scale_exp(__uint_as_float(rowmax[row]));
+      const float sc = tc::exp2i(e);
+      float v[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int b = 2 * tx + h;
+        // S[row][col + h]: side 0 from (a, b) of the pair, side 1 its transpose
+        v[h] = side == 0 ? ta[a][b] + tb[b][a] : tb[a][b] + ta[b][a];
+      }
+      uint16_t h0[3], h1[3];
+      tc::split_parts<tc::KIND_F16X3>(v[0] * sc, h0);
+      tc::split_parts<tc::KIND_F16X3>(v[1] * sc, h1);
+      *reinterpret_cast<uint32_t *>(planes + row * kp + col) = uint32_t(h0[0]) | (uint32_t(h1[0]) << 16);
+      *reinterpret_cast<uint32_t *>(planes + plane + row * kp + col) =
+          uint32_t(h0[1]) | (uint32_t(h1[1]) << 16);
+      if (tx == 0 && side == 0 && I0 == J0) scale[row] = tc::exp2i(-e);
+    }
+  }
+}
+
+// Z^T as f16x3 planes ([2][n][kp], zero padded): rows k (observations),
+// columns i (variables), z = (x - mean) * inv_norm.  |z| <= 1 (the centred
+// variable has unit norm), so one scale, 2^14, serves every row; scale[k] =
+// 2^-14 undoes it.
+__global__ void __launch_bounds__(256)
+zt_split_kernel(const float *__restrict__ X, int64_t p, int64_t n, int64_t kp,
+                const ColStats *__restrict__ st, uint16_t *__restrict__ planes,
+                float *__restrict__ scale) {
+  __shared__ float tile[32][33];
+  __shared__ float cen[32][4];
+  const int64_t k0 = int64_t(blockIdx.x) * 32, i0 = int64_t(blockIdx.y) * 32;
+  const int tx = threadIdx.x, ty0 = threadIdx.y;
+  if (ty0 == 0) {
+    const int64_t i = i0 + tx;
+    if (i < p) {
+      const ColStats s = st[i];
+      const Centerer c(s);
+      cen[tx][0] = c.mhi;
+      cen[tx][1] = c.mlo;
+      cen[tx][2] = c.inv;
+      cen[tx][3] = s.flags ? 1.f : 0.f;
+    }
+    if (blockIdx.y == 0 && k0 + tx < n) scale[k0 + tx] = 1.f / 16384.f;
+  }
+  __syncthreads();
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t i = i0 + ty, k = k0 + tx;
+    float z = 0.f;
+    if (i < p && k < n && cen[ty][3] == 0.f)
+      z = ((X[i * n + k] - cen[ty][0]) - cen[ty][1]) * cen[ty][2];
+    tile[ty][tx] = z;  // rows i
+  }
+  __syncthreads();
+  const int64_t plane = n * kp;
+  for (int ty = ty0; ty < 32; ty += 8) {
+    const int64_t k = k0 + ty, i = i0 + tx;
+    if (k >= n || i >= kp) continue;
+    uint16_t h[3];
+    tc::split_parts<tc::KIND_F16X3>(tile[tx][ty] * 16384.f, h);
+    planes[k * kp + i] = h[0];
+    planes[plane + k * kp + i] = h[1];
+  }
+}
+
 // Z^T: rows k (observations), columns i (variables, ld kp), zero padded.
 template <class T>
 __global__ void zt_operand_kernel(const float *__restrict__ X, int64_t p, int64_t n, int64_t kp,
@@ -153,47 +307,6 @@ __global__ void zt_operand_kernel(const float *__restrict__ X, int64_t p, int64_
 }
 
 constexpr int kFinThreads = 256;
-
-// Rows of a float matrix (nrows x kp) as f16x3 planes ([2][nrows][kp]), each
-// row scaled by the power of two that brings its largest magnitude into
-// [2^14, 2^15); scale[row] = the factor that undoes it.  One warp per row,
-// four consecutive values per lane (kp is a multiple of 64 and the rows are
-// 16-byte aligned).
-__global__ void __launch_bounds__(256)
-f16x3_rows_kernel(const float *__restrict__ M, int64_t nrows, int64_t kp,
-                  uint16_t *__restrict__ planes, float *__restrict__ scale) {
-  const int64_t row = (int64_t(blockIdx.x) * 256 + threadIdx.x) >> 5;
-  if (row >= nrows) return;  // whole warps
-  const int lane = threadIdx.x & 31;
-  const float4 *m = reinterpret_cast<const float4 *>(M + row * kp);
-  const int64_t k4 = kp >> 2;
-  float amax = 0.f;
-  for (int64_t k = lane; k < k4; k += 32) {
-    const float4 v = m[k];
-    amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
-  }
-  amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(amax)));
-  const int e = tc::f16_scale_exp(amax);
-  const float sc = tc::exp2i(e);
-  if (lane == 0) scale[row] = tc::exp2i(-e);
-  const int64_t plane = nrows * kp;
-  uint2 *p0 = reinterpret_cast<uint2 *>(planes + row * kp);
-  uint2 *p1 = reinterpret_cast<uint2 *>(planes + plane + row * kp);
-  for (int64_t k = lane; k < k4; k += 32) {
-    const float4 v = m[k];
-    const float e4[4] = {v.x, v.y, v.z, v.w};
-    uint32_t h[2] = {0u, 0u}, l[2] = {0u, 0u};
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      uint16_t pp[3];
-      tc::split_parts<tc::KIND_F16X3>(e4[q] * sc, pp);
-      h[q >> 1] |= uint32_t(pp[0]) << (16 * (q & 1));
-      l[q >> 1] |= uint32_t(pp[1]) << (16 * (q & 1));
-    }
-    p0[k] = make_uint2(h[0], h[1]);
-    p1[k] = make_uint2(l[0], l[1]);
-  }
-}
 
 // Sum of the lanes' (hi, lo) float pairs, left in every lane (TwoSum).
 __device__ __forceinline__ void warp_pair_sum_f(float &hi, float &lo) {
@@ -835,25 +948,23 @@ int cor_backward_impl(const float *dX, int64_t p, int64_t n, const float *dG, fl
     cudaError_t e = launch_allpairs_simt<OpDotB, OutStore, 8, 8>(a, OpDotB{}, OutStore{W, n}, s);
     if (e != cudaSuccess) return fail(GT_ECUDA, "adjoint GEMM launch: %s", cudaGetErrorString(e));
   } else if (path == GT_GRAM_TC_F16X3 || path == GT_GRAM_TC_F16X6) {
-    // f16x3 with every operand row scaled by a power of two (G + G^T and z^T
-    // are not unit-scaled): three products, the scales undone in the store
-    void *pSf = nullptr, *pZf = nullptr, *psc = nullptr;
-    GT_TRY(ws_get(WS_ADJ0, size_t(p) * size_t(kp) * 4, &pSf));
-    GT_TRY(ws_get(WS_ADJ1, size_t(n) * size_t(kp) * 4, &pZf));
+    // f16x3 with every operand row scaled by a power of two (G + G^T is not
+    // unit-scaled; z^T is bounded by 1 and takes one scale): three products,
+    // the scales undone in the store
+    void *prm = nullptr, *psc = nullptr;
+    GT_TRY(ws_get(WS_ADJ0, size_t(p) * 4, &prm));
     GT_TRY(ws_get(WS_ADJ2, size_t(p + n) * 4, &psc));
     GT_TRY(ws_get(WS_SCRATCH0, size_t(2) * size_t(p) * size_t(kp) * 2, &pS));
     GT_TRY(ws_get(WS_SCRATCH1, size_t(2) * size_t(n) * size_t(kp) * 2, &pZ));
-    auto *Sf = static_cast<float *>(pSf), *Zf = static_cast<float *>(pZf);
+    auto *rowmax = static_cast<unsigned *>(prm);
     auto *scS = static_cast<float *>(psc), *scZ = scS + p;
-    sym_operand_kernel<float><<<dim3(unsigned(kp / 64), unsigned(cdiv(p, 64))), blk, 0, s>>>(
-        dG, p, kp, 1, Sf);
-    zt_operand_kernel<float><<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
-        dX, p, n, kp, st, 1, Zf);
-    f16x3_rows_kernel<<<unsigned(cdiv(p, 8)), 256, 0, s>>>(Sf, p, kp,
-                                                            static_cast<uint16_t *>(pS), scS);
-    f16x3_rows_kernel<<<unsigned(cdiv(n, 8)), 256, 0, s>>>(Zf, n, kp,
-                                                            static_cast<uint16_t *>(pZ), scZ);
-    count_launch(4);
+    GT_CUDA(cudaMemsetAsync(rowmax, 0, size_t(p) * 4, s));
+    const dim3 pairs(unsigned(kp / 64), unsigned(kp / 64));
+    sym_rowmax_kernel<<<pairs, blk, 0, s>>>(dG, p, rowmax);
+    sym_split_kernel<<<pairs, blk, 0, s>>>(dG, p, kp, rowmax, static_cast<uint16_t *>(pS), scS);
+    zt_split_kernel<<<dim3(unsigned(cdiv(n, 32)), unsigned(kp / 32)), blk, 0, s>>>(
+        dX, p, n, kp, st, static_cast<uint16_t *>(pZ), scZ);
+    count_launch(3);
     GT_CUDA(cudaGetLastError());
     GT_TRY(gemm_tc_store_scaled(pS, p, pZ, n, kp, scS, scZ, W, n, s));
   } else {
