@@ -124,7 +124,6 @@ sym_operand_kernel(const float *__restrict__ G, int64_t p, int64_t kp, int ns, T
 // by the power of two that brings that maximum into [2^14, 2^15) and writes
 // the two f16 planes ([2][p][kp], zero padded) and the factors that undo the
 // scales.  G is read twice in all, S never stored in float.
-template <int PASS>
 __device__ __forceinline__ void sym_pair_tiles(const float *__restrict__ G, int64_t p,
                                                float (&ta)[64][65], float (&tb)[64][65],
                                                int64_t &I0, int64_t &J0) {
@@ -158,7 +157,7 @@ sym_rowmax_kernel(const float *__restrict__ G, int64_t p, unsigned *__restrict__
   __shared__ float ta[64][65], tb[64][65];
   __shared__ float cm[8][64];
   int64_t I0, J0;
-  sym_pair_tiles<1>(G, p, ta, tb, I0, J0);
+  sym_pair_tiles(G, p, ta, tb, I0, J0);
   const int tx = threadIdx.x, ty = threadIdx.y;
   float c0 = 0.f, c1 = 0.f;  // this thread's columns b = 2 tx, 2 tx + 1 (rows J0 + b of S)
 #pragma unroll 4
@@ -193,7 +192,7 @@ sym_split_kernel(const float *__restrict__ G, int64_t p, int64_t kp,
   if (blockIdx.y > blockIdx.x) return;
   __shared__ float ta[64][65], tb[64][65];
   int64_t I0, J0;
-  sym_pair_tiles<2>(G, p, ta, tb, I0, J0);
+  sym_pair_tiles(G, p, ta, tb, I0, J0);
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t plane = p * kp;
   // rows I0 + a, columns J0 + b (and, off the diagonal, rows J0 + a, columns I0 + b)
