@@ -207,12 +207,6 @@ template <class Fin>
 struct staged_block<Fin, std::void_t<decltype(Fin::kStagedBlock)>>
     : std::integral_constant<bool, Fin::kStagedBlock> {};
 
-// Output stores of the finishes: streaming (evict-first in L2), so that the
-// outputs, written once, do not push the operand panels out of L2.
-__device__ __forceinline__ void st_stream(float *p, float v) {
-  asm volatile("st.global.cs.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
-}
-
 __device__ __forceinline__ float clamp_r(float r) { return r > 1.f ? 1.f : (r < -1.f ? -1.f : r); }
 
 // hostSignif's rule (src/correlation.cpp:51-64), t = r sqrt(n-2) / sqrt(1-r^2)
@@ -234,9 +228,9 @@ struct PearsonFinish {
   __device__ __forceinline__ bool skip() const { return gate && *gate != 0; }
 
   __device__ __forceinline__ void put(float *pc, float *pt, float *pp, float v) const {
-    if (corr) st_stream(pc, v);
-    if (ts) st_stream(pt, signif_fast(v, sq_nm2));
-    if (pairs) st_stream(pp, npairs);
+    if (corr) tc::st_stream(pc, v);
+    if (ts) tc::st_stream(pt, signif_fast(v, sq_nm2));
+    if (pairs) tc::st_stream(pp, npairs);
   }
 
   // A block from registers: g[j] = entry (r, c0 + j), lanes on consecutive rows.
@@ -303,9 +297,9 @@ struct PearsonFinish {
       for (int j = 0; j < 32; j++) {
         if (j < jn && j > dj) {
           const float v = clamp_r(wsm[lane * 33 + j] * gscale);
-          if (corr) st_stream(corr + o, v);
-          if (ts) st_stream(ts + o, signif_fast(v, sq_nm2));
-          if (pairs) st_stream(pairs + o, npairs);
+          if (corr) tc::st_stream(corr + o, v);
+          if (ts) tc::st_stream(ts + o, signif_fast(v, sq_nm2));
+          if (pairs) tc::st_stream(pairs + o, npairs);
         }
         o += ld;
       }
@@ -319,9 +313,9 @@ struct PearsonFinish {
         if (i < in_ && i <= di) {
           float v = clamp_r(wsm[i * 33 + lane] * gscale);
           if (symmetric && i == di && v == v) v = 1.f;
-          if (corr) st_stream(corr + o, v);
-          if (ts) st_stream(ts + o, signif_fast(v, sq_nm2));
-          if (pairs) st_stream(pairs + o, npairs);
+          if (corr) tc::st_stream(corr + o, v);
+          if (ts) tc::st_stream(ts + o, signif_fast(v, sq_nm2));
+          if (pairs) tc::st_stream(pairs + o, npairs);
         }
         o += ld;
       }

@@ -377,7 +377,7 @@ struct EuclidLineFinish {
           const float d2 = fmaf(ra * cs[e], g[4 * k4 + e], s);
           // (pend << 1) | sign of d2 - tau s, in one funnel shift
           pend = __funnelshift_l(__float_as_uint(fmaf(-tau, s, d2)), pend, 1);
-          st_stream(orow + co[e], tc::sqrt_approx(fabsf(d2)));
+          tc::st_stream(orow + co[e], tc::sqrt_approx(fabsf(d2)));
         }
       }
     } else {
@@ -393,7 +393,7 @@ struct EuclidLineFinish {
           const float d2 = fmaf(ra * cs[e], g[4 * k4 + e], s);
           const bool valid = (int64_t(cid[4 * k4 + e]) < r) && (r < n);
           pend = (pend << 1) | unsigned(valid & (d2 < tau * s));
-          if (valid) st_stream(orow + co[e], tc::sqrt_approx(fabsf(d2)));
+          if (valid) tc::st_stream(orow + co[e], tc::sqrt_approx(fabsf(d2)));
         }
       }
     }

@@ -332,9 +332,20 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
         const float tsv = signif_pw(val, np);
         const int64_t i0 = r * a.ld + c, i1 = c * a.ld + r;
         const bool mirror = a.symmetric && r != c;
-        if (a.corr) { a.corr[i0] = val; if (mirror) a.corr[i1] = val; }
-        if (a.ts) { a.ts[i0] = tsv; if (mirror) a.ts[i1] = tsv; }
-        if (a.pairs) { a.pairs[i0] = np; if (mirror) a.pairs[i1] = np; }
+        // streaming stores: the outputs, written once, leave the operand
+        // planes in L2
+        if (a.corr) {
+          tc::st_stream(a.corr + i0, val);
+          if (mirror) tc::st_stream(a.corr + i1, val);
+        }
+        if (a.ts) {
+          tc::st_stream(a.ts + i0, tsv);
+          if (mirror) tc::st_stream(a.ts + i1, tsv);
+        }
+        if (a.pairs) {
+          tc::st_stream(a.pairs + i0, np);
+          if (mirror) tc::st_stream(a.pairs + i1, np);
+        }
       }
     }
     if (!ok) *abort_flag = 1;
