@@ -698,59 +698,84 @@ __global__ void adj_points_kernel(const float *__restrict__ X, int64_t n, int64_
 // W as the GEMM's A operand (rows i, columns j, ld kp, three bf16 planes),
 // from the full distance matrix D and G (MODE 0: W = (G + G^T) / D) or the
 // targets delta in R's dist layout (MODE 1: W = 2 (D - delta) / D); W_ii and
-// W_ij with D_ij = 0 are 0.  Per 32 x 32 tile: the rows' partial sums of W
-// (rsum[i * nbj + jb]) and, for MODE 1, the tile's part of the stress
-// sum_{i<j} (D - delta)^2 (lpart[ib * nbj + jb]); both are reduced in a fixed
-// order afterwards.  G^T, and delta below the diagonal (stored by column
-// there), go through shared memory so that every global read is coalesced;
-// the stress sums as compensated float pairs.
+// W_ij with D_ij = 0 are 0.  Per 32 x 64 tile (two columns per thread, so the
+// plane stores are 4 bytes): the rows' partial sums of W (rsum[i * nbj + jb])
+// and, for MODE 1, the tile's part of the stress sum_{i<j} (D - delta)^2
+// (lpart[ib * nbj + jb]); both are reduced in a fixed order afterwards.  G^T,
+// and delta below the diagonal (stored by column there), go through shared
+// memory so that every global read is coalesced; the stress sums as
+// compensated float pairs.
+constexpr int kAwRows = 32, kAwCols = 64;
 template <int MODE>
-__global__ void adj_weight_kernel(const float *__restrict__ D, const float *__restrict__ aux,
-                                  int64_t n, int64_t kp, __nv_bfloat16 *__restrict__ Wp,
-                                  float *__restrict__ rsum, double *__restrict__ lpart) {
-  // MODE 0: tt[jj][ii] = G[j][i]; MODE 1: tt[ii][jj] = delta(i, j), i != j
-  __shared__ float tt[32][33];
+__global__ void __launch_bounds__(256)
+adj_weight_kernel(const float *__restrict__ D, const float *__restrict__ aux, int64_t n,
+                  int64_t kp, __nv_bfloat16 *__restrict__ Wp, float *__restrict__ rsum,
+                  double *__restrict__ lpart) {
+  // MODE 0: tt[jj][ii] = G[j][i] (64 x 32); MODE 1: tt[ii][jj] = delta(i, j), i != j (32 x 64)
+  __shared__ float tt[MODE == 0 ? kAwCols : kAwRows][MODE == 0 ? kAwRows + 1 : kAwCols + 1];
   __shared__ double lsh[8];
-  const int64_t i0 = int64_t(blockIdx.y) * 32, j0 = int64_t(blockIdx.x) * 32;
+  const int64_t i0 = int64_t(blockIdx.y) * kAwRows, j0 = int64_t(blockIdx.x) * kAwCols;
   const int tx = threadIdx.x, ty0 = threadIdx.y;
   const int64_t nbj = gridDim.x;
-  for (int ty = ty0; ty < 32; ty += 8) {
-    if (MODE == 0) {
-      const int64_t j = j0 + ty, i = i0 + tx;
-      tt[ty][tx] = (j < n && i < n) ? aux[j * n + i] : 0.f;
-    } else {
-      // above the diagonal: row i of the dist layout, consecutive j
-      const int64_t i = i0 + ty, j = j0 + tx;
-      if (i < n && j < n && i < j) tt[ty][tx] = aux[n * i - i * (i + 1) / 2 + j - i - 1];
-      // below: delta(i, j) = delta(j, i), row j of the dist layout, consecutive i
-      const int64_t i2 = i0 + tx, j2 = j0 + ty;
-      if (i2 < n && j2 < n && i2 > j2) tt[tx][ty] = aux[n * j2 - j2 * (j2 + 1) / 2 + i2 - j2 - 1];
+  if (MODE == 0) {
+    for (int jj = ty0; jj < kAwCols; jj += 8) {
+      const int64_t j = j0 + jj, i = i0 + tx;
+      tt[jj][tx] = (j < n && i < n) ? aux[j * n + i] : 0.f;
+    }
+  } else {
+    // above the diagonal: row i of the dist layout, consecutive j
+    for (int ii = ty0; ii < kAwRows; ii += 8) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int jj = tx + 32 * h;
+        const int64_t i = i0 + ii, j = j0 + jj;
+        if (i < n && j < n && i < j) tt[ii][jj] = aux[n * i - i * (i + 1) / 2 + j - i - 1];
+      }
+    }
+    // below: delta(i, j) = delta(j, i), row j of the dist layout, consecutive i
+    for (int jj = ty0; jj < kAwCols; jj += 8) {
+      const int64_t i = i0 + tx, j = j0 + jj;
+      if (i < n && j < n && i > j) tt[tx][jj] = aux[n * j - j * (j + 1) / 2 + i - j - 1];
     }
   }
   __syncthreads();
   const int64_t plane = n * kp;
   FloatPairSum lsum;
-  for (int ty = ty0; ty < 32; ty += 8) {
-    const int64_t i = i0 + ty, j = j0 + tx;
-    float w = 0.f;
-    if (i < n && j < n && i != j) {
-      const float d = D[i * n + j];
-      if (MODE == 0) {
-        if (d > 0.f) w = __fdividef(aux[i * n + j] + tt[tx][ty], d);
-      } else {
-        const float del = tt[ty][tx];
-        const float e = d > 0.f ? d - del : -del;  // coincident points: in the stress only
-        if (d > 0.f) w = __fdividef(2.f * e, d);
-        if (i < j) {
-          const float q = e * e;
-          lsum.add(q);
-          lsum.lo += fmaf(e, e, -q);
+  for (int ii = ty0; ii < kAwRows; ii += 8) {
+    const int64_t i = i0 + ii;
+    float w[2] = {0.f, 0.f};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int jj = 2 * tx + h;
+      const int64_t j = j0 + jj;
+      if (i < n && j < n && i != j) {
+        const float d = D[i * n + j];
+        if (MODE == 0) {
+          if (d > 0.f) w[h] = __fdividef(aux[i * n + j] + tt[jj][ii], d);
+        } else {
+          const float del = tt[ii][jj];
+          const float e = d > 0.f ? d - del : -del;  // coincident points: in the stress only
+          if (d > 0.f) w[h] = __fdividef(2.f * e, d);
+          if (i < j) {
+            const float q = e * e;
+            lsum.add(q);
+            lsum.lo += fmaf(e, e, -q);
+          }
         }
       }
     }
-    if (i < n && j < kp) put_parts<__nv_bfloat16>(Wp, plane, i * kp + j, w, 3);
-    // row sum of the tile: the 32 lanes of a row
-    float r = w;
+    const int64_t j = j0 + 2 * tx;  // even, and kp is a multiple of 64
+    if (i < n && j < kp) {
+      uint16_t a[3], b[3];
+      tc::split_parts<tc::KIND_BF16X6>(w[0], a);
+      tc::split_parts<tc::KIND_BF16X6>(w[1], b);
+      uint32_t *dst = reinterpret_cast<uint32_t *>(Wp + i * kp + j);
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        dst[q * (plane / 2)] = uint32_t(a[q]) | (uint32_t(b[q]) << 16);
+    }
+    // row sum of the tile: the 32 lanes of a row, two columns each
+    float r = w[0] + w[1];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
     if (tx == 0 && i < n) rsum[i * nbj + blockIdx.x] = r;
@@ -797,7 +822,8 @@ template <int MODE>
 int dist_backward_tc(const float *X, int64_t n, int64_t dim, const float *aux, float *dX,
                      double *loss, cudaStream_t s) {
   const int64_t kp = cdiv(n, kKPadB) * kKPadB;
-  const int64_t nbj = kp / 32, nbi = cdiv(n, 32);  // tile columns cover the padded k
+  // weight tiles: rows of 32, columns of 64 covering the padded k
+  const int64_t nbj = kp / kAwCols, nbi = cdiv(n, int64_t(kAwRows));
   void *pD = nullptr, *pW = nullptr, *pM = nullptr;
   // the full distance matrix (tcgen05 Gram, near-zero pairs recomputed exactly)
   GT_TRY(ws_get(WS_ADJ0, size_t(n) * size_t(n) * 4, &pD));
