@@ -16,16 +16,18 @@
 // each (times 2^14, as the f16x3 encoding: |z| <= 1).  A tile pairs 128 row
 // variables (TMEM lanes) with 32 column variables whose five planes are
 // stacked into one 160-row B operand [m; z hi; z lo; q hi; q lo], so each
-// k-step issues six MMAs into four TMEM regions and every sum of a pair sits
+// k-step issues six MMAs into three TMEM regions and every sum of a pair sits
 // in the lane of its row variable:
 //   R1 (160 columns)  A = m      x B rows 0..159: N, Sb hi, Sb lo, Sbb hi, Sbb lo
 //   R2 ( 64 columns)  A = z hi   x B rows 0..63 : Sa, Sab (hi.hi)
 //                     A = z lo   x B rows 0..63 : Sa, Sab (lo.hi)   (accumulated)
-//   R3 ( 32 columns)  A = z hi   x B rows 64..95: Sab (hi.lo)
+//                     A = z hi   x B rows 64..95: Sab (hi.lo), into R2's Sab columns
 //   R4 ( 32 columns)  A = q hi, q lo x B rows 0..31: Saa
-// K is accumulated in chunks of 256 observations (the tensor core's FP32
-// accumulation truncates every add); the epilogue adds each chunk into FP32
-// running sums and forms r, the t-score and the pair count from them.
+// 256 columns in all, so TMEM holds two accumulator sets and the MMAs of one
+// chunk run while the epilogue reads the other.  K is accumulated in chunks of
+// 256 observations (the tensor core's FP32 accumulation truncates every add);
+// the epilogue adds each chunk into FP32 running sums and forms r, the t-score
+// and the pair count from them.
 //
 // Kernel layout as in gram_tc.cu: persistent, one CTA per SM; warp 0 issues
 // the TMA loads, warp 1 the MMAs, warps 2..17 are the epilogue (4 per TMEM
@@ -55,7 +57,8 @@ constexpr int kPStage = kPlanes * (kPA + kPB);     // 50 KB
 constexpr int kPEpi = 16;                          // epilogue warps
 constexpr int kPThreads = 64 + 32 * kPEpi;         // + producer and MMA warps
 constexpr int kPSmem = kPStages * kPStage + 1024 + 256;
-constexpr int kR1 = 0, kR2 = 160, kR3 = 224, kR4 = 256;  // TMEM columns of the regions
+constexpr int kR1 = 0, kR2 = 160, kR4 = 224;  // TMEM columns of the regions
+constexpr int kPAcc = 256;                      // columns of one accumulator set (two fit)
 constexpr uint64_t kPDrainNs = 200000000ull;
 constexpr float kPScale = 16384.f;                 // 2^14
 
@@ -140,8 +143,8 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + kPStages * kPStage);
   uint64_t *empty = full + kPStages;
   uint64_t *accf = empty + kPStages;
-  uint64_t *acce = accf + 1;
-  uint64_t *mma_done = acce + 1;
+  uint64_t *acce = accf + 2;
+  uint64_t *mma_done = acce + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
@@ -151,8 +154,10 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(accf, 1);
-    tc::mbar_init(acce, kPEpi);
+    for (int b = 0; b < 2; b++) {
+      tc::mbar_init(&accf[b], 1);
+      tc::mbar_init(&acce[b], kPEpi);
+    }
     tc::mbar_init(mma_done, 1);
     *abort_flag = 0;
     tc::fence_barrier_init();
@@ -210,12 +215,15 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
       bool ok = true;
       for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
         for (int64_t ch = 0; ch < nch && ok; ch++, cc++) {
-          // one accumulator: wait until the epilogue has read the last chunk
-          if (!tc::mbar_wait(acce, uint32_t(cc & 1) ^ 1u, abort_flag, wc)) {
+          // two accumulator sets: wait until the epilogue has read the set's
+          // previous chunk
+          const int buf = int(cc & 1);
+          if (!tc::mbar_wait(&acce[buf], uint32_t((cc >> 1) & 1) ^ 1u, abort_flag, wc)) {
             ok = false;
             break;
           }
           tc::tc_fence_after();
+          const uint32_t d = tmem_base + uint32_t(buf * kPAcc);
           const int64_t kb0 = ch * kPChunkKb;
           const int64_t kb1 = kb0 + kPChunkKb < a.nk ? kb0 + kPChunkKb : a.nk;
           for (int64_t kb = kb0; kb < kb1; kb++, it++) {
@@ -238,16 +246,16 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
               const uint64_t aql = tc::smem_desc_kmajor(sa + 4 * kPA + k * 32, 64);
               const uint64_t b0 = tc::smem_desc_kmajor(sb + k * 32, 64);            // rows 0..
               const uint64_t b2 = tc::smem_desc_kmajor(sb + 2 * kPB + k * 32, 64);  // rows 64..
-              tc::umma_bf16(tmem_base + kR1, am, b0, id160, acc);
-              tc::umma_bf16(tmem_base + kR2, azh, b0, id64, acc);
-              tc::umma_bf16(tmem_base + kR2, azl, b0, id64, 1u);
-              tc::umma_bf16(tmem_base + kR3, azh, b2, id32, acc);
-              tc::umma_bf16(tmem_base + kR4, aqh, b0, id32, acc);
-              tc::umma_bf16(tmem_base + kR4, aql, b0, id32, 1u);
+              tc::umma_bf16(d + kR1, am, b0, id160, acc);
+              tc::umma_bf16(d + kR2, azh, b0, id64, acc);
+              tc::umma_bf16(d + kR2, azl, b0, id64, 1u);
+              tc::umma_bf16(d + kR2 + 32, azh, b2, id32, 1u);  // after the two above
+              tc::umma_bf16(d + kR4, aqh, b0, id32, acc);
+              tc::umma_bf16(d + kR4, aql, b0, id32, 1u);
             }
             tc::umma_commit(&empty[s]);
           }
-          if (ok) tc::umma_commit(accf);
+          if (ok) tc::umma_commit(&accf[buf]);
         }
       }
       if (!ok) *abort_flag = 1;
@@ -268,13 +276,14 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
 #pragma unroll
       for (int j = 0; j < 8; j++) sN[j] = sA[j] = sB[j] = sAA[j] = sBB[j] = sAB[j] = 0.f;
       for (int64_t ch = 0; ch < nch; ch++, cc++) {
-        const bool got = tc::mbar_wait(accf, uint32_t(cc & 1), abort_flag, wc);
+        const int buf = int(cc & 1);
+        const bool got = tc::mbar_wait(&accf[buf], uint32_t((cc >> 1) & 1), abort_flag, wc);
         if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
         tc::tc_fence_after();
-        const uint32_t tb = tmem_base + lanes + uint32_t(part * 8);
+        const uint32_t tb = tmem_base + lanes + uint32_t(buf * kPAcc + part * 8);
         float v[16];
         tmem_ld8x2(tb + kR1, tb + kR1 + 32, v);  // N, Sb hi
 #pragma unroll
@@ -294,15 +303,15 @@ pairwise_tc_kernel(const __grid_constant__ PairwiseArgs a, const tc::WaitCfg wc)
           sBB[j] += v[j];
           sA[j] += v[8 + j];
         }
-        tmem_ld8x2(tb + kR2 + 32, tb + kR3, v);  // Sab (hi.hi + lo.hi), Sab (hi.lo)
+        tmem_ld8x2(tb + kR2 + 32, tb + kR4, v);  // Sab (hi.hi + lo.hi + hi.lo), Saa
 #pragma unroll
-        for (int j = 0; j < 8; j++) sAB[j] += v[j] + v[8 + j];
-        tmem_ld8x2(tb + kR4, tb + kR4, v);  // Saa (loaded twice: the pair form)
-#pragma unroll
-        for (int j = 0; j < 8; j++) sAA[j] += v[j];
+        for (int j = 0; j < 8; j++) {
+          sAB[j] += v[j];
+          sAA[j] += v[8 + j];
+        }
         tc::tc_fence_before();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(acce);
+        if (lane == 0) tc::mbar_arrive(&acce[buf]);
       }
       if (!ok) break;
       const int64_t r = int64_t(tl.x) + q * 32 + lane;
