@@ -332,8 +332,8 @@ def run_ours(args, ranks: Ranks):
         g.set_gram_path(headline)
 
     # end to end through the host C ABI, copies inside the timed region: with
-    # ordinary pageable numpy buffers (what R's .C hands the library: gt_pmcc
-    # page-locks them for the call), and with page-locked buffers
+    # ordinary pageable numpy buffers (what R's .C hands the library; gt_pmcc
+    # runs the banded pipeline into them), and with page-locked buffers
     del corr, ts, pairs
     torch.cuda.empty_cache()
     e2e_steps = max(3, args.steps // 4)
