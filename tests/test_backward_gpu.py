@@ -45,7 +45,9 @@ def path(request, gpu):
     g.set_gram_path(old)
 
 
-@pytest.mark.parametrize("p,n,sym", [(32, 64, True), (100, 257, False), (300, 1000, True)])
+@pytest.mark.parametrize("p,n,sym", [(32, 64, True), (100, 257, False), (300, 1000, True),
+                                     (3, 5, False), (2, 7, True), (65, 130, False),
+                                     (129, 64, True)])
 def test_cor_backward_vs_oracle(gpu, oracle_mod, path, p, n, sym):
     rng = np.random.default_rng(p + n)
     X = (rng.standard_normal((p, n)) * 2 + 10).astype(np.float32)
@@ -55,6 +57,17 @@ def test_cor_backward_vs_oracle(gpu, oracle_mod, path, p, n, sym):
     got = cor_bwd_device(gpu, X, G)
     want = oracle_mod.cor_backward(X, G.astype(np.float64))
     assert rel(got, want) <= TOL[path], rel(got, want)
+
+
+def test_cor_backward_single_variable(gpu, path):
+    """One variable: C = 1 whatever X is, so the gradient is zero; what the
+    kernels return is rounding at the scale |G| / |x - mean| of the terms."""
+    rng = np.random.default_rng(4)
+    X = (rng.standard_normal((1, 5)) * 3 + 1).astype(np.float32)
+    G = np.array([[2.5]], np.float32)
+    got = cor_bwd_device(gpu, X, G)
+    scale = abs(float(G[0, 0])) / float(np.linalg.norm(X - X.mean()))
+    assert np.abs(got).max() <= 1e-5 * scale
 
 
 def test_cor_backward_constant_variable_has_zero_gradient(gpu, oracle_mod, path):
