@@ -122,7 +122,7 @@ def test_dist_backward_vs_oracle(gpu, oracle_mod, n, d):
         assert rel(got, want) <= 2e-5, rel(got, want)
 
 
-@pytest.mark.parametrize("n,d", [(64, 32), (1000, 32), (8192, 32)])
+@pytest.mark.parametrize("n,d", [(64, 32), (1000, 32), (8192, 32), (5000, 16), (3, 8)])
 def test_mds_stress_vs_oracle(gpu, oracle_mod, n, d):
     import gputools_gb300 as g
     rng = np.random.default_rng(n)
@@ -166,7 +166,7 @@ def _dist_bwd(lib, X, G):
 
 
 @pytest.mark.parametrize("n,d,offset", [(700, 65, 0.0), (1000, 128, 50.0), (600, 512, 3.0),
-                                        (130, 1000, 0.0)])
+                                        (130, 1000, 0.0), (12, 100, 1.0)])
 def test_dist_backward_tensor_core_dims(gpu, oracle_mod, n, d, offset):
     """Above 64 dimensions: GEMMs plus the rank-1 correction, on points with a
     common offset (the centring keeps the two terms from cancelling) and a
