@@ -99,3 +99,33 @@ def test_dist_object_layout():
     # R order: (2,1),(3,1),(4,1),(3,2),(4,2),(4,3)
     assert list(d.values) == [m[1, 0], m[2, 0], m[3, 0], m[2, 1], m[3, 1], m[3, 2]]
     np.testing.assert_array_equal(d.to_matrix(), m)
+
+
+def test_problem_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the batch problem structs have the header's size
+    and field offsets (a C program compiled against the header prints them)."""
+    from gputools_gb300 import _lib
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stddef.h>\n#include <stdio.h>\n#include "gputools_gb300.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gt_cor_problem),\n'
+        "         offsetof(gt_cor_problem, X), offsetof(gt_cor_problem, p),\n"
+        "         offsetof(gt_cor_problem, n), offsetof(gt_cor_problem, corr),\n"
+        "         offsetof(gt_cor_problem, ts), offsetof(gt_cor_problem, pairs),\n"
+        "         offsetof(gt_cor_problem, ld));\n"
+        '  printf("%zu %zu %zu %zu %zu\\n", sizeof(gt_kendall_problem),\n'
+        "         offsetof(gt_kendall_problem, X), offsetof(gt_kendall_problem, p),\n"
+        "         offsetof(gt_kendall_problem, n), offsetof(gt_kendall_problem, out));\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    lines = subprocess.run([str(exe)], capture_output=True, text=True,
+                           check=True).stdout.split("\n")
+    cor = [int(v) for v in lines[0].split()]
+    ken = [int(v) for v in lines[1].split()]
+    C, K = _lib.CorProblem, _lib.KendallProblem
+    assert cor == [ctypes.sizeof(C)] + [getattr(C, f).offset
+                                        for f in ("X", "p", "n", "corr", "ts", "pairs", "ld")]
+    assert ken == [ctypes.sizeof(K)] + [getattr(K, f).offset for f in ("X", "p", "n", "out")]
