@@ -7,11 +7,18 @@
 // (inst/cuda/distance.cu:40-78 and siblings, inst/cuda/correlation.cu:7-292).
 // Here a 256-thread CTA computes a BM x BN output tile: operand rows are
 // staged through shared memory in BK = 16 float slabs with 128-bit coalesced
-// loads (register double-buffered), and each thread keeps TM x TN
-// accumulators.  Thread (ty, tx) owns rows ty + 16 i and columns tx + 16 j, so
-// lanes of a warp touch consecutive output columns (coalesced stores) and the
-// padded 20-float shared rows are read conflict-free.  For symmetric problems
-// only tiles with ti <= tj run; off-diagonal tiles also store the mirror.
+// loads (register double-buffered), stored k-major (one shared row per k, all
+// of the slab's points side by side), and each thread keeps TM x TN
+// accumulators.  Thread (ty, tx) owns the rows 64 g + 4 ty + e (g < TM / 4,
+// e < 4) and the columns tx + 16 j, so lanes of a warp touch consecutive
+// output columns and the stores coalesce.  The column slab is stored
+// permuted so that the thread's columns 16 (4 g + e) + tx sit side by side
+// too: each k step reads TM / 4 + TN / 4 conflict-free 128-bit words and
+// holds only TM + TN operand values, so the 8 x 8 tiles of single-accumulator
+// reductions fit 128 registers and two CTAs share an SM: one CTA's slab
+// loads and output stores run under the other's arithmetic.  Every entry
+// still sums its k terms in ascending order.  For symmetric problems only
+// tiles with ti <= tj run; off-diagonal tiles also store the mirror.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,7 +31,21 @@ namespace gt {
 
 constexpr int kSimtThreads = 256;
 constexpr int kSimtBK = 16;
-constexpr int kSimtLd = 20;  // padded shared row (floats); 80 B keeps float4 alignment
+
+// k-major shared slab of ROWS points: row k holds the points' values at k,
+// padded by 4 floats (keeps 16-byte alignment; the slab stores then meet at
+// most two-way bank conflicts)
+template <int ROWS>
+constexpr int simt_ld() { return ROWS + 4; }
+
+// The shared row of the thread's accumulator row i: 64 (i / 4) + 4 ty + i % 4.
+__device__ __forceinline__ int simt_row(int i, int ty) { return 64 * (i >> 2) + 4 * ty + (i & 3); }
+
+// Where the column slab keeps tile column c = 16 j + t: 64 (j / 4) + 4 t + j % 4.
+__device__ __forceinline__ int simt_col_pos(int c) {
+  const int j = c >> 4, t = c & 15;
+  return 64 * (j >> 2) + 4 * t + (j & 3);
+}
 
 struct SimtArgs {
   const float *R;  // row operand: nr rows of K floats, stride ldr
@@ -59,13 +80,20 @@ __device__ __forceinline__ void simt_load(float4 (&reg)[ROWS * 4 / kSimtThreads]
   }
 }
 
-template <int ROWS>
+// Stores a loaded slab k-major: value k of row `row` at sm[k * LD + row], or
+// for the column slab (COLS) at sm[k * LD + simt_col_pos(row)].
+template <int ROWS, bool COLS>
 __device__ __forceinline__ void simt_store(float *sm, const float4 (&reg)[ROWS * 4 / kSimtThreads]) {
+  constexpr int LD = simt_ld<ROWS>();
 #pragma unroll
   for (int s = 0; s < ROWS * 4 / kSimtThreads; s++) {
     int q = threadIdx.x + s * kSimtThreads;
     int row = q >> 2, c4 = q & 3;
-    *reinterpret_cast<float4 *>(sm + row * kSimtLd + c4 * 4) = reg[s];
+    float *p = sm + (c4 * 4) * LD + (COLS ? simt_col_pos(row) : row);
+    p[0] = reg[s].x;
+    p[LD] = reg[s].y;
+    p[2 * LD] = reg[s].z;
+    p[3 * LD] = reg[s].w;
   }
 }
 
@@ -96,17 +124,24 @@ struct HasStagedMirror : std::false_type {};
 template <class T>
 struct HasStagedMirror<T, std::void_t<decltype(T::kStagedMirror)>>
     : std::bool_constant<T::kStagedMirror> {};
+// Two CTAs per SM (at most 128 registers a thread) where the accumulators
+// leave room: up to 64 of them.
+template <int TM, int TN, int NACC>
+constexpr int simt_min_blocks() { return TM * TN * NACC <= 64 ? 2 : 1; }
+
 template <class Op, class Out, int TM, int TN>
-__global__ void __launch_bounds__(kSimtThreads)
+__global__ void __launch_bounds__(kSimtThreads, simt_min_blocks<TM, TN, Op::NACC>())
 allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   constexpr int BM = 16 * TM, BN = 16 * TN, NA = Op::NACC;
+  constexpr int LDA = simt_ld<BM>(), LDB = simt_ld<BN>();
+  static_assert(TM % 4 == 0 && TN % 4 == 0, "rows and columns are owned in groups of four");
   if (a.run_if && *a.run_if == 0) return;  // a gated launch whose gate is closed
   const int ti = blockIdx.y, tj = blockIdx.x;
   if (a.symmetric && ti > tj) return;
   const int64_t row0 = int64_t(ti) * BM, col0 = int64_t(tj) * BN;
 
-  __shared__ __align__(16) float sA[2][BM * kSimtLd];
-  __shared__ __align__(16) float sB[2][BN * kSimtLd];
+  __shared__ __align__(16) float sA[2][kSimtBK * LDA];
+  __shared__ __align__(16) float sB[2][kSimtBK * LDB];
 
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   float acc[TM][TN][NA];
@@ -118,8 +153,8 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   float4 ra[BM * 4 / kSimtThreads], rb[BN * 4 / kSimtThreads];
   simt_load<BM, Op>(ra, a.R, a.ldr, a.nr, row0, 0, a.K, a.vec_ok);
   simt_load<BN, Op>(rb, a.C, a.ldc, a.nc, col0, 0, a.K, a.vec_ok);
-  simt_store<BM>(sA[0], ra);
-  simt_store<BN>(sB[0], rb);
+  simt_store<BM, false>(sA[0], ra);
+  simt_store<BN, true>(sB[0], rb);
   __syncthreads();
 
   const int64_t nk = (a.K + kSimtBK - 1) / kSimtBK;
@@ -130,32 +165,38 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
       simt_load<BM, Op>(ra, a.R, a.ldr, a.nr, row0, (kb + 1) * kSimtBK, a.K, a.vec_ok);
       simt_load<BN, Op>(rb, a.C, a.ldc, a.nc, col0, (kb + 1) * kSimtBK, a.K, a.vec_ok);
     }
-    const float *pa = sA[buf];
-    const float *pb = sB[buf];
+    const float *pa = sA[buf] + 4 * ty;
+    const float *pb = sB[buf] + 4 * tx;
 #pragma unroll
-    for (int kk = 0; kk < kSimtBK / 4; kk++) {
+    for (int kk = 0; kk < kSimtBK; kk++) {
       if constexpr (SkipPad<Op>::value) {
-        if (kb * kSimtBK + kk * 4 >= a.K) break;  // the last slab's padding (uniform)
+        if (kb * kSimtBK + kk >= a.K) break;  // the last slab's padding (uniform)
       }
-      float4 av[TM];
+      float av[TM], bv[TN];
+#pragma unroll
+      for (int g = 0; g < TM / 4; g++) {
+        const float4 v = *reinterpret_cast<const float4 *>(pa + kk * LDA + 64 * g);
+        av[4 * g] = v.x;
+        av[4 * g + 1] = v.y;
+        av[4 * g + 2] = v.z;
+        av[4 * g + 3] = v.w;
+      }
+#pragma unroll
+      for (int g = 0; g < TN / 4; g++) {
+        const float4 v = *reinterpret_cast<const float4 *>(pb + kk * LDB + 64 * g);
+        bv[4 * g] = v.x;
+        bv[4 * g + 1] = v.y;
+        bv[4 * g + 2] = v.z;
+        bv[4 * g + 3] = v.w;
+      }
 #pragma unroll
       for (int i = 0; i < TM; i++)
-        av[i] = *reinterpret_cast<const float4 *>(pa + (ty + 16 * i) * kSimtLd + kk * 4);
 #pragma unroll
-      for (int j = 0; j < TN; j++) {
-        const float4 bv = *reinterpret_cast<const float4 *>(pb + (tx + 16 * j) * kSimtLd + kk * 4);
-#pragma unroll
-        for (int i = 0; i < TM; i++) {
-          op.step(acc[i][j], av[i].x, bv.x);
-          op.step(acc[i][j], av[i].y, bv.y);
-          op.step(acc[i][j], av[i].z, bv.z);
-          op.step(acc[i][j], av[i].w, bv.w);
-        }
-      }
+        for (int j = 0; j < TN; j++) op.step(acc[i][j], av[i], bv[j]);
     }
     if (more) {
-      simt_store<BM>(sA[buf ^ 1], ra);
-      simt_store<BN>(sB[buf ^ 1], rb);
+      simt_store<BM, false>(sA[buf ^ 1], ra);
+      simt_store<BN, true>(sB[buf ^ 1], rb);
     }
     __syncthreads();
   }
@@ -167,11 +208,11 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
       // (now idle) operand buffers: each warp writes 32 consecutive floats of
       // a mirrored row per store
       constexpr int kLdT = BN + 1;
-      static_assert(32 * kLdT <= 2 * BM * kSimtLd, "a 32-row chunk fits the operand buffers");
+      static_assert(32 * kLdT <= 2 * kSimtBK * LDA, "a 32-row chunk fits the operand buffers");
       float *T = &sA[0][0];
 #pragma unroll
       for (int i = 0; i < TM; i++) {
-        const int64_t r = row0 + ty + 16 * i;
+        const int64_t r = row0 + simt_row(i, ty);
 #pragma unroll
         for (int j = 0; j < TN; j++) {
           const int64_t c = col0 + tx + 16 * j;
@@ -184,11 +225,13 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
 #pragma unroll
       for (int q = 0; q < BM / 32; q++) {
         __syncthreads();  // the previous chunk (or the main loop) is done with T
+        // rows 32 q .. 32 q + 31: four rows of each thread of half the tile's ty
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const int i = 2 * q + h;  // rows ty + 16 i of this chunk
+        for (int i = 0; i < TM; i++) {
+          const int lr = simt_row(i, ty) - 32 * q;
+          if (lr < 0 || lr >= 32) continue;
 #pragma unroll
-          for (int j = 0; j < TN; j++) T[(ty + 16 * h) * kLdT + tx + 16 * j] = acc[i][j][0];
+          for (int j = 0; j < TN; j++) T[lr * kLdT + tx + 16 * j] = acc[i][j][0];
         }
         __syncthreads();
         const int64_t r = row0 + 32 * q + lane;
@@ -202,7 +245,7 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   }
 #pragma unroll
   for (int i = 0; i < TM; i++) {
-    const int64_t r = row0 + ty + 16 * i;
+    const int64_t r = row0 + simt_row(i, ty);
     if (r >= a.nr) continue;
 #pragma unroll
     for (int j = 0; j < TN; j++) {

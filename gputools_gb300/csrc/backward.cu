@@ -39,14 +39,6 @@ namespace {
 
 constexpr int64_t kKPadB = 64;
 
-// z of a variable in float arithmetic (0 for a flagged variable).
-struct ZCenter {
-  Centerer cen;
-  bool zero;
-  __device__ __forceinline__ explicit ZCenter(const ColStats &s) : cen(s), zero(s.flags != 0) {}
-  __device__ __forceinline__ float operator()(float x) const { return zero ? 0.f : cen(x); }
-};
-
 template <class T>
 __device__ __forceinline__ void put_parts(T *dst, int64_t plane, int64_t idx, float v, int ns);
 
