@@ -33,8 +33,9 @@ constexpr int kSimtThreads = 256;
 constexpr int kSimtBK = 16;
 
 // k-major shared slab of ROWS points: row k holds the points' values at k,
-// padded by 4 floats (keeps 16-byte alignment; the slab stores then meet at
-// most two-way bank conflicts)
+// padded by 4 floats (keeps 16-byte alignment).  The slab stores, one 4-byte
+// store per k step and thread, meet two-way (row slab) or four-way (permuted
+// column slab) bank conflicts; the operand reads meet none.
 template <int ROWS>
 constexpr int simt_ld() { return ROWS + 4; }
 
