@@ -116,10 +116,18 @@ __device__ __forceinline__ void simt_store(float *sm, const float4 (&reg)[ROWS *
 //                                              at K instead of computing its padding
 //                                              (for costly steps or small K; the
 //                                              check slows the cheap steps down)
+//   static constexpr int kUnrollK = u;         optional: unroll the slab's k loop
+//                                              u times (default: fully); a fully
+//                                              unrolled slab of a long step outgrows
+//                                              the instruction cache
 template <class T, class = void>
 struct SkipPad : std::false_type {};
 template <class T>
 struct SkipPad<T, std::void_t<decltype(T::kSkipPad)>> : std::bool_constant<T::kSkipPad> {};
+template <class T, class = void>
+struct UnrollK : std::integral_constant<int, kSimtBK> {};
+template <class T>
+struct UnrollK<T, std::void_t<decltype(T::kUnrollK)>> : std::integral_constant<int, T::kUnrollK> {};
 template <class T, class = void>
 struct HasStagedMirror : std::false_type {};
 template <class T>
@@ -135,6 +143,7 @@ __global__ void __launch_bounds__(kSimtThreads, simt_min_blocks<TM, TN, Op::NACC
 allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
   constexpr int BM = 16 * TM, BN = 16 * TN, NA = Op::NACC;
   constexpr int LDA = simt_ld<BM>(), LDB = simt_ld<BN>();
+  constexpr int KU = UnrollK<Op>::value;
   static_assert(TM % 4 == 0 && TN % 4 == 0, "rows and columns are owned in groups of four");
   if (a.run_if && *a.run_if == 0) return;  // a gated launch whose gate is closed
   const int ti = blockIdx.y, tj = blockIdx.x;
@@ -168,7 +177,7 @@ allpairs_simt_kernel(SimtArgs a, Op op, Out out) {
     }
     const float *pa = sA[buf] + 4 * ty;
     const float *pb = sB[buf] + 4 * tx;
-#pragma unroll
+#pragma unroll KU
     for (int kk = 0; kk < kSimtBK; kk++) {
       if constexpr (SkipPad<Op>::value) {
         if (kb * kSimtBK + kk >= a.K) break;  // the last slab's padding (uniform)
