@@ -410,11 +410,18 @@ struct OutStore {
 // ------------------------------------------------------------ distances
 constexpr int kDbRows = 128;   // rows i per CTA (one per thread)
 constexpr int kDbCols = 32;    // points j per shared tile
+static_assert(kDbRows / 32 == 4, "the coefficient copies step rows by four warps");
 
 // Asynchronous 4-byte copy global -> shared (cp.async); bytes = 0 fills zero.
 __device__ __forceinline__ void cp_async4(float *dst, const float *src, int bytes) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
                "r"(bytes)
+               : "memory");
+}
+// The same for 16 bytes (both addresses 16-byte aligned).
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)),
+               "l"(src), "r"(bytes)
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() {
@@ -465,43 +472,68 @@ dist_backward_kernel(const float *__restrict__ X, int64_t n, int64_t dim,
   const int64_t js = blockIdx.y;
   const int64_t jbeg = js * jchunk;
   const int64_t jend = (jbeg + jchunk < n) ? jbeg + jchunk : n;
-  // copies of the tile of points jt .. jt + 31 into buffer b (one commit group)
+  // points in 16-byte copies when every row starts on a 16-byte boundary
+  const bool vec = (dim & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  // copies of the tile of points jt .. jt + 31 into buffer b (one commit group);
+  // the indices step from row to row (no products per copy)
   auto issue = [&](int b, int64_t jt) {
     float *xb = xj + b * L::XJ;
-    for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
-      const int jj = e / DMAX, k = e - jj * DMAX;
-      const int64_t j = jt + jj;
-      const bool ok = j < jend && k < dim;
-      cp_async4(xb + e, ok ? X + j * dim + k : X, ok ? 4 : 0);
+    if (vec) {
+      for (int e = tid; e < kDbCols * DMAX / 4; e += kDbRows) {
+        const int jj = e / (DMAX / 4), k = 4 * (e - jj * (DMAX / 4));
+        const int64_t j = jt + jj;
+        const bool ok = j < jend && k < dim;
+        cp_async16(xb + 4 * e, ok ? X + j * dim + k : X, ok ? 16 : 0);
+      }
+    } else {
+      for (int e = tid; e < kDbCols * DMAX; e += kDbRows) {
+        const int jj = e / DMAX, k = e - jj * DMAX;
+        const int64_t j = jt + jj;
+        const bool ok = j < jend && k < dim;
+        cp_async4(xb + e, ok ? X + j * dim + k : X, ok ? 4 : 0);
+      }
     }
     float *ca = cfa + b * L::CFA;
     if (MODE == 0) {
       float *cb = cfb + b * L::CFB;
+      const int64_t gj = jt + lane;
+      int64_t gi = i0 + warp, off = gi * n + gj;  // G[gi][gj]
       for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
-        const int64_t gi = i0 + ii, gj = jt + lane;
         const bool ok = gi < n && gj < jend;
-        cp_async4(ca + ii * (kDbCols + 1) + lane, ok ? aux + gi * n + gj : aux, ok ? 4 : 0);
+        cp_async4(ca + ii * (kDbCols + 1) + lane, ok ? aux + off : aux, ok ? 4 : 0);
+        gi += kDbRows / 32;
+        off += (kDbRows / 32) * n;
       }
+      int64_t gj2 = jt, off2 = jt * n + i;  // G[gj2][i]
       for (int jj = 0; jj < kDbCols; jj++) {
-        const int64_t gj = jt + jj;
-        const bool ok = gj < jend && i < n;
-        cp_async4(cb + jj * (kDbRows + 1) + tid, ok ? aux + gj * n + i : aux, ok ? 4 : 0);
+        const bool ok = gj2 < jend && i < n;
+        cp_async4(cb + jj * (kDbRows + 1) + tid, ok ? aux + off2 : aux, ok ? 4 : 0);
+        gj2++;
+        off2 += n;
       }
     } else {
-      // delta in R dist layout: (a > b) at n*b - b*(b+1)/2 + a - b - 1; each
-      // cell comes from exactly one side of the diagonal (the diagonal and the
-      // cells past the tile are never read)
-      for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
-        const int64_t gi = i0 + ii, gj = jt + lane;
-        if (gi < n && gj < jend && gj > gi)
-          cp_async4(ca + ii * (kDbCols + 1) + lane, aux + (n * gi - gi * (gi + 1) / 2 + gj - gi - 1),
-                    4);
+      // delta in R dist layout: (a > b) at B(b) + a with B(b) = n b - b (b + 1) / 2 - b - 1;
+      // each cell comes from exactly one side of the diagonal (the diagonal and
+      // the cells past the tile are never read), and a side the tile does not
+      // reach is skipped whole
+      if (jt + kDbCols - 1 > i0) {  // cells with gj > gi: row gi, consecutive gj
+        const int64_t gj = jt + lane;
+        int64_t gi = i0 + warp, base = n * gi - gi * (gi + 1) / 2 - gi - 1;
+        for (int ii = warp; ii < kDbRows; ii += kDbRows / 32) {
+          if (gi < n && gj < jend && gj > gi)
+            cp_async4(ca + ii * (kDbCols + 1) + lane, aux + (base + gj), 4);
+          base += 4 * n - 4 * gi - 14;  // B(gi + 4) - B(gi)
+          gi += 4;
+        }
       }
-      for (int jj = 0; jj < kDbCols; jj++) {
-        const int64_t gj = jt + jj;
-        if (gj < jend && i < n && i > gj)
-          cp_async4(ca + tid * (kDbCols + 1) + jj, aux + (n * gj - gj * (gj + 1) / 2 + i - gj - 1),
-                    4);
+      if (i0 + kDbRows - 1 > jt) {  // cells with i > gj: row gj, this thread's i
+        int64_t gj = jt, base = n * gj - gj * (gj + 1) / 2 - gj - 1;
+        for (int jj = 0; jj < kDbCols; jj++) {
+          if (gj < jend && i < n && i > gj)
+            cp_async4(ca + tid * (kDbCols + 1) + jj, aux + (base + i), 4);
+          base += n - gj - 2;  // B(gj + 1) - B(gj)
+          gj++;
+        }
       }
     }
     cp_async_commit();

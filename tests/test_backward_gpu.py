@@ -122,7 +122,7 @@ def test_dist_backward_vs_oracle(gpu, oracle_mod, n, d):
         assert rel(got, want) <= 2e-5, rel(got, want)
 
 
-@pytest.mark.parametrize("n,d", [(64, 32), (1000, 32), (8192, 32), (5000, 16), (3, 8)])
+@pytest.mark.parametrize("n,d", [(64, 32), (1000, 32), (8192, 32), (5000, 16), (3, 8), (701, 13)])
 def test_mds_stress_vs_oracle(gpu, oracle_mod, n, d):
     import gputools_gb300 as g
     rng = np.random.default_rng(n)
