@@ -166,9 +166,10 @@ def _dist_bwd(lib, X, G):
 
 
 @pytest.mark.parametrize("n,d,offset", [(700, 65, 0.0), (1000, 128, 50.0), (600, 512, 3.0),
-                                        (130, 1000, 0.0), (12, 100, 1.0)])
+                                        (130, 1000, 0.0), (12, 100, 1.0), (8193, 40, 2.0)])
 def test_dist_backward_tensor_core_dims(gpu, oracle_mod, n, d, offset):
-    """Above 64 dimensions: GEMMs plus the rank-1 correction, on points with a
+    """Above 64 dimensions, and above 32 from 8192 points: GEMMs plus the
+    rank-1 correction, on points with a
     common offset (the centring keeps the two terms from cancelling) and a
     duplicated point (its zero distances contribute nothing)."""
     rng = np.random.default_rng(n + d)
@@ -180,7 +181,7 @@ def test_dist_backward_tensor_core_dims(gpu, oracle_mod, n, d, offset):
     assert rel(got, want) <= 2e-5, rel(got, want)
 
 
-@pytest.mark.parametrize("n,d", [(500, 128), (2048, 200)])
+@pytest.mark.parametrize("n,d", [(500, 128), (2048, 200), (8192, 48)])
 def test_mds_stress_tensor_core_dims(gpu, oracle_mod, n, d):
     import gputools_gb300 as g
     rng = np.random.default_rng(n + 1)
@@ -197,8 +198,8 @@ def test_mds_stress_tensor_core_dims(gpu, oracle_mod, n, d):
 
 
 def test_mds_stress_coincident_points_fused_path(gpu, oracle_mod):
-    """The fused path (<= 64 dimensions) counts coincident points in the
-    stress, as the oracle does."""
+    """The fused path (200 points x 16 dimensions) counts coincident points in
+    the stress, as the oracle does."""
     import gputools_gb300 as g
     rng = np.random.default_rng(77)
     X = rng.standard_normal((200, 16)).astype(np.float32)
