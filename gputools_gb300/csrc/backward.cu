@@ -17,9 +17,9 @@
 //
 // Distances.  dL/dx_i = sum_j W_ij (x_i - x_j) = x_i rowsum(W)_i - (W X)_i with
 // W_ij = (G_ij + G_ji) / D_ij (0 where D_ij = 0), or for MDS stress
-// W_ij = 2 (D_ij - delta_ij) / D_ij.  Up to 32 dimensions (64 below 8192
-// points) a fused CUDA-core kernel recomputes D_ij from the points and never
-// materialises W.  Otherwise the adjoint is GEMMs plus a rank-1 correction: D comes from the tcgen05
+// W_ij = 2 (D_ij - delta_ij) / D_ij.  Up to 32 dimensions (64 outside 8192 ..
+// 32768 points) a fused CUDA-core kernel recomputes D_ij from the points and
+// never materialises W.  Otherwise the adjoint is GEMMs plus a rank-1 correction: D comes from the tcgen05
 // Euclidean path (exact near-zero recomputation included), one pass over D
 // and G writes W as split-bf16 planes with its row sums, W X runs on the
 // tcgen05 GEMM, and dX = X diag(rowsum W) - W X is formed on the points
@@ -905,8 +905,9 @@ int launch_dist_backward(const float *X, int64_t n, int64_t dim, const float *au
   // measured: the tensor-core form is 10-15 % faster from 33 dimensions at 8192
   // points and more (the fused kernel pads 33-64 dimensions to 64 and runs two
   // CTAs per SM there), equal at 4096 points, and up to 2.5 times slower at 32
-  // dimensions and fewer
-  if (dim > 64 || (dim > 32 && n >= 8192))
+  // dimensions and fewer.  It holds about 10 n^2 bytes of workspace, so above
+  // 32768 points (11 GB) the fused kernel, which holds none, keeps those sizes.
+  if (dim > 64 || (dim > 32 && n >= 8192 && n <= 32768))
     return dist_backward_tc<MODE>(X, n, dim, aux, dX, loss, s);
   const int64_t ib = cdiv(n, kDbRows);
   // the kernel for the dimension, its shared memory, and the CTAs per SM

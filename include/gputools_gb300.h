@@ -275,10 +275,10 @@ int gt_cor_backward_device(const float *d_X, int64_t p, int64_t n,
 
 /* dL/dX of the Euclidean distances D of the rows of X (n x dim row-major)
  * given G = dL/dD (n x n, G[i*n + j]); terms with D_ij = 0 contribute 0.
- * Up to 32 dimensions, and up to 64 below 8192 points, one fused CUDA-core
- * pass (D recomputed, nothing n x n stored); otherwise D from the tensor-core
- * distance path, W = (G + G^T) / D as split-bf16 planes and W X on the tensor
- * cores (about 10 n^2 bytes of device workspace). */
+ * Up to 32 dimensions, and up to 64 outside 8192..32768 points, one fused
+ * CUDA-core pass (D recomputed, nothing n x n stored); otherwise D from the
+ * tensor-core distance path, W = (G + G^T) / D as split-bf16 planes and W X on
+ * the tensor cores (about 10 n^2 bytes of device workspace). */
 int gt_dist_backward_device(const float *d_X, int64_t n, int64_t dim,
                             const float *d_G, float *d_dX, void *stream);
 
