@@ -114,6 +114,24 @@ def test_cfg_4000x100_rows_sampled(gpu, oracle_mod, rng):
         check_close(got[rows], want)
 
 
+def test_large_tiles_ragged_k_rows_sampled(gpu, oracle_mod, rng):
+    """3100 points take the 128 x 128 tiles of the CUDA-core engine; 17
+    dimensions leave one value in the second k-slab, and 3100 = 24 x 128 + 28
+    leaves a ragged last tile row."""
+    base = rng.standard_normal((3100, 17)).astype(np.float32)
+    base[base > 1.5] = 0.0  # zero coordinates: canberra's 0/0 terms
+    bern = (rng.random((3100, 17)) < 0.3).astype(np.float32)
+    rows = np.concatenate([rng.choice(3072, 12, replace=False), np.arange(3090, 3100)])
+    for m in METHODS:
+        pts = bern if m == "binary" else base
+        p = 3.0 if m == "minkowski" else 2.0
+        got = rdistances(gpu, pts, m, p)
+        want = oracle_mod.dist(pts, m, p, b=pts[rows])
+        want[np.arange(len(rows)), rows] = 0.0
+        check_close(got[rows], want)
+        assert np.array_equal(got, got.T), m
+
+
 def test_device_layouts_agree(gpu, rng):
     import torch
     import gputools_gb300 as g

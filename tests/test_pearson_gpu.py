@@ -88,6 +88,31 @@ def test_everything_two_sets(gpu, oracle_mod, rng, path, na, nb, n):
     check_ts(ts, corr, pairs, wt, wc)
 
 
+def test_fp32_large_tiles_rows_sampled(gpu, oracle_mod, rng):
+    """3200 variables (one set) and 2500 x 2400 (two sets) take the 128 x 128
+    tiles of the CUDA-core Gram on the FP32 path; sampled rows, the ragged
+    last tile rows among them, against the oracle."""
+    import gputools_gb300 as g
+    old = g.get_gram_path()
+    g.set_gram_path("fp32")
+    try:
+        X = rng.standard_normal((3200, 150)).astype(np.float32)
+        corr, pairs, ts = rpmcc(gpu, 0, X, X.copy())
+        rows = np.concatenate([rng.choice(3072, 10, replace=False), np.arange(3190, 3200)])
+        wc, wp, wt = oracle_mod.pearson(X[rows], X, use=0)
+        check_r(corr[rows], wc, tol("fp32", 150))
+        assert np.array_equal(corr, corr.T)
+        A = rng.standard_normal((2500, 60)).astype(np.float32)
+        B = (rng.standard_normal((2400, 60)) * 3 - 2).astype(np.float32)
+        corr, pairs, ts = rpmcc(gpu, 0, A, B)
+        rows = np.concatenate([rng.choice(2432, 10, replace=False), np.arange(2490, 2500)])
+        wc, wp, wt = oracle_mod.pearson(A[rows], B, use=0)
+        check_r(corr[rows], wc, tol("fp32", 60))
+        assert np.array_equal(pairs, np.full_like(pairs, 60.0))
+    finally:
+        g.set_gram_path(old)
+
+
 @pytest.mark.parametrize("p,n", [(2, 5), (65, 40), (300, 500), (513, 129)])
 def test_everything_symmetric_copies(gpu, oracle_mod, rng, path, p, n):
     """gpuCor(x): R passes two copies of x through .C; the library recognises
