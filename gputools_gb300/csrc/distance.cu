@@ -15,7 +15,7 @@
 //    (inst/cuda/distance.cu:294), so the two differ only when zeros occur.
 //  * minkowski evaluates |a-b|^p exactly for p = 1, 2, 3 and with powf
 //    otherwise (the reference uses the low-accuracy __powf, :471, :487); the
-//    final root is taken in double.
+//    final root is FP32 (cbrtf for p = 3, else 2^(log2(s) / p)).
 #include "common.cuh"
 #include "allpairs_simt.cuh"
 #include "kernels.cuh"
@@ -93,6 +93,29 @@ struct OpBinaryBits {
   __device__ float finish(const float (&c)[2], int64_t) const {
     const float d = float(__float_as_int(c[1]));
     return d != 0.f ? float(__float_as_int(c[0])) / d : 0.f;
+  }
+};
+
+// The same counts packed in one 32-bit accumulator (bits on in either << 16 |
+// bits on in exactly one), for fewer than 65536 coordinates, where neither
+// count can carry out of its half: a single-accumulator operation, so large
+// problems take the 128 x 128 tiles (the binary kernel spends its time per
+// tile, not on its two words of arithmetic per pair).
+struct OpBinaryPacked {
+  static constexpr int NACC = 1;
+  static constexpr bool kSkipPad = true;
+  static constexpr int kUnrollK = 1;  // a few words per point: the slab's loop stops early
+  __device__ static float pad() { return 0.f; }
+  __device__ void init(float (&c)[1]) const { c[0] = __uint_as_float(0u); }
+  __device__ void step(float (&c)[1], float a, float b) const {
+    const unsigned x = __float_as_uint(a), y = __float_as_uint(b);
+    c[0] = __uint_as_float(__float_as_uint(c[0]) + __popc(x ^ y) +
+                           (unsigned(__popc(x | y)) << 16));
+  }
+  __device__ float finish(const float (&c)[1], int64_t) const {
+    const unsigned v = __float_as_uint(c[0]);
+    const float d = float(int(v >> 16));
+    return d != 0.f ? float(int(v & 0xffffu)) / d : 0.f;
   }
 };
 
@@ -215,8 +238,11 @@ int dist_simt(const float *d_pts, int64_t n, int64_t dim, float *d_out, int layo
                                                              static_cast<unsigned *>(pb));
     count_launch();
     e = cudaGetLastError();
-    if (e == cudaSuccess)
-      e = run_metric(OpBinaryBits{}, static_cast<const float *>(pb), n, words, d_out, layout, st);
+    if (e == cudaSuccess) {
+      const float *bits = static_cast<const float *>(pb);
+      e = dim < 65536 ? run_metric(OpBinaryPacked{}, bits, n, words, d_out, layout, st)
+                      : run_metric(OpBinaryBits{}, bits, n, words, d_out, layout, st);
+    }
     break;
   }
   case GT_MINKOWSKI:

@@ -177,6 +177,26 @@ def test_binary_exact(gpu, rng, n, d):
     np.testing.assert_array_equal(got.view(np.int32), want.view(np.int32))
 
 
+@pytest.mark.parametrize("n,d", [(3200, 70), (40, 70000)])
+def test_binary_exact_large(gpu, rng, n, d):
+    """3200 points take the 128 x 128 tiles with both counts packed in one
+    accumulator; 70000 coordinates (counts past 16 bits) keep them apart.
+    Bit for bit against the float32 quotient of the exact counts."""
+    pts = (rng.random((n, d)) < 0.2).astype(np.float32)
+    pts[3] = 0.0
+    pts[7, ::5] = np.nan
+    nz = (pts != 0).astype(np.float64)
+    both = nz @ nz.T                       # exact: integers below 2^53
+    cnt = nz.sum(1)
+    x = (cnt[:, None] + cnt[None, :] - 2 * both).astype(np.float32)
+    o = (cnt[:, None] + cnt[None, :] - both).astype(np.float32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        want = np.where(o != 0, x / np.where(o != 0, o, 1), 0).astype(np.float32)
+    np.fill_diagonal(want, 0.0)
+    got = rdistances(gpu, pts, "binary")
+    np.testing.assert_array_equal(got.view(np.int32), want.view(np.int32))
+
+
 def test_canberra_extreme_operands(gpu, oracle_mod, rng):
     # |a - b| / |a + b| at a = -b (an infinite term), with subnormal and tiny
     # magnitudes and zero coordinates: float results agree with the FP64
