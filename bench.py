@@ -56,15 +56,20 @@ def dist_env():
 
 
 class Ranks:
-    def __init__(self):
+    """One process per GPU under torchrun (NCCL); "gloo" runs the same barrier
+    and max-over-ranks on CPU tensors (the multi-process tests)."""
+
+    def __init__(self, backend: str = "nccl"):
         self.world, self.rank, self.local = dist_env()
         self.dist = None
+        self.device = "cuda" if backend == "nccl" else "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local)
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
             os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            dist.init_process_group("nccl")
+            dist.init_process_group(backend)
             self.dist = dist
 
     def barrier(self):
@@ -75,7 +80,7 @@ class Ranks:
         if not self.dist:
             return v
         import torch
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
 
