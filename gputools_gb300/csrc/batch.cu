@@ -343,9 +343,9 @@ int pearson_batch_plan(const gt_cor_problem *probs, int64_t count, int flags,
     }
     cache_store(key, choice);
     best->config_ms = best_ms;
-    char tmp[160];
+    char tmp[sizeof(best->config) + 64];
     std::snprintf(tmp, sizeof(tmp), "%s, tuned %.3f ms", best->config, best_ms);
-    std::snprintf(best->config, sizeof(best->config), "%s", tmp);
+    std::snprintf(best->config, sizeof(best->config), "%.*s", int(sizeof(best->config) - 1), tmp);
     int st = plan_finalize(best, flags);
     if (st != GT_OK) {
       plan_free(best);

@@ -1681,8 +1681,7 @@ int pearson_batch_prepare(const gt_cor_problem *probs, int64_t count, int kind, 
     const gt_cor_problem &q = probs[i];
     if (q.p == 0) continue;
     const PearsonBatchInput &b = inputs[pidx++];
-    PearsonBatchProblem d;
-    std::memset(&d, 0, sizeof(d));
+    PearsonBatchProblem d{};  // value-initialised: zero bytes, padding included
     GT_TRY(make_plane_map(&d.map_a, planes + b.plane_off, b.p, b.kpad, nsplit, kBM, bk, f16));
     GT_TRY(make_plane_map(&d.map_b, planes + b.plane_off, b.p, b.kpad, nsplit, kBN, bk, f16));
     d.ts = make_tiles(b.p, b.p, kUpper, band_group(int64_t(kBN) * b.kpad * 2 * nsplit));
