@@ -13,9 +13,9 @@
 //    denominator only (a = -b != 0) is +Inf.  The reference kernel instead
 //    skips every zero-denominator term and never rescales
 //    (inst/cuda/distance.cu:294), so the two differ only when zeros occur.
-//  * minkowski evaluates |a-b|^p exactly for p = 1, 2, 3 and with powf
-//    otherwise (the reference uses the low-accuracy __powf, :471, :487); the
-//    final root is FP32 (cbrtf for p = 3, else 2^(log2(s) / p)).
+//  * minkowski evaluates |a-b|^p exactly for p = 1, 2, 3 and as
+//    2^(p log2 |a-b|) otherwise (the reference uses the low-accuracy __powf,
+//    :471, :487); the final root is FP32 (cbrtf for p = 3, else 2^(log2(s) / p)).
 #include "common.cuh"
 #include "allpairs_simt.cuh"
 #include "kernels.cuh"
@@ -154,7 +154,12 @@ struct OpMinkP {
   float p;
   __device__ static float pad() { return 0.f; }
   __device__ void init(float (&c)[1]) const { c[0] = 0.f; }
-  __device__ void step(float (&c)[1], float a, float b) const { c[0] += powf(fabsf(a - b), p); }
+  // |a - b|^p as 2^(p log2 |a - b|) (0, Inf and NaN come out as from powf;
+  // relative error about 2 |p log2 |a - b|| ulp, against powf's 1 ulp, at less
+  // than half of powf's instructions)
+  __device__ void step(float (&c)[1], float a, float b) const {
+    c[0] += exp2f(p * log2f(fabsf(a - b)));
+  }
   // s^(1/p) in FP32 as 2^(log2(s) / p): relative error about |log2 s| ulp
   __device__ float finish(const float (&c)[1], int64_t) const {
     return c[0] > 0.f ? exp2f(__fdiv_rn(log2f(c[0]), p)) : c[0];
