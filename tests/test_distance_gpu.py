@@ -70,6 +70,18 @@ def test_minkowski_powers(gpu, oracle_mod, rng, p):
     check_close(got, want, rtol=5e-5)
 
 
+@pytest.mark.parametrize("p", [0.5, 2.5, 4.0, 7.0])
+def test_minkowski_wide_range(gpu, oracle_mod, rng, p):
+    """Coordinates over nine decades (no term leaves the float range): the
+    terms 2^(p log2 |a - b|) keep the float tolerance where |p log2 |a - b||
+    is large."""
+    pts = (rng.standard_normal((60, 11)) * 10.0 ** rng.uniform(-5, 4, (60, 11))).astype(np.float32)
+    got = rdistances(gpu, pts, "minkowski", p)
+    want = oracle_mod.dist(pts, "minkowski", p)
+    np.fill_diagonal(want, 0.0)
+    check_close(got, want, rtol=5e-5)
+
+
 def test_canberra_zero_terms_follow_R(gpu, oracle_mod, rng):
     pts = rng.standard_normal((40, 12)).astype(np.float32)
     pts[rng.random(pts.shape) < 0.4] = 0.0
