@@ -75,6 +75,59 @@ __global__ void kendall_masks_kernel(const float *__restrict__ X, int64_t nvar, 
   }
 }
 
+// The same words, chunks and untied counts from a variable's observations
+// staged once in shared memory: one CTA per variable, for n up to
+// kKmSmemN (every word otherwise reads both of its observations from L1/L2).
+constexpr int kKmThreads = 256;
+constexpr int64_t kKmSmemN = 12288;  // 48 KB of observations
+__global__ void __launch_bounds__(kKmThreads)
+kendall_masks_smem_kernel(const float *__restrict__ X, int n, int d0, int drows, int Wn,
+                          uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
+  extern __shared__ float xs[];  // [n]
+  __shared__ unsigned long long part[kKmThreads / 32];
+  const int64_t v = blockIdx.x;
+  const float *x = X + v * int64_t(n);
+  for (int k = threadIdx.x; k < n; k += kKmThreads) xs[k] = x[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t per_var = int64_t(drows) * Wn;
+  const int64_t chunks = (per_var + 31) / 32;
+  unsigned long long untied_bits = 0;
+  for (int64_t c = warp; c < chunks; c += kKmThreads / 32) {
+    const int64_t base = c * 32;
+    const int cnt = per_var - base < 32 ? int(per_var - base) : 32;
+    int dr = int(base / Wn), w = int(base - int64_t(dr) * Wn);
+    uint2 mine = make_uint2(0u, 0u);
+    for (int e = 0; e < cnt; e++) {  // warp-uniform
+      const int d = d0 + dr + 1, i = 32 * w + lane;
+      bool untied = false, greater = false;
+      if (i < n && (2 * d < n || i < n / 2)) {
+        int j = i + d;
+        if (j >= n) j -= n;
+        const float xi = xs[i], xj = xs[j];
+        untied = xj != xi;
+        greater = xj > xi;
+      }
+      const unsigned u = __ballot_sync(0xffffffffu, untied);
+      const unsigned g = __ballot_sync(0xffffffffu, greater);
+      if (lane == e) mine = make_uint2(u, g);
+      untied_bits += __popc(u);
+      if (++w == Wn) {
+        w = 0;
+        dr++;
+      }
+    }
+    if (lane < cnt) M[v * per_var + base + lane] = mine;
+  }
+  if (lane == 0) part[warp] = untied_bits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int q = 0; q < kKmThreads / 32; q++) tot += part[q];
+    if (tot) atomicAdd(&T[v], tot);
+  }
+}
+
 // Counts of one 64 x 64 tile of variable pairs over words [kbeg, kend):
 // both[i][j] = popc(m), disc[i][j] = popc(m & (Gr ^ Gc)) with m = Ur & Uc,
 // for rows row0 + ty + 16 i of MR and columns col0 + tx + 16 j of MC.
@@ -194,6 +247,20 @@ int grid_cap(int64_t work, int threads) {
   return int(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
+// The masks of pair rows d0 + 1 .. d0 + dr of nv variables (and their untied
+// counts added to T): observations staged in shared memory when they fit.
+void launch_kendall_masks(const float *X, int64_t nv, int64_t n, int64_t d0, int64_t dr,
+                          int64_t Wn, uint2 *M, unsigned long long *T, cudaStream_t s) {
+  if (n <= kKmSmemN && nv <= 2147483647LL) {
+    kendall_masks_smem_kernel<<<unsigned(nv), kKmThreads, size_t(n) * sizeof(float), s>>>(
+        X, int(n), int(d0), int(dr), int(Wn), M, T);
+  } else {
+    kendall_masks_kernel<<<grid_cap(nv * cdiv(dr * Wn, 32) * 32, 256), 256, 0, s>>>(X, nv, n, d0,
+                                                                                  dr, Wn, M, T);
+  }
+  count_launch();
+}
+
 }  // namespace
 
 int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64_t n, int same,
@@ -225,13 +292,8 @@ int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64
       const int64_t dr = (Dr - d0 < rows_chunk) ? Dr - d0 : rows_chunk;
       const int64_t K = dr * Wn;
       uint2 *MXs = M, *MYs = same ? M : M + nx * K;
-      kendall_masks_kernel<<<grid_cap(nx * cdiv(K, 32) * 32, 256), 256, 0, s>>>(dX, nx, n, d0, dr,
-                                                                                Wn, MXs, TX);
-      count_launch();
-      if (!same)
-        kendall_masks_kernel<<<grid_cap(ny * cdiv(K, 32) * 32, 256), 256, 0, s>>>(dY, ny, n, d0,
-                                                                                  dr, Wn, MYs, TY);
-      if (!same) count_launch();
+      launch_kendall_masks(dX, nx, n, d0, dr, Wn, MXs, TX, s);
+      if (!same) launch_kendall_masks(dY, ny, n, d0, dr, Wn, MYs, TY, s);
       const int64_t gy = cdiv(ny, 64), gx = cdiv(nx, 64);
       if (gy > 65535 || gx > 2147483647LL) return fail(GT_EINVAL, "too many variables");
       const int64_t tiles = same ? gx * (gx + 1) / 2 : gx * gy;
