@@ -227,17 +227,37 @@ kendall_count_kernel(const uint2 *__restrict__ MR, int64_t nr, const uint2 *__re
   }
 }
 
-// out[y*nx + x] = S / (sqrt(Tx) * sqrt(Ty)), clamped; R's evaluation order.
+// sqrt(T_v) of every variable, the factors of tau-b's denominator.
+__global__ void kendall_roots_kernel(const unsigned long long *__restrict__ T, int64_t nvar,
+                                     double *__restrict__ root) {
+  const int64_t v = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (v < nvar) root[v] = __dsqrt_rn(double(T[v]));
+}
+
+// out[y*nx + x] = S / (sqrt(Tx) * sqrt(Ty)), clamped; R's evaluation order,
+// with the roots computed once per variable (the same operations as taub).
+// A block walks whole rows, so no index is divided.
 __global__ void kendall_finish_kernel(const unsigned long long *__restrict__ S,
-                                      const unsigned long long *__restrict__ TX,
-                                      const unsigned long long *__restrict__ TY, int64_t nx,
-                                      int64_t ny, int same, double *__restrict__ out) {
-  const int64_t total = nx * ny;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t y = i / nx, x = i - y * nx;
-    const double r = (same && x == y) ? 1.0 : taub((long long)S[i], TX[x], TY[y]);
-    out[i] = r;
+                                      const double *__restrict__ RX,
+                                      const double *__restrict__ RY, int64_t nx, int64_t ny,
+                                      int same, double *__restrict__ out) {
+  for (int64_t y = blockIdx.x; y < ny; y += gridDim.x) {
+    const double ry = RY[y];
+    for (int64_t x = threadIdx.x; x < nx; x += blockDim.x) {
+      const int64_t i = y * nx + x;
+      const double rx = RX[x];
+      double r;
+      if (same && x == y) {
+        r = 1.0;
+      } else if (rx == 0.0 || ry == 0.0) {
+        r = __longlong_as_double(0x7ff8000000000000LL);  // a constant variable
+      } else {
+        r = __ddiv_rn(double((long long)S[i]), __dmul_rn(rx, ry));
+        if (r > 1.0) r = 1.0;
+        if (r < -1.0) r = -1.0;
+      }
+      out[i] = r;
+    }
   }
 }
 
@@ -278,9 +298,10 @@ int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64
 
   void *pS = nullptr, *pT = nullptr, *pM = nullptr;
   GT_TRY(ws_get(WS_SCRATCH0, size_t(nx) * size_t(ny) * 8, &pS));
-  GT_TRY(ws_get(WS_SCRATCH1, size_t(nvar) * 8, &pT));
+  GT_TRY(ws_get(WS_SCRATCH1, size_t(nvar) * 16, &pT));  // untied counts, then their roots
   auto *S = static_cast<unsigned long long *>(pS);
   auto *T = static_cast<unsigned long long *>(pT);
+  auto *root = reinterpret_cast<double *>(T + nvar);
   GT_CUDA(cudaMemsetAsync(S, 0, size_t(nx) * size_t(ny) * 8, s));
   GT_CUDA(cudaMemsetAsync(T, 0, size_t(nvar) * 8, s));
   unsigned long long *TX = T, *TY = same ? T : T + nx;
@@ -311,8 +332,11 @@ int kendall_impl(const float *dX, int64_t nx, const float *dY, int64_t ny, int64
       GT_CUDA(cudaGetLastError());
     }
   }
-  kendall_finish_kernel<<<grid_cap(nx * ny, 256), 256, 0, s>>>(S, TX, TY, nx, ny, same, d_out);
-  count_launch();
+  kendall_roots_kernel<<<unsigned(cdiv(nvar, 256)), 256, 0, s>>>(T, nvar, root);
+  const double *RX = root, *RY = same ? root : root + nx;
+  const int64_t fgrid = ny < int64_t(sm_count()) * 16 ? ny : int64_t(sm_count()) * 16;
+  kendall_finish_kernel<<<unsigned(fgrid), 256, 0, s>>>(S, RX, RY, nx, ny, same, d_out);
+  count_launch(2);
   GT_CUDA(cudaGetLastError());
   return GT_OK;
 }
