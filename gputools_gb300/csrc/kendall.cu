@@ -361,12 +361,18 @@ __device__ __forceinline__ int64_t find_segment(const int64_t *__restrict__ pref
 }
 
 constexpr int kKbMaskThreads = 128;
+constexpr int kKbStage = 4096;  // observations staged in shared memory (16 KB)
 
+// One CTA per variable of the batch: warps take chunks of 32 consecutive
+// words (lane e keeps word e, one coalesced store per chunk), reading the
+// observations from shared memory when they fit; the untied count is the
+// CTA's sum.  The same words and counts either way.
 __global__ void __launch_bounds__(kKbMaskThreads)
 kendall_batch_masks_kernel(const KendallBatchProblem *__restrict__ P,
                            const int64_t *__restrict__ var_prefix, int64_t nprob,
                            uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
   __shared__ unsigned long long part[kKbMaskThreads / 32];
+  __shared__ float xs[kKbStage];
   const int64_t gv = blockIdx.x;
   const int64_t pi = find_segment(var_prefix, nprob, gv);
   const KendallBatchProblem pr = P[pi];
@@ -374,31 +380,47 @@ kendall_batch_masks_kernel(const KendallBatchProblem *__restrict__ P,
   const float *x = pr.X + v * pr.n;
   uint2 *mv = M + pr.mask_off + v * pr.K;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long cnt = 0;
-  for (int64_t t = warp; t < pr.K; t += kKbMaskThreads / 32) {
-    const int64_t dr = t / pr.Wn, w = t - dr * pr.Wn;
-    const int64_t d = dr + 1;
-    const int64_t i = 32 * w + lane;
-    const bool valid = i < pr.n && (2 * d < pr.n || i < pr.n / 2);
-    bool untied = false, greater = false;
-    if (valid) {
-      int64_t j = i + d;
-      if (j >= pr.n) j -= pr.n;
-      untied = x[j] != x[i];
-      greater = x[j] > x[i];
-    }
-    const unsigned u = __ballot_sync(0xffffffffu, untied);
-    const unsigned g = __ballot_sync(0xffffffffu, greater);
-    if (lane == 0) {
-      mv[t] = make_uint2(u, g);
-      cnt += __popc(u);
-    }
+  const bool staged = pr.n <= kKbStage;  // CTA-uniform
+  if (staged) {
+    for (int64_t k = threadIdx.x; k < pr.n; k += kKbMaskThreads) xs[k] = x[k];
+    __syncthreads();
   }
+  const int64_t n = pr.n, Wn = pr.Wn, K = pr.K;
+  unsigned long long cnt = 0;
+  auto words = [&](auto rd) {
+    for (int64_t base = 32 * int64_t(warp); base < K; base += 32 * (kKbMaskThreads / 32)) {
+      const int m = K - base < 32 ? int(K - base) : 32;
+      int64_t dr = base / Wn, w = base - dr * Wn;
+      uint2 mine = make_uint2(0u, 0u);
+      for (int e = 0; e < m; e++) {  // warp-uniform
+        const int64_t d = dr + 1, i = 32 * w + lane;
+        bool untied = false, greater = false;
+        if (i < n && (2 * d < n || i < n / 2)) {
+          int64_t j = i + d;
+          if (j >= n) j -= n;
+          const float xi = rd(i), xj = rd(j);
+          untied = xj != xi;
+          greater = xj > xi;
+        }
+        const unsigned u = __ballot_sync(0xffffffffu, untied);
+        const unsigned g = __ballot_sync(0xffffffffu, greater);
+        if (lane == e) mine = make_uint2(u, g);
+        cnt += __popc(u);
+        if (++w == Wn) {
+          w = 0;
+          dr++;
+        }
+      }
+      if (lane < m) mv[base + lane] = mine;
+    }
+  };
+  if (staged) words([&](int64_t k) { return xs[k]; });
+  else words([&](int64_t k) { return x[k]; });
   if (lane == 0) part[warp] = cnt;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long tot = 0;
-    for (int w = 0; w < kKbMaskThreads / 32; w++) tot += part[w];
+    for (int q = 0; q < kKbMaskThreads / 32; q++) tot += part[q];
     T[pr.var_off + v] = tot;
   }
 }
