@@ -190,7 +190,7 @@ int kendall_batch_plan(const gt_kendall_problem *probs, int64_t count, int flags
       (st = plan_upload(p, tile_prefix, &d_tp)) || (st = plan_upload(p, cta_tiles, &d_ct)) ||
       (st = plan_upload(p, cta_off, &d_co)) ||
       (st = plan_alloc(p, size_t(mask_words) * sizeof(uint2), &d_m)) ||
-      (st = plan_alloc(p, size_t(vars) * 8, &d_t))) {
+      (st = plan_alloc(p, size_t(vars) * 16, &d_t))) {  // untied counts, then their roots
     plan_free(p);
     return st;
   }

@@ -185,10 +185,11 @@ __device__ __forceinline__ void tile_counts(const uint2 *__restrict__ MR, int64_
 }
 
 // tau-b = S / (sqrt(Tx) * sqrt(Ty)) in IEEE double, R's evaluation order,
-// clamped to [-1, 1]; NaN when either variable is constant.
-__device__ __forceinline__ double taub(long long S, unsigned long long tx, unsigned long long ty) {
-  if (tx == 0 || ty == 0) return __longlong_as_double(0x7ff8000000000000LL);
-  double r = __ddiv_rn(double(S), __dmul_rn(__dsqrt_rn(double(tx)), __dsqrt_rn(double(ty))));
+// clamped to [-1, 1]; NaN when either variable is constant.  rx = sqrt(Tx)
+// and ry = sqrt(Ty) (__dsqrt_rn) are taken once per variable.
+__device__ __forceinline__ double taub(long long S, double rx, double ry) {
+  if (rx == 0.0 || ry == 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+  double r = __ddiv_rn(double(S), __dmul_rn(rx, ry));
   if (r > 1.0) r = 1.0;
   if (r < -1.0) r = -1.0;
   return r;
@@ -234,9 +235,7 @@ __global__ void kendall_roots_kernel(const unsigned long long *__restrict__ T, i
   if (v < nvar) root[v] = __dsqrt_rn(double(T[v]));
 }
 
-// out[y*nx + x] = S / (sqrt(Tx) * sqrt(Ty)), clamped; R's evaluation order,
-// with the roots computed once per variable (the same operations as taub).
-// A block walks whole rows, so no index is divided.
+// out[y*nx + x] = tau-b; a block walks whole rows, so no index is divided.
 __global__ void kendall_finish_kernel(const unsigned long long *__restrict__ S,
                                       const double *__restrict__ RX,
                                       const double *__restrict__ RY, int64_t nx, int64_t ny,
@@ -245,18 +244,7 @@ __global__ void kendall_finish_kernel(const unsigned long long *__restrict__ S,
     const double ry = RY[y];
     for (int64_t x = threadIdx.x; x < nx; x += blockDim.x) {
       const int64_t i = y * nx + x;
-      const double rx = RX[x];
-      double r;
-      if (same && x == y) {
-        r = 1.0;
-      } else if (rx == 0.0 || ry == 0.0) {
-        r = __longlong_as_double(0x7ff8000000000000LL);  // a constant variable
-      } else {
-        r = __ddiv_rn(double((long long)S[i]), __dmul_rn(rx, ry));
-        if (r > 1.0) r = 1.0;
-        if (r < -1.0) r = -1.0;
-      }
-      out[i] = r;
+      out[i] = (same && x == y) ? 1.0 : taub((long long)S[i], RX[x], ry);
     }
   }
 }
@@ -370,7 +358,8 @@ constexpr int kKbStage = 4096;  // observations staged in shared memory (16 KB)
 __global__ void __launch_bounds__(kKbMaskThreads)
 kendall_batch_masks_kernel(const KendallBatchProblem *__restrict__ P,
                            const int64_t *__restrict__ var_prefix, int64_t nprob,
-                           uint2 *__restrict__ M, unsigned long long *__restrict__ T) {
+                           uint2 *__restrict__ M, unsigned long long *__restrict__ T,
+                           double *__restrict__ root) {
   __shared__ unsigned long long part[kKbMaskThreads / 32];
   __shared__ float xs[kKbStage];
   const int64_t gv = blockIdx.x;
@@ -422,6 +411,7 @@ kendall_batch_masks_kernel(const KendallBatchProblem *__restrict__ P,
     unsigned long long tot = 0;
     for (int q = 0; q < kKbMaskThreads / 32; q++) tot += part[q];
     T[pr.var_off + v] = tot;
+    root[pr.var_off + v] = __dsqrt_rn(double(tot));
   }
 }
 
@@ -430,7 +420,7 @@ kendall_batch_count_kernel(const KendallBatchProblem *__restrict__ P,
                            const int64_t *__restrict__ tile_prefix, int64_t nprob,
                            const int64_t *__restrict__ cta_tiles,
                            const int64_t *__restrict__ cta_off, const uint2 *__restrict__ M,
-                           const unsigned long long *__restrict__ T) {
+                           const double *__restrict__ root) {
   __shared__ __align__(16) uint2 sR[64 * kKLd];
   __shared__ __align__(16) uint2 sC[64 * kKLd];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -457,7 +447,7 @@ kendall_batch_count_kernel(const KendallBatchProblem *__restrict__ P,
         if (c >= pr.p) continue;
         const long long sv = (long long)both[i][j] - 2LL * (long long)disc[i][j];
         const double tau =
-            (r == c) ? 1.0 : taub(sv, T[pr.var_off + c], T[pr.var_off + r]);
+            (r == c) ? 1.0 : taub(sv, root[pr.var_off + c], root[pr.var_off + r]);
         pr.out[r * pr.p + c] = tau;
         if (ti != tj) pr.out[c * pr.p + r] = tau;
       }
@@ -471,14 +461,16 @@ int kendall_batch_launch(const KendallBatchProblem *d_probs, const int64_t *d_va
                          int64_t nprob, int64_t total_vars, const int64_t *d_tile_prefix,
                          const int64_t *d_cta_tiles, const int64_t *d_cta_off, int64_t ncta,
                          uint2 *d_masks, unsigned long long *d_T, cudaStream_t s) {
+  // d_T holds the untied counts of all variables, then their square roots
+  double *root = reinterpret_cast<double *>(d_T + total_vars);
   if (total_vars > 0) {
     kendall_batch_masks_kernel<<<unsigned(total_vars), kKbMaskThreads, 0, s>>>(
-        d_probs, d_var_prefix, nprob, d_masks, d_T);
+        d_probs, d_var_prefix, nprob, d_masks, d_T, root);
     count_launch();
   }
   if (ncta > 0) {
     kendall_batch_count_kernel<<<unsigned(ncta), kKT, 0, s>>>(d_probs, d_tile_prefix, nprob,
-                                                             d_cta_tiles, d_cta_off, d_masks, d_T);
+                                                             d_cta_tiles, d_cta_off, d_masks, root);
     count_launch();
   }
   GT_CUDA(cudaGetLastError());

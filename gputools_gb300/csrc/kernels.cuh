@@ -103,7 +103,8 @@ int gemm_tc_store_scaled(const void *planesA, int64_t nA, const void *planesB, i
                          cudaStream_t s);
 
 // kendall.cu: batched problems.  Masks of problem i start at mask_off
-// (uint2 words, K = Dr * Wn per variable); untied counts at var_off.
+// (uint2 words, K = Dr * Wn per variable); untied counts at var_off.  d_T
+// holds 2 * total_vars 8-byte slots: the untied counts, then their roots.
 struct KendallBatchProblem {
   const float *X;  // variable-major p x n
   int64_t p, n, Dr, Wn, K;
